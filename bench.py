@@ -1,0 +1,333 @@
+"""Benchmark: direct-SCF Fock builds (J and K) per second on one GB300.
+
+Workload (N=1): the (H2O)8 water cluster in the 6-31G-shaped basis
+(104 Cartesian functions), Schwarz threshold 1e-12 -- a full J+K build per
+step, every unique shell quartet computed once.  Synthetic, seeded geometry
+(rchem_gb300.geometry.config("h2o8_631g")); the density is the core-guess
+density of that system.
+
+Timing: W warm-up builds, then K timed builds, each bracketed by CUDA events
+on the stream the kernels run on; a 256 MiB buffer is written between timed
+builds (outside the events) so L2 (~126 MB) holds nothing of the previous
+build.  ``value`` is FP64 Fock builds/s with D, J and K resident on the device;
+``e2e`` is the same through the C ABI with host arrays (H2D of D and D2H of J
+and K inside the timed region).  The mixed FP32/FP64 form is reported under
+``forms``.
+
+--impl reference: the reference's algorithm (src/basis.rs:383-428 loops over
+the THO integrals of libpyquante2/cints.c with its own Boys function), run by
+the CPU oracle with all host threads on a bounded sample of J/K elements and
+extrapolated to a whole build.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "h2o8_631g"
+WORKLOAD_DESC = "(H2O)8 water cluster, 6-31G-shaped basis (104 Cartesian functions), direct-SCF J+K Fock build"
+METRIC = "Fock builds/s"
+NOMINAL_FP64_TFLOPS = 1.25
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="J/K elements timed for the CPU baseline (0: auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def core_guess_density(rc, b, nocc):
+    S = rc.S(b)
+    H = rc.T(b) + rc.V(b)
+    w, U = np.linalg.eigh(S)
+    X = U @ np.diag(w ** -0.5) @ U.T
+    _, Cp = np.linalg.eigh(X.T @ H @ X)
+    C = X @ Cp
+    return C[:, :nocc] @ C[:, :nocc].T, H
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.lines:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True):
+    """The reference's JK_direct loops (2 THO ERIs per primitive quartet) on a
+    seeded sample of J/K elements, all host threads; returns builds/s
+    extrapolated to the n^2 elements of a build, threads and sample size."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config(workload)
+    ob = O.expand_basis(Z, R, rc.load_bse(bname))
+    port = O.port()
+    port.set_boys(not boys_shipped)
+    threads = port.num_threads()
+    n = ob.n
+    rng = np.random.default_rng(17)
+    X = rng.normal(size=(n, n))
+    D = X @ X.T / n
+    m = sample or max(threads, 2 * threads)
+    rates = []
+    for s in range(steps):
+        mus = rng.integers(0, n, m)
+        nus = rng.integers(0, n, m)
+        t0 = time.perf_counter()
+        O.JK_direct_elements(ob, D, mus, nus)
+        dt = time.perf_counter() - t0
+        rates.append(m / (dt * n * n))
+    port.set_boys(True)
+    return rates, threads, m, n
+
+
+def run_reference(a):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return 0
+    steps = max(1, a.steps)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build_port()
+    cpu_reference_rate(a.workload, a.cpu_sample, steps=max(1, min(a.warmup, 1)))  # warm-up
+    rates, threads, m, n = cpu_reference_rate(a.workload, a.cpu_sample, steps=steps)
+    value = float(np.mean(rates))
+    sample = ("%d J/K elements per step (seeded random (mu,nu)) of the %d x %d Fock matrix by the JK_direct loops "
+              "(src/basis.rs:392-425), THO ERIs with the Numerical-Recipes Boys function as shipped; "
+              "extrapolated to a full build" % (m, n, n))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": a.gpus,
+        "steps": steps, "warmup": a.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "description": WORKLOAD_DESC, "nbf": n},
+        "cpu_baseline": {"value": value, "unit": "builds/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        return run_reference(a)
+    import torch
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import rchem_gb300 as rc
+    from rchem_gb300 import _lib
+
+    bname, Z, R = rc.geometry.config(a.workload)
+    nocc = int(sum(Z)) // 2
+    b = rc.Basis(Z, R, bname)
+    n = b.nbf
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    Dh, H = core_guess_density(rc, b, nocc)
+    D = torch.from_numpy(Dh).cuda()
+    J = torch.empty_like(D)
+    K = torch.empty_like(D)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def run(tau32, steps, warmup):
+        for _ in range(warmup):
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+        evs = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    # ---- timed region: FP64 form -----------------------------------------
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        ms64 = run(0.0, a.steps, a.warmup)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    st64 = b.stats()
+    J64, K64 = J.cpu().numpy(), K.cpu().numpy()
+    ms = float(np.mean(ms64))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+
+    # ---- mixed form (same timing) -----------------------------------------
+    ms32 = run(1e-6, a.steps, a.warmup)
+    st32 = b.stats()
+    Jm, Km = J.cpu().numpy(), K.cpu().numpy()
+    dE = float(np.sum(Dh * (2 * (Jm - J64) - (Km - K64))))  # energy change at fixed D, sum (H+F) o D
+    ms_mixed = float(np.mean(ms32))
+
+    # ---- end to end through the C ABI with host arrays ---------------------
+    Jh, Kh = np.empty((n, n)), np.empty((n, n))
+    for _ in range(a.warmup):
+        rc.JK_direct(Jh, Kh, b, Dh)
+    te = []
+    for _ in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        rc.JK_direct(Jh, Kh, b, Dh)
+        te.append(time.perf_counter() - t1)
+    e2e = world / float(np.mean(te))
+
+    # ---- roofline: FP64 CUDA-core FMA pipe ---------------------------------
+    import ctypes
+
+    pk = ctypes.c_double(0.0)
+    peak64 = None
+    if _lib.lib().rchem_peak_fma(64, ctypes.byref(pk)) == 0:
+        peak64 = pk.value
+    pk32 = ctypes.c_double(0.0)
+    peak32 = pk32.value if _lib.lib().rchem_peak_fma(32, ctypes.byref(pk32)) == 0 else None
+    achieved = st64["flops_fp64"] / (ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(a.workload)
+        except (ValueError, OSError):
+            traffic = None
+
+    # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        rates, threads, m, _ = cpu_reference_rate(a.workload, a.cpu_sample, steps=1)
+        cpu = {"value": rates[0], "unit": "builds/s", "cores": threads, "kind": "port",
+               "sample": "%d J/K elements by the JK_direct loops (src/basis.rs:392-425) with THO ERIs and the "
+                         "shipped NR Boys function, extrapolated to the %d^2 elements of a build" % (m, n)}
+
+    clocks = clk.summary()
+    launches = st64["kernels"] + 1  # class kernels + symmetrise
+    line = {
+        "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "description": WORKLOAD_DESC, "basis": bname, "nbf": n,
+                   "schwarz_tau": 1e-12, "density": "core guess",
+                   "l2": "256 MiB buffer written between timed steps (outside the events)"},
+        "eris_per_s": st64["eris_fp64"] / (ms * 1e-3),
+        "forms": {
+            "fp64": {"builds_per_s": 1000.0 / ms, "ms": ms, "quartets": st64["quartets_fp64"],
+                     "eris": st64["eris_fp64"], "prim_quartets": st64["prim_quartets_fp64"]},
+            "mixed": {"builds_per_s": 1000.0 / ms_mixed, "ms": ms_mixed, "fp32_tau": 1e-6,
+                      "quartets_fp64": st32["quartets_fp64"], "quartets_fp32": st32["quartets_fp32"],
+                      "speedup_vs_fp64": ms / ms_mixed, "dE_fixed_density_Eh": dE,
+                      "max_abs_dJ": float(np.abs(Jm - J64).max()), "max_abs_dK": float(np.abs(Km - K64).max())},
+        },
+        "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": 2 * n * n * 8},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                     "frac": (achieved / peak64) if peak64 else None, "traffic": traffic,
+                     "peak_source": "measured in this run (rchem_peak_fma: DFMA chains on every SM)",
+                     "peak_fp32": peak32, "nominal_fp64": NOMINAL_FP64_TFLOPS,
+                     "flops_per_build": st64["flops_fp64"]},
+        "gpu_launches": launches * a.steps,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    b.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,114 @@
+/*
+ * rchem_gpu.h -- C ABI of librchem_gpu.so, the GB300 (sm_103a) implementation
+ * of rchem's restricted Hartree-Fock hot path: contracted-Gaussian ERIs, the
+ * Boys function, the one-electron integrals and the direct-SCF Fock build.
+ *
+ * Plain C types only.  Matrices are row-major FP64, n x n, in the reference's
+ * AO order (atoms in order, shells in basis-file order, each angular momentum
+ * of a shell in order, Cartesian components in src/shell.rs:1-12 order),
+ * coordinates in bohr.  Every array argument lives where the accompanying
+ * `where` / opts->where says (RCHEM_HOST or RCHEM_DEVICE).  Calls are
+ * asynchronous on the basis handle's stream and synchronise before returning.
+ *
+ * Errors: every entry returns an int status (RCHEM_OK = 0); rchem_last_error()
+ * gives the message of the calling thread's last failure.  Nothing exits the
+ * process or prints.  (The reference panics through unwrap()/assert!, e.g.
+ * src/basis.rs:89-105,163,191.)
+ *
+ * Threading: a handle is used by one host thread at a time.
+ */
+#ifndef RCHEM_GPU_H
+#define RCHEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    RCHEM_OK = 0,
+    RCHEM_ERR_INVALID = 1,     /* bad argument (null pointer, size, non-finite value) */
+    RCHEM_ERR_UNSUPPORTED = 2, /* l > 2 on a shell, too many primitives, ... */
+    RCHEM_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    RCHEM_ERR_NOMEM = 4        /* device or host allocation failed */
+};
+
+enum { RCHEM_HOST = 0, RCHEM_DEVICE = 1 };
+
+#define RCHEM_MAX_L 2      /* Cartesian s, p, d shells */
+#define RCHEM_MAX_NPRIM 16 /* primitives per shell */
+
+typedef struct rchem_basis_s *rchem_basis;
+
+/* Message of the calling thread's last error ("" if none). */
+const char *rchem_last_error(void);
+/* ABI version, currently 1. */
+int rchem_abi_version(void);
+
+/*
+ * Basis::new (src/basis.rs:181-211).  The reference fetches the basis through
+ * embedded Python (src/basis.rs:87-106); here the caller passes the shells,
+ * already expanded to pure angular momenta in AO order: a combined sp shell is
+ * its s shell followed by its p shell with the same exponents.
+ *   atomnos[natoms], coords[3*natoms] (bohr)
+ *   shell_atom[nshells], shell_l[nshells] (0..2), shell_nprim[nshells]
+ *   exps[], coefs[]: the shells' primitives back to back (raw basis-file
+ *   contraction coefficients; the primitive normalisation of basis.rs:140-149
+ *   is applied here, the contraction is not renormalised, as in the reference).
+ * All arrays are host arrays.  The handle owns its own CUDA stream.
+ */
+int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords, int nshells,
+                       const int *shell_atom, const int *shell_l, const int *shell_nprim, const double *exps,
+                       const double *coefs);
+int rchem_basis_destroy(rchem_basis b);
+/* Number of contracted Cartesian functions (the reference's cgtos.len()). */
+int rchem_basis_nbf(rchem_basis b);
+/* Use the caller's CUDA stream (a cudaStream_t) instead of the handle's own. */
+int rchem_basis_set_stream(rchem_basis b, void *stream);
+
+/* S, T and V matrices: basis::S / T / V, src/basis.rs:234,273,316.
+ * V = sum_C Z_C V_C over the handle's atoms. */
+int rchem_S(rchem_basis b, double *out, int where);
+int rchem_T(rchem_basis b, double *out, int where);
+int rchem_V(rchem_basis b, double *out, int where);
+/* Multipole-moment matrix <mu|(x-Cx)^ox (y-Cy)^oy (z-Cz)^oz|nu>, the integral of
+ * src/integrals/os86.rs:775-828, normalised like S.  center: 3 host doubles. */
+int rchem_moment(rchem_basis b, const double *center, int ox, int oy, int oz, double *out, int where);
+
+/* Fock-build options.  Zero-initialised options mean: FP64 everywhere,
+ * Schwarz threshold 1e-12, host arrays. */
+typedef struct {
+    double schwarz_tau; /* drop quartets with Q_ab Q_cd < tau (0 => 1e-12; <0 => no screening) */
+    double fp32_tau;    /* quartets with Q_ab Q_cd < fp32_tau in FP32, FP64 accumulation (0 => FP64 only) */
+    int where;          /* RCHEM_HOST or RCHEM_DEVICE for D, J, K */
+    int reserved;
+} rchem_jk_opts;
+
+/* Work done by the last Fock build of a handle. */
+typedef struct {
+    long long quartets_fp64, quartets_fp32; /* contracted shell quartets computed */
+    long long prim_quartets_fp64, prim_quartets_fp32;
+    long long eris_fp64, eris_fp32;         /* contracted Cartesian integrals computed (unique, 8-fold) */
+    double flops_fp64, flops_fp32;          /* algorithmic FLOPs (generated op counts) */
+    long long warp_tasks;                   /* warps launched */
+    int kernels;                            /* class kernels launched */
+    int reserved;
+} rchem_jk_stats;
+
+/*
+ * JK_direct (src/basis.rs:383-428): J_mn = sum_ls (mn|ls) D_ls,
+ * K_mn = sum_ls (ml|ns) D_ls, for a symmetric density D.  J and K are
+ * overwritten (the reference zero-fills them first, basis.rs:389-390).
+ * Each unique quartet is computed once (8-fold symmetry), Schwarz-screened.
+ */
+int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
+int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
+
+/* build_I (src/basis.rs:430-460): the dense n^4 ERI tensor I[m][n][l][s]. */
+int rchem_build_I(rchem_basis b, double *I, int where);
+/* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */
+int rchem_jk_inmem(int n, const double *I, const double *D, double *J, double *K, int where);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RCHEM_GPU_H */

@@ -1,0 +1,17 @@
+"""rchem_gb300 -- GB300-native (sm_103a) RHF hot path of berquist/rchem.
+
+The compute lives in librchem_gpu.so (hand-written CUDA, C ABI in include/);
+this package is the host-side mirror of the reference's basis API
+(src/basis.rs) plus input readers.  Importing it loads the shared library
+lazily; every compute call fails loudly if the library is not built.
+"""
+from . import geometry
+from ._lib import RchemError
+from .basis import JK_direct, JK_inmem, S, T, V, Basis, build_I, moment
+from .bse import available_basis_sets, expand_shells, load_bse, read_xyz
+from . import cints
+
+__all__ = [
+    "Basis", "S", "T", "V", "JK_direct", "build_I", "JK_inmem", "moment", "RchemError", "load_bse",
+    "expand_shells", "read_xyz", "available_basis_sets", "geometry", "cints",
+]

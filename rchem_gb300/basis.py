@@ -1,0 +1,188 @@
+"""Host-side mirror of the reference's basis API (src/basis.rs), GPU-backed.
+
+Same names and meanings as the reference:
+
+=====================================  =========================================
+reference (src/basis.rs)               here
+=====================================  =========================================
+``Basis::new(atomnos, coords, name)``  ``Basis(atomnos, coords, name)``  :181
+``S(&basis)``                          ``S(basis)``                      :234
+``T(&basis)``                          ``T(basis)``                      :273
+``V(&basis, coords, atomnos)``         ``V(basis, coords, atomnos)``     :316
+``JK_direct(&mut J, &mut K, &b, &D)``  ``JK_direct(J, K, basis, D)``     :383
+``build_I(&basis)``                    ``build_I(basis)``                :430
+``JK_inmem(&I, &D)``                   ``JK_inmem(I, D)``                :462
+=====================================  =========================================
+
+Arrays may be numpy arrays (host) or CUDA torch tensors (device); outputs
+follow the input kind.  All work runs through librchem_gpu.so: there is no
+CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .bse import expand_shells, load_bse
+
+
+def _is_cuda(x) -> bool:
+    return hasattr(x, "is_cuda") and bool(x.is_cuda)
+
+
+def _ptr(x):
+    if _is_cuda(x):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class Basis:
+    """A basis on the GPU: shells, shell pairs, Schwarz bounds, Boys tables."""
+
+    def __init__(self, atomnos, coords, basis_set_name="sto-3g-fit"):
+        self.atomnos = np.ascontiguousarray(atomnos, dtype=np.int32).reshape(-1)
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        self.name = basis_set_name if isinstance(basis_set_name, str) else "custom"
+        self.shells = expand_shells(self.atomnos, load_bse(basis_set_name))
+        h = C.c_void_p()
+        L = _lib.lib()
+        sh = self.shells
+        _lib.check(L.rchem_basis_create(C.byref(h), len(self.atomnos), self.atomnos.ctypes.data,
+                                        self.coords.ctypes.data, len(sh.l), sh.atom.ctypes.data, sh.l.ctypes.data,
+                                        sh.nprim.ctypes.data, sh.exps.ctypes.data, sh.coefs.ctypes.data))
+        self._h = h
+        self.nbf = int(L.rchem_basis_nbf(h))
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("basis is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _lib.lib().rchem_basis_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr: int):
+        """Run this basis' work on a caller-owned CUDA stream (e.g. torch's)."""
+        _lib.check(_lib.lib().rchem_basis_set_stream(self.handle, C.c_void_p(stream_ptr)))
+
+    def stats(self) -> dict:
+        st = _lib.JKStats()
+        _lib.check(_lib.lib().rchem_jk_stats_get(self.handle, C.byref(st)))
+        return st.as_dict()
+
+    def _new(self, like=None, shape=None):
+        shape = shape or (self.nbf, self.nbf)
+        if like is not None and _is_cuda(like):
+            import torch
+
+            return torch.empty(shape, dtype=torch.float64, device=like.device)
+        return np.empty(shape, dtype=np.float64)
+
+
+def _onee(fn, basis, device=False):
+    out = basis._new()
+    if device:
+        import torch
+
+        out = torch.empty((basis.nbf, basis.nbf), dtype=torch.float64, device="cuda")
+    _lib.check(fn(basis.handle, C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))
+    return out
+
+
+def S(basis: Basis, device=False):
+    return _onee(_lib.lib().rchem_S, basis, device)
+
+
+def T(basis: Basis, device=False):
+    return _onee(_lib.lib().rchem_T, basis, device)
+
+
+def V(basis: Basis, atomcoords=None, atomnos=None, device=False):
+    """V = sum_C Z_C V_C over the basis' own atoms (the reference passes the
+    same coordinates and atomic numbers it built the basis from)."""
+    if atomcoords is not None and not np.allclose(np.asarray(atomcoords).reshape(-1, 3), basis.coords):
+        raise ValueError("V over atoms other than the basis' own is not supported")
+    return _onee(_lib.lib().rchem_V, basis, device)
+
+
+def moment(basis: Basis, center, order, device=False):
+    """<mu|(x-Cx)^ox (y-Cy)^oy (z-Cz)^oz|nu> (src/integrals/os86.rs:775-828)."""
+    c = np.ascontiguousarray(center, dtype=np.float64)
+    out = basis._new()
+    if device:
+        import torch
+
+        out = torch.empty((basis.nbf, basis.nbf), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().rchem_moment(basis.handle, c.ctypes.data, int(order[0]), int(order[1]), int(order[2]),
+                                       C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))
+    return out
+
+
+def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0):
+    """Fill J and K (in place, like the reference) from the density D."""
+    dev = _is_cuda(D)
+    if dev != _is_cuda(J) or dev != _is_cuda(K):
+        raise ValueError("D, J and K must all be host arrays or all CUDA tensors")
+    if not dev:
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        for X in (J, K):
+            if not (isinstance(X, np.ndarray) and X.dtype == np.float64 and X.flags.c_contiguous):
+                raise ValueError("J and K must be C-contiguous float64 arrays")
+    else:
+        D = D.contiguous()
+    n = basis.nbf
+    for X in (D, J, K):
+        if tuple(X.shape) != (n, n):
+            raise ValueError("expected %dx%d matrices" % (n, n))
+    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
+                    where=_lib.DEVICE if dev else _lib.HOST)
+    _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
+                                          C.c_void_p(_ptr(K)), C.byref(o)))
+
+
+def build_I(basis: Basis, device=False):
+    n = basis.nbf
+    if device:
+        import torch
+
+        out = torch.empty((n, n, n, n), dtype=torch.float64, device="cuda")
+    else:
+        out = np.empty((n, n, n, n), dtype=np.float64)
+    _lib.check(_lib.lib().rchem_build_I(basis.handle, C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))
+    return out
+
+
+def JK_inmem(I, D):
+    n = D.shape[0]
+    dev = _is_cuda(D)
+    if dev:
+        import torch
+
+        J = torch.empty((n, n), dtype=torch.float64, device=D.device)
+        K = torch.empty_like(J)
+        I, D = I.contiguous(), D.contiguous()
+    else:
+        I = np.ascontiguousarray(I, dtype=np.float64)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        J = np.empty((n, n))
+        K = np.empty((n, n))
+    _lib.check(_lib.lib().rchem_jk_inmem(n, C.c_void_p(_ptr(I)), C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
+                                         C.c_void_p(_ptr(K)), _lib.DEVICE if dev else _lib.HOST))
+    return J, K

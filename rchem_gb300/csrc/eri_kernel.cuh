@@ -1,0 +1,292 @@
+// eri_kernel.cuh -- the HGP ERI class kernel and its fused epilogues.
+//
+// Work unit: one warp = one bra shell pair against up to 32 ket shell pairs
+// taken from one pair group (same l_C, l_D and primitive-pair count, sorted by
+// Schwarz bound), one ket pair per lane.  Every lane therefore runs the same
+// primitive loop trip counts.  Per primitive quartet: Boys function, the
+// generated Obara--Saika VRR into the [e0|f0] contraction accumulators (held in
+// registers); per contracted quartet: the generated HRR, then
+//   EPI_JK    -- the 8-fold-symmetric J/K scatter (contracted with D in
+//                registers, bra J block reduced across the warp with shuffles,
+//                everything else added with FP64 atomics into J-hat / K-hat),
+//   EPI_STORE -- the dense ERI tensor (all 8 index permutations),
+//   EPI_DIAG  -- the Schwarz diagonal max |(ab|ab)| (bra = ket = lane's pair).
+//
+// The reference computes the same quantities with no symmetry and no
+// screening, one primitive ERI per call (src/basis.rs:383-428,
+// libpyquante2/cints.c:72-115).
+#pragma once
+#include <cuda_runtime.h>
+#include "rchem_types.h"
+#include "boys.cuh"
+
+template <int LA, int LB, int LC, int LD> struct EriClass;
+
+enum { EPI_JK = 0, EPI_STORE = 1, EPI_DIAG = 2 };
+
+template <typename R> struct PrimLoad;
+template <> struct PrimLoad<double> {
+    static __device__ __forceinline__ void get(const EriArgs &a, int idx, double &p, double &ohp, double *P,
+                                               double *PA, double &K) {
+        const double2 *q = reinterpret_cast<const double2 *>(a.prims + idx);
+        const double2 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2), v3 = __ldg(q + 3), v4 = __ldg(q + 4);
+        p = v0.x; ohp = v0.y; P[0] = v1.x; P[1] = v1.y; P[2] = v2.x; PA[0] = v2.y; PA[1] = v3.x; PA[2] = v3.y; K = v4.x;
+    }
+};
+template <> struct PrimLoad<float> {
+    static __device__ __forceinline__ void get(const EriArgs &a, int idx, float &p, float &ohp, float *P, float *PA,
+                                               float &K) {
+        const float4 *q = reinterpret_cast<const float4 *>(a.prims32 + idx);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2);
+        p = v0.x; ohp = v0.y; P[0] = v0.z; P[1] = v0.w; P[2] = v1.x; PA[0] = v1.y; PA[1] = v1.z; PA[2] = v1.w; K = v2.x;
+    }
+};
+
+template <typename R> struct Tabs;
+template <> struct Tabs<double> {
+    static __device__ __forceinline__ const double *boys(const EriArgs &a) { return a.boys64; }
+    static __device__ __forceinline__ const double *ex(const EriArgs &a) { return a.exp64; }
+    static __device__ __forceinline__ double dens(const EriArgs &a, int i) { return __ldg(a.D + i); }
+    static __device__ __forceinline__ void ab(const ShellPair &s, double *v) { v[0] = s.AB[0]; v[1] = s.AB[1]; v[2] = s.AB[2]; }
+};
+template <> struct Tabs<float> {
+    static __device__ __forceinline__ const float *boys(const EriArgs &a) { return a.boys32; }
+    static __device__ __forceinline__ const float *ex(const EriArgs &a) { return a.exp32; }
+    static __device__ __forceinline__ float dens(const EriArgs &a, int i) { return __ldg(a.D32 + i); }
+    static __device__ __forceinline__ void ab(const ShellPair &s, float *v) { v[0] = s.AB32[0]; v[1] = s.AB32[1]; v[2] = s.AB32[2]; }
+};
+
+template <typename R> __device__ __forceinline__ R warp_sum(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int LA, int LB, int LC, int LD, typename R, int EPI>
+__global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
+    using C = EriClass<LA, LB, LC, LD>;
+    constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, L = C::L;
+    const int lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (w >= a.ntasks) return;  // warp-uniform
+    const EriTask t = a.tasks[w];
+    const bool active = lane < t.nket;
+    const int kidx = t.ket0 + (active ? lane : 0);
+    const int bidx = (EPI == EPI_DIAG) ? kidx : t.bra;
+    const ShellPair bp = a.pairs[bidx];
+    const ShellPair kp = a.pairs[kidx];
+
+    R acc[C::NE * C::NF];
+#pragma unroll
+    for (int i = 0; i < C::NE * C::NF; ++i) acc[i] = R(0);
+
+    const R *btab = Tabs<R>::boys(a);
+    const R *etab = Tabs<R>::ex(a);
+    for (int ia = 0; ia < bp.npp; ++ia) {
+        R p, ohp, P[3], PA[3], Kab;
+        PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, P, PA, Kab);
+        for (int ic = 0; ic < kp.npp; ++ic) {
+            R q, ohq, Q[3], QC[3], Kcd;
+            PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Q, QC, Kcd);
+            const R pq = p + q;
+            const R rs = rchem_rsqrt(pq);
+            const R ipq = rs * rs;
+            const R PQx = P[0] - Q[0], PQy = P[1] - Q[1], PQz = P[2] - Q[2];
+            const R qi = q * ipq, pi = p * ipq;
+            const R T = p * qi * (PQx * PQx + PQy * PQy + PQz * PQz);
+            const R pref = Kab * Kcd * rs;
+            R F[L + 1];
+            boys_eval<L, C::BOYS_DIRECT, R>(T, pref, btab, etab, F);
+            C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi * PQx, -qi * PQy, -qi * PQz, QC[0], QC[1], QC[2],
+                               pi * PQx, pi * PQy, pi * PQz, ohp, ohq, R(0.5) * ipq, qi, pi);
+        }
+    }
+
+    R AB[3], CD[3];
+    Tabs<R>::ab(bp, AB);
+    Tabs<R>::ab(kp, CD);
+    R out[NA * NB * NC * ND];
+    C::template hrr<R>(acc, out, AB[0], AB[1], AB[2], CD[0], CD[1], CD[2]);
+
+#define IDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
+    if constexpr (EPI == EPI_DIAG) {
+        if constexpr (LA == LC && LB == LD) {
+            if (active) {
+                double m = 0.0;
+#pragma unroll
+                for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                    for (int ib = 0; ib < NB; ++ib) m = fmax(m, fabs((double)out[IDX(ia, ib, ia, ib)]));
+                a.J[kidx] = sqrt(m);
+            }
+        }
+        return;
+    }
+    const int n = a.nbf;
+    const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
+    if constexpr (EPI == EPI_STORE) {
+        if (active) {
+            const size_t N1 = (size_t)n, N2 = N1 * n, N3 = N2 * n;
+#pragma unroll
+            for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                    for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+                        for (int id = 0; id < ND; ++id) {
+                            const double v = (double)out[IDX(ia, ib, ic, id)];
+                            const size_t i = m0 + ia, j = n0 + ib, k = l0 + ic, l = s0 + id;
+                            a.eri[i * N3 + j * N2 + k * N1 + l] = v;
+                            a.eri[j * N3 + i * N2 + k * N1 + l] = v;
+                            a.eri[i * N3 + j * N2 + l * N1 + k] = v;
+                            a.eri[j * N3 + i * N2 + l * N1 + k] = v;
+                            a.eri[k * N3 + l * N2 + i * N1 + j] = v;
+                            a.eri[l * N3 + k * N2 + i * N1 + j] = v;
+                            a.eri[k * N3 + l * N2 + j * N1 + i] = v;
+                            a.eri[l * N3 + k * N2 + j * N1 + i] = v;
+                        }
+        }
+        return;
+    }
+
+    // ---- EPI_JK: degeneracy-weighted 8-fold scatter -------------------------
+    R deg = active ? R(1) : R(0);
+    if (bp.diag) deg *= R(0.5);
+    if (kp.diag) deg *= R(0.5);
+    if (bidx == kidx) deg *= R(0.5);
+
+    // J-hat bra block: sum over the ket of 2 (ab|cd) D_cd, reduced over the warp
+    {
+        R Dcd[NC * ND];
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = Tabs<R>::dens(a, (l0 + ic) * n + s0 + id);
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib) {
+                R s = R(0);
+#pragma unroll
+                for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+                    for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dcd[ic * ND + id];
+                s = warp_sum<R>(s * deg);
+                if (lane == 0) atomicAdd(a.J + (m0 + ia) * n + n0 + ib, 2.0 * (double)s);
+            }
+    }
+    if (!active) return;
+    // J-hat ket block: 2 (ab|cd) D_ab
+    {
+        R Dab[NA * NB];
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = Tabs<R>::dens(a, (m0 + ia) * n + n0 + ib);
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                R s = R(0);
+#pragma unroll
+                for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                    for (int ib = 0; ib < NB; ++ib) s += out[IDX(ia, ib, ic, id)] * Dab[ia * NB + ib];
+                atomicAdd(a.J + (l0 + ic) * n + s0 + id, 2.0 * (double)(s * deg));
+            }
+    }
+    // K-hat[a][c] += (ab|cd) D_bd
+    {
+        R Dbd[NB * ND];
+#pragma unroll
+        for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = Tabs<R>::dens(a, (n0 + ib) * n + s0 + id);
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) {
+                R s = R(0);
+#pragma unroll
+                for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                    for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dbd[ib * ND + id];
+                atomicAdd(a.K + (m0 + ia) * n + l0 + ic, (double)(s * deg));
+            }
+    }
+    // K-hat[b][c] += (ab|cd) D_ad
+    {
+        R Dad[NA * ND];
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = Tabs<R>::dens(a, (m0 + ia) * n + s0 + id);
+#pragma unroll
+        for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) {
+                R s = R(0);
+#pragma unroll
+                for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                    for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dad[ia * ND + id];
+                atomicAdd(a.K + (n0 + ib) * n + l0 + ic, (double)(s * deg));
+            }
+    }
+    // K-hat[a][d] += (ab|cd) D_bc
+    {
+        R Dbc[NB * NC];
+#pragma unroll
+        for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = Tabs<R>::dens(a, (n0 + ib) * n + l0 + ic);
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                R s = R(0);
+#pragma unroll
+                for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                    for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dbc[ib * NC + ic];
+                atomicAdd(a.K + (m0 + ia) * n + s0 + id, (double)(s * deg));
+            }
+    }
+    // K-hat[b][d] += (ab|cd) D_ac
+    {
+        R Dac[NA * NC];
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = Tabs<R>::dens(a, (m0 + ia) * n + l0 + ic);
+#pragma unroll
+        for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+                R s = R(0);
+#pragma unroll
+                for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                    for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dac[ia * NC + ic];
+                atomicAdd(a.K + (n0 + ib) * n + s0 + id, (double)(s * deg));
+            }
+    }
+#undef IDX
+}
+
+template <int LA, int LB, int LC, int LD>
+void launch_eri_class(const EriArgs &a, int fp32, int epi, cudaStream_t s) {
+    if (a.ntasks <= 0) return;
+    const int threads = 128;
+    const long long nthreads = (long long)a.ntasks * 32;
+    const int blocks = (int)((nthreads + threads - 1) / threads);
+    if (epi == EPI_JK) {
+        if (fp32) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
+        else eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+    } else if (epi == EPI_STORE) {
+        eri_class_kernel<LA, LB, LC, LD, double, EPI_STORE><<<blocks, threads, 0, s>>>(a);
+    } else if constexpr (LA == LC && LB == LD) {
+        eri_class_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<blocks, threads, 0, s>>>(a);
+    }
+}

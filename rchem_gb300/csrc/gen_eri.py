@@ -1,0 +1,365 @@
+"""Code generator for the Head-Gordon--Pople ERI class kernels.
+
+For every angular-momentum class (la lb | lc ld) with la >= lb, lc >= ld and
+l <= 2 per shell it writes straight-line code, templated on the real type R
+(double for the FP64 form, float for the FP32 part of the mixed form):
+
+* ``vrr_<cls>(...)``  -- Obara--Saika vertical recursion for one primitive
+  quartet, from the scaled Boys values F[m] to [e0|f0]^(0) for every Cartesian
+  e with la <= |e| <= la+lb and f with lc <= |f| <= lc+ld, added into the
+  contraction accumulators ``acc``;
+* ``hrr_<cls>(...)``  -- the horizontal recursion on the contracted
+  accumulators, (a,b+1_i| = (a+1_i,b| + AB_i (a,b| on the bra and the same
+  with CD on the ket, producing the (ab|cd) block in the reference's Cartesian
+  order (src/shell.rs:1-12), each function scaled by its component
+  normalisation factor (src/basis.rs:140-149 relative to the (l,0,0)
+  component).
+
+It also writes the per-class operation counts (FMA = 2 FLOP) that the
+benchmark uses as the algorithmic FLOPs of a launch.  The algorithm follows
+Head-Gordon & Pople (1988) and Obara & Saika (1986); the reference's own
+implementation of the same recursions is libpyquante2/chgp.c:138-219,412-586.
+
+Usage: python gen_eri.py OUTDIR
+"""
+from __future__ import annotations
+
+import itertools
+import os
+import sys
+
+LMAX = 2  # per shell (s, p, d)
+
+
+def ijk_list(l):
+    out = []
+    for a in range(1, l + 2):
+        for b in range(1, a + 1):
+            out.append((l + 1 - a, a - b, b - 1))
+    return out
+
+
+def ncart(l):
+    return (l + 1) * (l + 2) // 2
+
+
+def comps_range(lo, hi):
+    out = []
+    for l in range(lo, hi + 1):
+        out.extend(ijk_list(l))
+    return out
+
+
+def fact2(n):
+    r = 1
+    while n > 1:
+        r *= n
+        n -= 2
+    return r
+
+
+def comp_norm(c):
+    """N(alpha,l,m,n) / N(alpha,L,0,0)."""
+    L = sum(c)
+    return ((fact2(2 * L - 1)) / (fact2(2 * c[0] - 1) * fact2(2 * c[1] - 1) * fact2(2 * c[2] - 1))) ** 0.5
+
+
+def sub(v, i, k=1):
+    w = list(v)
+    w[i] -= k
+    return tuple(w)
+
+
+def add(v, i, k=1):
+    w = list(v)
+    w[i] += k
+    return tuple(w)
+
+
+XYZ = "xyz"
+
+
+def classes():
+    pairs = [(a, b) for a in range(LMAX + 1) for b in range(a + 1)]  # ss ps pp ds dp dd
+    pairs.sort(key=lambda ab: (ab[0] + ab[1], ab[0]))
+    out = []
+    for i, bra in enumerate(pairs):
+        for ket in pairs[: i + 1]:
+            out.append(bra + ket)
+    return pairs, out
+
+
+class Emitter:
+    def __init__(self):
+        self.lines = []
+        self.names = {}
+        self.nfma = 0  # fused multiply-adds
+        self.nmul = 0  # plain multiplies / adds
+
+    def emit(self, s):
+        self.lines.append("    " + s)
+
+
+def gen_vrr(la, lb, lc, ld, choose):
+    """Returns (code lines, list of (target e, f) in accumulator order, op counts)."""
+    E, F = la + lb, lc + ld
+    L = E + F
+    em = Emitter()
+    memo = {}
+
+    def name(e, f, m):
+        return "v_%d%d%d_%d%d%d_%d" % (e + f + (m,))
+
+    def node(e, f, m):
+        key = (e, f, m)
+        if key in memo:
+            return memo[key]
+        if sum(e) == 0 and sum(f) == 0:
+            memo[key] = "F[%d]" % m
+            return memo[key]
+        terms = []
+        if sum(f) == 0:
+            i = choose(e)
+            e1 = sub(e, i)
+            a = node(e1, f, m)
+            b = node(e1, f, m + 1)
+            expr = "PA%s*%s + WP%s*%s" % (XYZ[i], a, XYZ[i], b)
+            nf, nm = 1, 1
+            if e1[i] > 0:
+                e2 = sub(e1, i)
+                c = node(e2, f, m)
+                d = node(e2, f, m + 1)
+                expr = "%s + R(%d)*ohp*(%s - rho_p*%s)" % (expr, e1[i], c, d)
+                nf += 2
+                nm += 0 if e1[i] == 1 else 0
+        else:
+            i = choose(f)
+            f1 = sub(f, i)
+            a = node(e, f1, m)
+            b = node(e, f1, m + 1)
+            expr = "QC%s*%s + WQ%s*%s" % (XYZ[i], a, XYZ[i], b)
+            nf, nm = 1, 1
+            if f1[i] > 0:
+                f2 = sub(f1, i)
+                c = node(e, f2, m)
+                d = node(e, f2, m + 1)
+                expr = "%s + R(%d)*ohq*(%s - rho_q*%s)" % (expr, f1[i], c, d)
+                nf += 2
+            if e[i] > 0:
+                g = node(sub(e, i), f1, m + 1)
+                expr = "%s + R(%d)*ohpq*%s" % (expr, e[i], g)
+                nf += 1
+        nm_ = name(e, f, m)
+        em.emit("const R %s = %s;" % (nm_, expr))
+        em.nfma += nf
+        em.nmul += nm
+        memo[key] = nm_
+        return nm_
+
+    targets = [(e, f) for e in comps_range(la, E) for f in comps_range(lc, F)]
+    for k, (e, f) in enumerate(targets):
+        v = node(e, f, 0)
+        em.emit("acc[%d] += %s;" % (k, v))
+        em.nmul += 1
+    return em, targets, L
+
+
+def gen_hrr(la, lb, lc, ld, targets, choose):
+    """HRR on contracted accumulators -> out[] in (a,b,c,d) Cartesian order."""
+    em = Emitter()
+    E, F = la + lb, lc + ld
+    eidx = {e: k for k, e in enumerate(comps_range(la, E))}
+    fidx = {f: k for k, f in enumerate(comps_range(lc, F))}
+    nf = len(fidx)
+    # bra: (a,b|f) for every f in the ket accumulator range
+    bra_memo = {}
+
+    def bra(a, b, f):
+        key = (a, b, f)
+        if key in bra_memo:
+            return bra_memo[key]
+        if sum(b) == 0:
+            s = "acc[%d]" % (eidx[a] * nf + fidx[f])
+            bra_memo[key] = s
+            return s
+        i = choose(b)
+        b1 = sub(b, i)
+        x = bra(add(a, i), b1, f)
+        y = bra(a, b1, f)
+        nm = "hb_%d%d%d_%d%d%d_%d%d%d" % (a + b + f)
+        em.emit("const R %s = %s + AB%s*%s;" % (nm, x, XYZ[i], y))
+        em.nfma += 1
+        bra_memo[key] = nm
+        return nm
+
+    ket_memo = {}
+
+    def ket(a, b, c, d):
+        key = (a, b, c, d)
+        if key in ket_memo:
+            return ket_memo[key]
+        if sum(d) == 0:
+            s = bra(a, b, c)
+            ket_memo[key] = s
+            return s
+        i = choose(d)
+        d1 = sub(d, i)
+        x = ket(a, b, add(c, i), d1)
+        y = ket(a, b, c, d1)
+        nm = "hk_%d%d%d_%d%d%d_%d%d%d_%d%d%d" % (a + b + c + d)
+        em.emit("const R %s = %s + CD%s*%s;" % (nm, x, XYZ[i], y))
+        em.nfma += 1
+        ket_memo[key] = nm
+        return nm
+
+    k = 0
+    for a in ijk_list(la):
+        for b in ijk_list(lb):
+            for c in ijk_list(lc):
+                for d in ijk_list(ld):
+                    v = ket(a, b, c, d)
+                    s = comp_norm(a) * comp_norm(b) * comp_norm(c) * comp_norm(d)
+                    if abs(s - 1.0) < 1e-15:
+                        em.emit("out[%d] = %s;" % (k, v))
+                    else:
+                        em.emit("out[%d] = R(%.17g)*%s;" % (k, s, v))
+                        em.nmul += 1
+                    k += 1
+    return em
+
+
+def choose_first(v):
+    for i in range(3):
+        if v[i] > 0:
+            return i
+    raise ValueError
+
+
+def choose_last(v):
+    for i in (2, 1, 0):
+        if v[i] > 0:
+            return i
+    raise ValueError
+
+
+def choose_max(v):
+    best = max(v)
+    for i in range(3):
+        if v[i] == best:
+            return i
+    raise ValueError
+
+
+CHOICES = {"first": choose_first, "last": choose_last, "max": choose_max}
+
+
+def best_vrr(la, lb, lc, ld):
+    best = None
+    for nm, ch in CHOICES.items():
+        em, targets, L = gen_vrr(la, lb, lc, ld, ch)
+        cost = em.nfma + em.nmul
+        if best is None or cost < best[0]:
+            best = (cost, nm, em, targets, L)
+    return best
+
+
+def best_hrr(la, lb, lc, ld, targets):
+    best = None
+    for nm, ch in CHOICES.items():
+        em = gen_hrr(la, lb, lc, ld, targets, ch)
+        cost = em.nfma + em.nmul
+        if best is None or cost < best[0]:
+            best = (cost, nm, em)
+    return best
+
+
+# Boys-function cost model of boys.cuh (must stay in sync with it):
+#   Taylor about the nearest grid point with NTAY terms for each m (direct)
+#   or for F_L and exp(-T) followed by the downward recursion.
+NTAY64 = 8
+NTAY32 = 4
+
+
+def boys_ops(L, ntay=NTAY64):
+    direct = (ntay - 1) * (L + 1) + (ntay - 1)  # Horner per m + the (-d/k) multipliers
+    downward = (ntay - 1) + 2 * (ntay - 1) + 2 * L + 2
+    return min(direct, downward), (direct <= downward)
+
+
+def main(outdir):
+    os.makedirs(outdir, exist_ok=True)
+    pairs, cls = classes()
+    table = []
+    for (la, lb, lc, ld) in cls:
+        tag = "%d%d%d%d" % (la, lb, lc, ld)
+        cost_v, chv, vem, targets, L = best_vrr(la, lb, lc, ld)
+        cost_h, chh, hem = best_hrr(la, lb, lc, ld, targets)
+        NE = len(comps_range(la, la + lb))
+        NF = len(comps_range(lc, lc + ld))
+        NA, NB, NC, ND = ncart(la), ncart(lb), ncart(lc), ncart(ld)
+        bops, direct = boys_ops(L)
+        # per primitive quartet: set-up (pq, rsqrt via library, rho, PQ, T, pref,
+        # WP/WQ, rho_p, rho_q, ohpq): counted as 24 FP64 ops + rsqrt (~6)
+        setup = 30
+        prim_flops = 2 * (vem.nfma + bops) + (vem.nmul + setup + (L + 1))
+        # per contracted quartet: HRR + scatter (6 FMA per integral)
+        contr_flops = 2 * hem.nfma + hem.nmul + 2 * 6 * NA * NB * NC * ND
+        lines = []
+        lines.append("// class (%d%d|%d%d): VRR %s-choice %d ops, HRR %s-choice %d ops" % (la, lb, lc, ld, chv, cost_v, chh, cost_h))
+        lines.append("template <> struct EriClass<%d,%d,%d,%d> {" % (la, lb, lc, ld))
+        lines.append("  static constexpr int L = %d, NE = %d, NF = %d, NA = %d, NB = %d, NC = %d, ND = %d;" % (L, NE, NF, NA, NB, NC, ND))
+        lines.append("  static constexpr bool BOYS_DIRECT = %s;" % ("true" if direct else "false"))
+        lines.append("  static constexpr double PRIM_FLOPS = %d.0, CONTR_FLOPS = %d.0;" % (prim_flops, contr_flops))
+        lines.append("  template <typename R> __host__ __device__ static __forceinline__ void vrr(R* __restrict__ acc, const R* __restrict__ F,")
+        lines.append("      R PAx, R PAy, R PAz, R WPx, R WPy, R WPz, R QCx, R QCy, R QCz, R WQx, R WQy, R WQz,")
+        lines.append("      R ohp, R ohq, R ohpq, R rho_p, R rho_q) {")
+        lines.append("    (void)PAx; (void)PAy; (void)PAz; (void)WPx; (void)WPy; (void)WPz; (void)QCx; (void)QCy; (void)QCz;")
+        lines.append("    (void)WQx; (void)WQy; (void)WQz; (void)ohp; (void)ohq; (void)ohpq; (void)rho_p; (void)rho_q;")
+        lines.extend(vem.lines)
+        lines.append("  }")
+        lines.append("  template <typename R> __host__ __device__ static __forceinline__ void hrr(const R* __restrict__ acc, R* __restrict__ out,")
+        lines.append("      R ABx, R ABy, R ABz, R CDx, R CDy, R CDz) {")
+        lines.append("    (void)ABx; (void)ABy; (void)ABz; (void)CDx; (void)CDy; (void)CDz;")
+        lines.extend(hem.lines)
+        lines.append("  }")
+        lines.append("};")
+        with open(os.path.join(outdir, "eri_class_%s.inc" % tag), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        table.append((la, lb, lc, ld, prim_flops, contr_flops, NA * NB * NC * ND))
+    # one translation unit per class (compiled in parallel)
+    for (la, lb, lc, ld) in cls:
+        tag = "%d%d%d%d" % (la, lb, lc, ld)
+        with open(os.path.join(outdir, "eri_%s.cu" % tag), "w") as f:
+            f.write("// generated by gen_eri.py -- do not edit\n")
+            f.write('#include "../eri_kernel.cuh"\n#include "eri_class_%s.inc"\n' % tag)
+            f.write("void rchem_launch_eri_%s(const EriArgs &a, int fp32, int epi, cudaStream_t s) {\n" % tag)
+            f.write("    launch_eri_class<%d, %d, %d, %d>(a, fp32, epi, s);\n}\n" % (la, lb, lc, ld))
+    with open(os.path.join(outdir, "eri_dispatch.h"), "w") as f:
+        f.write("// generated by gen_eri.py -- do not edit\n#pragma once\n#include <cuda_runtime.h>\n")
+        f.write('#include "../rchem_types.h"\n')
+        for (la, lb, lc, ld) in cls:
+            f.write("void rchem_launch_eri_%d%d%d%d(const EriArgs &a, int fp32, int epi, cudaStream_t s);\n" % (la, lb, lc, ld))
+        f.write("typedef void (*rchem_eri_launcher)(const EriArgs &, int, int, cudaStream_t);\n")
+        f.write("static const rchem_eri_launcher rchem_eri_launchers[%d] = {\n" % len(cls))
+        for (la, lb, lc, ld) in cls:
+            f.write("  rchem_launch_eri_%d%d%d%d,\n" % (la, lb, lc, ld))
+        f.write("};\n")
+    # index header
+    with open(os.path.join(outdir, "eri_classes.h"), "w") as f:
+        f.write("// generated by gen_eri.py -- do not edit\n#pragma once\n")
+        f.write("#define RCHEM_NCLASS %d\n" % len(cls))
+        f.write("static const int rchem_class_l[%d][4] = {\n" % len(cls))
+        for t in table:
+            f.write("  {%d,%d,%d,%d},\n" % t[:4])
+        f.write("};\n")
+        f.write("static const double rchem_class_flops[%d][2] = {\n" % len(cls))
+        for t in table:
+            f.write("  {%d.0, %d.0},\n" % t[4:6])
+        f.write("};\n")
+    return table
+
+
+if __name__ == "__main__":
+    tab = main(sys.argv[1] if len(sys.argv) > 1 else "_gen")
+    for t in tab:
+        print("(%d%d|%d%d) prim %6d flops  contr %7d flops  %4d ints" % t)

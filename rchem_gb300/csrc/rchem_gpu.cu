@@ -1,0 +1,1089 @@
+// rchem_gpu.cu -- C ABI (include/rchem_gpu.h, include/rchem_cints.h), the
+// host-side planner and the non-class kernels of librchem_gpu.so.
+//
+// Planner: shells -> shell pairs (l_A >= l_B) -> primitive pairs with all
+// per-pair quantities precomputed -> Schwarz bounds Q_ab on the GPU (the class
+// kernels' diagonal epilogue) -> pair groups (l_A, l_B, primitive-pair count),
+// each sorted by Q descending -> per-class warp task lists.  Because a group
+// is sorted by Q, the kets surviving Q_ab Q_cd >= tau for a bra are a prefix
+// of every ket group, found by binary search: no quartet list is ever built.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rchem_cints.h"
+#include "../../include/rchem_gpu.h"
+#include "_gen/eri_classes.h"
+#include "_gen/eri_dispatch.h"
+#include "boys.cuh"
+#include "eri_kernel.cuh"
+#include "md.cuh"
+#include "rchem_types.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+static int set_err(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return set_err(e_ == cudaErrorMemoryAllocation ? RCHEM_ERR_NOMEM : RCHEM_ERR_CUDA, "%s: %s", \
+                           #call, cudaGetErrorString(e_));                                             \
+    } while (0)
+
+#define CKR(expr)                      \
+    do {                               \
+        int r_ = (expr);               \
+        if (r_ != RCHEM_OK) return r_; \
+    } while (0)
+
+extern "C" const char *rchem_last_error(void) { return g_err; }
+extern "C" int rchem_abi_version(void) { return 1; }
+
+// ---------------------------------------------------------------------------
+// Boys tables (one copy per device)
+// ---------------------------------------------------------------------------
+static double boys_series(int m, double x) {
+    // F_m(x) = e^{-x} sum_k (2x)^k / prod_{i=0..k} (2m+2i+1): every term positive
+    double term = 1.0 / (2 * m + 1), sum = term;
+    for (int k = 1; k < 1000; ++k) {
+        term *= 2.0 * x / (2 * m + 2 * k + 1);
+        sum += term;
+        if (term < sum * 1e-18) break;
+    }
+    return std::exp(-x) * sum;
+}
+
+struct DevTables {
+    double *boys64 = nullptr, *exp64 = nullptr;
+    float *boys32 = nullptr, *exp32 = nullptr;
+};
+static DevTables g_tabs[64];
+static std::mutex g_tab_mu;
+
+static int get_tables(const DevTables **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_err(RCHEM_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lk(g_tab_mu);
+    DevTables &t = g_tabs[dev];
+    if (!t.boys64) {
+        std::vector<double> b64((size_t)BOYS_NGRID * BOYS_NCOL), e64(BOYS_NGRID);
+        std::vector<float> b32((size_t)BOYS_NGRID * BOYS_NCOL), e32(BOYS_NGRID);
+        for (int i = 0; i < BOYS_NGRID; ++i) {
+            const double T = (double)i * BOYS_H;  // exact: h = 1/16
+            for (int m = 0; m < BOYS_NCOL; ++m) {
+                const double f = boys_series(m, T);
+                b64[(size_t)i * BOYS_NCOL + m] = f;
+                b32[(size_t)i * BOYS_NCOL + m] = (float)f;
+            }
+            e64[i] = std::exp(-T);
+            e32[i] = (float)e64[i];
+        }
+        DevTables n;
+        CK(cudaMalloc(&n.boys64, b64.size() * sizeof(double)));
+        CK(cudaMalloc(&n.exp64, e64.size() * sizeof(double)));
+        CK(cudaMalloc(&n.boys32, b32.size() * sizeof(float)));
+        CK(cudaMalloc(&n.exp32, e32.size() * sizeof(float)));
+        CK(cudaMemcpy(n.boys64, b64.data(), b64.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(n.exp64, e64.data(), e64.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(n.boys32, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(n.exp32, e32.data(), e32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        t = n;
+    }
+    *out = &t;
+    return RCHEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+static int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+static double fact2(int n) {
+    double r = 1.0;
+    for (int i = n; i > 1; i -= 2) r *= i;
+    return r;
+}
+
+// PGTO::normalization, src/basis.rs:140-149
+static double pgto_norm(double alpha, int l, int m, int n) {
+    const int L = l + m + n;
+    const double num = std::pow(2.0, 2.0 * L + 1.5) * std::pow(alpha, L + 1.5);
+    const double den = fact2(2 * l - 1) * fact2(2 * m - 1) * fact2(2 * n - 1) * std::pow(M_PI, 1.5);
+    return std::sqrt(num / den);
+}
+
+// Cartesian component k of a shell with angular momentum l, src/shell.rs:1-12
+RCHEM_HD inline void cart_comp(int l, int k, int *lmn) {
+    int idx = 0;
+    for (int a = 1; a <= l + 1; ++a)
+        for (int b = 1; b <= a; ++b, ++idx)
+            if (idx == k) {
+                lmn[0] = l + 1 - a;
+                lmn[1] = a - b;
+                lmn[2] = b - 1;
+                return;
+            }
+    lmn[0] = lmn[1] = lmn[2] = 0;
+}
+
+static int pair_cls(int la, int lb) {
+    static const int t[3][3] = {{0, -1, -1}, {1, 2, -1}, {3, 4, 5}};
+    return t[la][lb];
+}
+static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
+
+static bool is_dev_ptr(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// ---------------------------------------------------------------------------
+// generic kernels (scalar cints entry points, one-electron matrices)
+// ---------------------------------------------------------------------------
+__global__ void k_eri_prim_batch(int count, const rchem_prim *pr, const double *boys, double *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const rchem_prim *q = pr + 4 * (size_t)i;
+    double R[4][3];
+    int l[4][3];
+    for (int k = 0; k < 4; ++k) {
+        R[k][0] = q[k].x; R[k][1] = q[k].y; R[k][2] = q[k].z;
+        l[k][0] = q[k].l; l[k][1] = q[k].m; l[k][2] = q[k].n;
+    }
+    out[i] = q[0].norm * q[1].norm * q[2].norm * q[3].norm *
+             md_eri_prim(R[0], l[0], q[0].alpha, R[1], l[1], q[1].alpha, R[2], l[2], q[2].alpha, R[3], l[3],
+                         q[3].alpha, boys);
+}
+
+__global__ void k_onee_prim_batch(int kind, int count, const rchem_prim *pr, const double *C, const double *boys,
+                                  double *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const rchem_prim *q = pr + 2 * (size_t)i;
+    const double A[3] = {q[0].x, q[0].y, q[0].z}, B[3] = {q[1].x, q[1].y, q[1].z};
+    const int la[3] = {q[0].l, q[0].m, q[0].n}, lb[3] = {q[1].l, q[1].m, q[1].n};
+    const double zero[3] = {0, 0, 0};
+    const double *Cc = (kind == 2) ? C + 3 * (size_t)i : zero;
+    double v = md_onee_prim(kind, A, la, q[0].alpha, B, lb, q[1].alpha, Cc, boys);
+    if (kind == 2) v *= q[0].norm * q[1].norm;
+    out[i] = v;
+}
+
+__global__ void k_boys_batch(int count, const int *m, const double *x, const double *b64, const float *b32,
+                             int prec, double *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int mm = m[i];
+    if (prec == 32) {
+        float F[BOYS_NCOL];
+        boys_eval_rt<float>(mm, (float)x[i], 1.0f, b32, F);
+        out[i] = F[mm];
+    } else {
+        double F[BOYS_NCOL];
+        boys_eval_rt<double>(mm, x[i], 1.0, b64, F);
+        out[i] = F[mm];
+    }
+}
+
+// one basis function for the one-electron kernels
+struct AODev {
+    int shell, lmn[3];
+    double cn;  // N(alpha,l,m,n)/N(alpha,L,0,0)
+};
+struct ShellDev {
+    double R[3];
+    int l, nprim, prim0, atom;
+};
+
+// kind: 0 S, 1 T, 2 V (sum over atoms, Z-weighted), 3 moment
+__global__ void k_onee_matrix(int kind, int nbf, const AODev *ao, const ShellDev *sh, const double *pexp,
+                              const double *pcoef, int natoms, const double *Z, const double *Ratoms,
+                              const double *boys, const double *center, int ox, int oy, int oz, double *out) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)nbf * nbf) return;
+    const int mu = (int)(idx / nbf), nu = (int)(idx % nbf);
+    if (nu > mu) return;  // lower triangle + mirror, src/basis.rs:237-248
+    const AODev a = ao[mu], b = ao[nu];
+    const ShellDev sa = sh[a.shell], sb = sh[b.shell];
+    const int ord[3] = {ox, oy, oz};
+    double v = 0.0;
+    for (int j = 0; j < sb.nprim; ++j) {
+        const double ebj = pexp[sb.prim0 + j], cbj = pcoef[sb.prim0 + j];
+        for (int i = 0; i < sa.nprim; ++i) {
+            const double eai = pexp[sa.prim0 + i], cc = pcoef[sa.prim0 + i] * cbj;
+            double x;
+            if (kind == 2) {
+                x = 0.0;
+                for (int c = 0; c < natoms; ++c)
+                    x += Z[c] * md_onee_prim(2, sa.R, a.lmn, eai, sb.R, b.lmn, ebj, Ratoms + 3 * c, boys);
+            } else if (kind == 3) {
+                x = md_moment_prim(sa.R, a.lmn, eai, sb.R, b.lmn, ebj, center, ord);
+            } else {
+                x = md_onee_prim(kind, sa.R, a.lmn, eai, sb.R, b.lmn, ebj, sa.R, boys);
+            }
+            v += cc * x;
+        }
+    }
+    v *= a.cn * b.cn;
+    out[(size_t)mu * nbf + nu] = v;
+    out[(size_t)nu * nbf + mu] = v;
+}
+
+// J = Jhat + Jhat^T, K = Khat + Khat^T
+__global__ void k_symmetrize(int n, const double *Jh, const double *Kh, double *J, double *K) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * n) return;
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    const size_t ij = (size_t)i * n + j, ji = (size_t)j * n + i;
+    J[ij] = Jh[ij] + Jh[ji];
+    K[ij] = Kh[ij] + Kh[ji];
+}
+
+__global__ void k_to_f32(long long n, const double *x, float *y) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (float)x[i];
+}
+
+// JK_inmem, src/basis.rs:462-484
+__global__ void k_jk_inmem(int n, const double *I, const double *D, double *J, double *K) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * n) return;
+    const int mu = (int)(idx / n), nu = (int)(idx % n);
+    if (nu > mu) return;
+    const size_t N1 = n, N2 = N1 * n, N3 = N2 * n;
+    double j = 0.0, k = 0.0;
+    for (int la = 0; la < n; ++la)
+        for (int sg = 0; sg < n; ++sg) {
+            const double d = D[(size_t)la * n + sg];
+            j += I[mu * N3 + nu * N2 + la * N1 + sg] * d;
+            k += I[mu * N3 + la * N2 + nu * N1 + sg] * d;
+        }
+    J[(size_t)mu * n + nu] = J[(size_t)nu * n + mu] = j;
+    K[(size_t)mu * n + nu] = K[(size_t)nu * n + mu] = k;
+}
+
+// ---------------------------------------------------------------------------
+// basis handle
+// ---------------------------------------------------------------------------
+struct PairGroup {
+    int cls, la, lb, npp, begin, end;
+};
+
+struct rchem_basis_s {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int natoms = 0, nbf = 0, nshells = 0;
+    std::vector<int> Z;
+    std::vector<double> R;
+    std::vector<ShellInfo> shells;
+    std::vector<double> pexp, pcoef;  // per primitive, coefficient x N(alpha,l,0,0)
+    std::vector<AODev> aos;
+    // pairs (sorted: by group, then Q descending)
+    std::vector<ShellPair> pairs;
+    std::vector<PairGroup> groups;
+    int nprims = 0;
+    // device
+    ShellPair *d_pairs = nullptr;
+    PairPrim *d_prims = nullptr;
+    PairPrim32 *d_prims32 = nullptr;
+    AODev *d_ao = nullptr;
+    ShellDev *d_sh = nullptr;
+    double *d_pexp = nullptr, *d_pcoef = nullptr, *d_Z = nullptr, *d_R = nullptr;
+    const DevTables *tabs = nullptr;
+    // plan
+    bool planned = false;
+    double plan_tau = -1.0, plan_tau32 = -1.0;
+    EriTask *d_tasks = nullptr;
+    size_t tasks_cap = 0;
+    long long task_off[RCHEM_NCLASS][2], task_cnt[RCHEM_NCLASS][2];
+    rchem_jk_stats plan_stats;
+    rchem_jk_stats last_stats;
+    // Fock-build work buffers
+    double *d_D = nullptr, *d_Jh = nullptr, *d_Kh = nullptr, *d_Jo = nullptr, *d_Ko = nullptr;
+    float *d_D32 = nullptr;
+};
+
+static void free_basis(rchem_basis b) {
+    if (!b) return;
+    void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
+                    b->d_R, b->d_tasks, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+template <typename T>
+static int upload(T **dst, const std::vector<T> &src, cudaStream_t s) {
+    if (src.empty()) return RCHEM_OK;
+    CK(cudaMalloc(dst, src.size() * sizeof(T)));
+    CK(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return RCHEM_OK;
+}
+
+static const double kPrimCut = 1e-22;  // drop primitive pairs with exp(-ab/p |AB|^2) below this
+
+static EriArgs base_args(rchem_basis b) {
+    EriArgs a;
+    memset(&a, 0, sizeof(a));
+    a.nbf = b->nbf;
+    a.pairs = b->d_pairs;
+    a.prims = b->d_prims;
+    a.prims32 = b->d_prims32;
+    a.boys64 = b->tabs->boys64;
+    a.exp64 = b->tabs->exp64;
+    a.boys32 = b->tabs->boys32;
+    a.exp32 = b->tabs->exp32;
+    return a;
+}
+
+// Schwarz bounds for every pair (class kernels, diagonal epilogue)
+static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
+    const int np = (int)b->pairs.size();
+    std::vector<EriTask> tasks;
+    std::vector<int> tkern;
+    for (const PairGroup &g : b->groups) {
+        for (int i = g.begin; i < g.end; i += 32) {
+            EriTask t;
+            t.bra = i;
+            t.ket0 = i;
+            t.nket = std::min(32, g.end - i);
+            t.flags = 0;
+            tasks.push_back(t);
+            tkern.push_back(quartet_kernel(g.cls, g.cls));
+        }
+    }
+    // tasks are already contiguous per group; launch per group range
+    EriTask *d_t = nullptr;
+    double *d_Q = nullptr;
+    CKR(upload(&d_t, tasks, b->stream));
+    CK(cudaMalloc(&d_Q, (size_t)np * sizeof(double)));
+    EriArgs a = base_args(b);
+    a.J = d_Q;
+    size_t pos = 0;
+    while (pos < tasks.size()) {
+        size_t e = pos;
+        while (e < tasks.size() && tkern[e] == tkern[pos]) ++e;
+        a.tasks = d_t + pos;
+        a.ntasks = (int)(e - pos);
+        rchem_eri_launchers[tkern[pos]](a, 0, EPI_DIAG, b->stream);
+        pos = e;
+    }
+    CK(cudaGetLastError());
+    Q.assign(np, 0.0);
+    CK(cudaMemcpyAsync(Q.data(), d_Q, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    cudaFree(d_t);
+    cudaFree(d_Q);
+    return RCHEM_OK;
+}
+
+static int build_pairs(rchem_basis b) {
+    struct Cand {
+        ShellPair sp;
+        std::vector<PairPrim> pp;
+        int cls;
+    };
+    std::vector<Cand> cands;
+    const double c_pref = std::sqrt(2.0) * std::pow(M_PI, 1.25);
+    for (int A = 0; A < b->nshells; ++A)
+        for (int B = 0; B < b->nshells; ++B) {
+            const ShellInfo &sa = b->shells[A], &sb = b->shells[B];
+            if (!(sa.l > sb.l || (sa.l == sb.l && A >= B))) continue;
+            Cand c;
+            double AB[3], r2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                AB[d] = sa.R[d] - sb.R[d];
+                r2 += AB[d] * AB[d];
+            }
+            for (int i = 0; i < sa.nprim; ++i)
+                for (int j = 0; j < sb.nprim; ++j) {
+                    const double aa = b->pexp[sa.prim0 + i], ab = b->pexp[sb.prim0 + j];
+                    const double p = aa + ab, E = std::exp(-aa * ab / p * r2);
+                    if (E < kPrimCut) continue;
+                    PairPrim q;
+                    q.p = p;
+                    q.ohp = 0.5 / p;
+                    for (int d = 0; d < 3; ++d) {
+                        q.P[d] = (aa * sa.R[d] + ab * sb.R[d]) / p;
+                        q.PA[d] = q.P[d] - sa.R[d];
+                    }
+                    q.K = b->pcoef[sa.prim0 + i] * b->pcoef[sb.prim0 + j] * E * c_pref / p;
+                    q.pad = 0.0;
+                    c.pp.push_back(q);
+                }
+            if (c.pp.empty()) continue;
+            ShellPair &s = c.sp;
+            memset(&s, 0, sizeof(s));
+            s.A = A;
+            s.B = B;
+            s.aoA = sa.ao;
+            s.aoB = sb.ao;
+            s.npp = (int)c.pp.size();
+            s.diag = (A == B) ? 1 : 0;
+            for (int d = 0; d < 3; ++d) {
+                s.AB[d] = AB[d];
+                s.AB32[d] = (float)AB[d];
+            }
+            s.la_lb = 10 * sa.l + sb.l;
+            c.cls = pair_cls(sa.l, sb.l);
+            cands.push_back(std::move(c));
+        }
+    // groups keyed by (class, npp)
+    std::map<std::pair<int, int>, std::vector<int>> gm;
+    for (int i = 0; i < (int)cands.size(); ++i) gm[{cands[i].cls, cands[i].sp.npp}].push_back(i);
+    b->pairs.clear();
+    b->groups.clear();
+    std::vector<PairPrim> prims;
+    for (auto &kv : gm) {
+        PairGroup g;
+        g.cls = kv.first.first;
+        g.npp = kv.first.second;
+        const ShellPair &s0 = cands[kv.second[0]].sp;
+        g.la = s0.la_lb / 10;
+        g.lb = s0.la_lb % 10;
+        g.begin = (int)b->pairs.size();
+        for (int ci : kv.second) {
+            Cand &c = cands[ci];
+            c.sp.prim0 = (int)prims.size();
+            c.sp.group = (int)b->groups.size();
+            prims.insert(prims.end(), c.pp.begin(), c.pp.end());
+            b->pairs.push_back(c.sp);
+        }
+        g.end = (int)b->pairs.size();
+        b->groups.push_back(g);
+    }
+    b->nprims = (int)prims.size();
+    std::vector<PairPrim32> p32(prims.size());
+    for (size_t i = 0; i < prims.size(); ++i) {
+        const PairPrim &q = prims[i];
+        PairPrim32 &r = p32[i];
+        r.p = (float)q.p;
+        r.ohp = (float)q.ohp;
+        for (int d = 0; d < 3; ++d) {
+            r.P[d] = (float)q.P[d];
+            r.PA[d] = (float)q.PA[d];
+        }
+        r.K = (float)q.K;
+        r.pad[0] = r.pad[1] = r.pad[2] = 0.f;
+    }
+    CKR(upload(&b->d_prims, prims, b->stream));
+    CKR(upload(&b->d_prims32, p32, b->stream));
+    CKR(upload(&b->d_pairs, b->pairs, b->stream));
+    // Schwarz bounds, then sort each group by Q descending
+    std::vector<double> Q;
+    CKR(compute_schwarz(b, Q));
+    for (size_t i = 0; i < b->pairs.size(); ++i) b->pairs[i].Q = Q[i];
+    for (const PairGroup &g : b->groups)
+        std::stable_sort(b->pairs.begin() + g.begin, b->pairs.begin() + g.end,
+                         [](const ShellPair &x, const ShellPair &y) { return x.Q > y.Q; });
+    CK(cudaMemcpyAsync(b->d_pairs, b->pairs.data(), b->pairs.size() * sizeof(ShellPair), cudaMemcpyHostToDevice,
+                       b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
+}
+
+// number of kets in [g.begin, g.end) with Q >= thr (Q sorted descending)
+static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double thr) {
+    auto it = std::partition_point(p.begin() + g.begin, p.begin() + g.end,
+                                   [thr](const ShellPair &s) { return s.Q >= thr; });
+    return (int)(it - (p.begin() + g.begin));
+}
+
+static int plan_tasks(rchem_basis b, double tau, double tau32) {
+    if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32) return RCHEM_OK;
+    std::vector<EriTask> lists[RCHEM_NCLASS][2];
+    rchem_jk_stats st;
+    memset(&st, 0, sizeof(st));
+    const std::vector<ShellPair> &P = b->pairs;
+    for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
+        const PairGroup &gb = b->groups[gbi];
+        for (int gki = 0; gki < (int)b->groups.size(); ++gki) {
+            const PairGroup &gk = b->groups[gki];
+            if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
+            const int k = quartet_kernel(gb.cls, gk.cls);
+            const int ncomp = ncart(gb.la) * ncart(gb.lb) * ncart(gk.la) * ncart(gk.lb);
+            const long long nprimq = (long long)gb.npp * gk.npp;
+            for (int ib = gb.begin; ib < gb.end; ++ib) {
+                const double Qb = P[ib].Q;
+                if (!(Qb > 0.0)) continue;
+                int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
+                if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
+                int m = (tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
+                for (int prec = 0; prec < 2; ++prec) {
+                    const int lo = prec ? m : 0, hi = prec ? nk : m;
+                    for (int j = lo; j < hi; j += 32) {
+                        EriTask t;
+                        t.bra = ib;
+                        t.ket0 = gk.begin + j;
+                        t.nket = std::min(32, hi - j);
+                        t.flags = (int)std::min<long long>(nprimq, 1 << 30);
+                        lists[k][prec].push_back(t);
+                    }
+                    const long long nq = hi - lo;
+                    if (nq <= 0) continue;
+                    const double fl = rchem_class_flops[k][0] * nprimq * nq + rchem_class_flops[k][1] * nq;
+                    if (prec) {
+                        st.quartets_fp32 += nq;
+                        st.prim_quartets_fp32 += nq * nprimq;
+                        st.eris_fp32 += nq * ncomp;
+                        st.flops_fp32 += fl;
+                    } else {
+                        st.quartets_fp64 += nq;
+                        st.prim_quartets_fp64 += nq * nprimq;
+                        st.eris_fp64 += nq * ncomp;
+                        st.flops_fp64 += fl;
+                    }
+                }
+            }
+        }
+    }
+    // heaviest tasks first inside each list (load balance of the tail)
+    size_t total = 0;
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p) {
+            std::stable_sort(lists[k][p].begin(), lists[k][p].end(),
+                             [](const EriTask &x, const EriTask &y) { return x.flags > y.flags; });
+            total += lists[k][p].size();
+        }
+    std::vector<EriTask> flat;
+    flat.reserve(total);
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p) {
+            b->task_off[k][p] = (long long)flat.size();
+            b->task_cnt[k][p] = (long long)lists[k][p].size();
+            flat.insert(flat.end(), lists[k][p].begin(), lists[k][p].end());
+            if (!lists[k][p].empty()) st.kernels += 1;
+        }
+    st.warp_tasks = (long long)flat.size();
+    if (flat.size() > b->tasks_cap) {
+        if (b->d_tasks) cudaFree(b->d_tasks);
+        b->d_tasks = nullptr;
+        b->tasks_cap = 0;
+        CK(cudaMalloc(&b->d_tasks, std::max<size_t>(flat.size(), 1) * sizeof(EriTask)));
+        b->tasks_cap = flat.size();
+    }
+    if (!flat.empty())
+        CK(cudaMemcpyAsync(b->d_tasks, flat.data(), flat.size() * sizeof(EriTask), cudaMemcpyHostToDevice,
+                           b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    b->plan_stats = st;
+    b->planned = true;
+    b->plan_tau = tau;
+    b->plan_tau32 = tau32;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords,
+                                  int nshells, const int *shell_atom, const int *shell_l, const int *shell_nprim,
+                                  const double *exps, const double *coefs) {
+    if (!out) return set_err(RCHEM_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (natoms <= 0 || nshells <= 0) return set_err(RCHEM_ERR_INVALID, "natoms=%d nshells=%d", natoms, nshells);
+    if (!atomnos || !coords || !shell_atom || !shell_l || !shell_nprim || !exps || !coefs)
+        return set_err(RCHEM_ERR_INVALID, "null array argument");
+    for (int i = 0; i < 3 * natoms; ++i)
+        if (!std::isfinite(coords[i])) return set_err(RCHEM_ERR_INVALID, "coordinate %d is not finite", i);
+    rchem_basis b = new rchem_basis_s();
+    CK(cudaGetDevice(&b->dev));
+    b->natoms = natoms;
+    b->Z.assign(atomnos, atomnos + natoms);
+    b->R.assign(coords, coords + 3 * natoms);
+    b->nshells = nshells;
+    int pos = 0, ao = 0;
+    for (int s = 0; s < nshells; ++s) {
+        const int l = shell_l[s], np = shell_nprim[s], at = shell_atom[s];
+        if (l < 0 || l > RCHEM_MAX_L) {
+            free_basis(b);
+            return set_err(RCHEM_ERR_UNSUPPORTED, "shell %d has l=%d (supported: 0..%d)", s, l, RCHEM_MAX_L);
+        }
+        if (np < 1 || np > RCHEM_MAX_NPRIM) {
+            free_basis(b);
+            return set_err(RCHEM_ERR_UNSUPPORTED, "shell %d has %d primitives (supported: 1..%d)", s, np,
+                           RCHEM_MAX_NPRIM);
+        }
+        if (at < 0 || at >= natoms) {
+            free_basis(b);
+            return set_err(RCHEM_ERR_INVALID, "shell %d on atom %d of %d", s, at, natoms);
+        }
+        ShellInfo si;
+        si.atom = at;
+        si.l = l;
+        si.nprim = np;
+        si.prim0 = (int)b->pexp.size();
+        si.ao = ao;
+        for (int d = 0; d < 3; ++d) si.R[d] = coords[3 * at + d];
+        for (int k = 0; k < np; ++k) {
+            const double e = exps[pos + k], c = coefs[pos + k];
+            if (!(e > 0.0) || !std::isfinite(e) || !std::isfinite(c)) {
+                free_basis(b);
+                return set_err(RCHEM_ERR_INVALID, "shell %d primitive %d: exponent %g coefficient %g", s, k, e, c);
+            }
+            b->pexp.push_back(e);
+            b->pcoef.push_back(c * pgto_norm(e, l, 0, 0));
+        }
+        pos += np;
+        for (int k = 0; k < ncart(l); ++k) {
+            AODev a;
+            a.shell = s;
+            cart_comp(l, k, a.lmn);
+            a.cn = std::sqrt(fact2(2 * l - 1) / (fact2(2 * a.lmn[0] - 1) * fact2(2 * a.lmn[1] - 1) *
+                                                  fact2(2 * a.lmn[2] - 1)));
+            b->aos.push_back(a);
+        }
+        ao += ncart(l);
+        b->shells.push_back(si);
+    }
+    b->nbf = ao;
+    int rc;
+    if ((rc = get_tables(&b->tabs)) != RCHEM_OK) {
+        free_basis(b);
+        return rc;
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        free_basis(b);
+        return set_err(RCHEM_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    b->own_stream = true;
+    std::vector<ShellDev> shd(nshells);
+    for (int s = 0; s < nshells; ++s) {
+        for (int d = 0; d < 3; ++d) shd[s].R[d] = b->shells[s].R[d];
+        shd[s].l = b->shells[s].l;
+        shd[s].nprim = b->shells[s].nprim;
+        shd[s].prim0 = b->shells[s].prim0;
+        shd[s].atom = b->shells[s].atom;
+    }
+    std::vector<double> Zd(b->Z.begin(), b->Z.end());
+    const size_t nn = (size_t)b->nbf * b->nbf;
+    if ((rc = upload(&b->d_sh, shd, b->stream)) != RCHEM_OK || (rc = upload(&b->d_ao, b->aos, b->stream)) != RCHEM_OK ||
+        (rc = upload(&b->d_pexp, b->pexp, b->stream)) != RCHEM_OK ||
+        (rc = upload(&b->d_pcoef, b->pcoef, b->stream)) != RCHEM_OK ||
+        (rc = upload(&b->d_Z, Zd, b->stream)) != RCHEM_OK || (rc = upload(&b->d_R, b->R, b->stream)) != RCHEM_OK) {
+        free_basis(b);
+        return rc;
+    }
+    if (cudaMalloc(&b->d_D, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_Jh, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_Kh, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_Jo, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_Ko, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_D32, nn * sizeof(float)) != cudaSuccess) {
+        free_basis(b);
+        return set_err(RCHEM_ERR_NOMEM, "work buffers for nbf=%d", ao);
+    }
+    if ((rc = build_pairs(b)) != RCHEM_OK) {
+        free_basis(b);
+        return rc;
+    }
+    memset(&b->last_stats, 0, sizeof(b->last_stats));
+    *out = b;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_basis_destroy(rchem_basis b) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    free_basis(b);
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_basis_nbf(rchem_basis b) { return b ? b->nbf : -1; }
+
+extern "C" int rchem_basis_set_stream(rchem_basis b, void *stream) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    b->own_stream = false;
+    b->stream = (cudaStream_t)stream;
+    return RCHEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// output staging: device results -> caller's buffer
+// ---------------------------------------------------------------------------
+static int finish_out(rchem_basis b, const double *d_src, double *dst, size_t n, int where) {
+    if (where == RCHEM_DEVICE) {
+        if (d_src != dst) CK(cudaMemcpyAsync(dst, d_src, n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+    } else {
+        CK(cudaMemcpyAsync(dst, d_src, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
+}
+
+static int onee(rchem_basis b, int kind, const double *center, int ox, int oy, int oz, double *out, int where) {
+    if (!b || !out) return set_err(RCHEM_ERR_INVALID, "null argument");
+    if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
+    double *dst = (where == RCHEM_DEVICE) ? out : b->d_Jo;
+    double *d_c = nullptr;
+    if (kind == 3) {
+        CK(cudaMalloc(&d_c, 3 * sizeof(double)));
+        CK(cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    }
+    const long long n2 = (long long)b->nbf * b->nbf;
+    const int th = 128;
+    k_onee_matrix<<<(unsigned)((n2 + th - 1) / th), th, 0, b->stream>>>(kind, b->nbf, b->d_ao, b->d_sh, b->d_pexp,
+                                                                         b->d_pcoef, b->natoms, b->d_Z, b->d_R,
+                                                                         b->tabs->boys64, d_c, ox, oy, oz, dst);
+    CK(cudaGetLastError());
+    int rc = finish_out(b, dst, out, (size_t)n2, where);
+    if (d_c) cudaFree(d_c);
+    return rc;
+}
+
+extern "C" int rchem_S(rchem_basis b, double *out, int where) { return onee(b, 0, nullptr, 0, 0, 0, out, where); }
+extern "C" int rchem_T(rchem_basis b, double *out, int where) { return onee(b, 1, nullptr, 0, 0, 0, out, where); }
+extern "C" int rchem_V(rchem_basis b, double *out, int where) { return onee(b, 2, nullptr, 0, 0, 0, out, where); }
+extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy, int oz, double *out, int where) {
+    if (!center) return set_err(RCHEM_ERR_INVALID, "null center");
+    if (ox < 0 || oy < 0 || oz < 0 || ox + oy + oz > 4) return set_err(RCHEM_ERR_UNSUPPORTED, "moment order");
+    return onee(b, 3, center, ox, oy, oz, out, where);
+}
+
+// ---------------------------------------------------------------------------
+// Fock build
+// ---------------------------------------------------------------------------
+extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts) {
+    if (!b || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "null argument");
+    rchem_jk_opts o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
+    const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
+    const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
+    CKR(plan_tasks(b, tau, tau32));
+    const int n = b->nbf;
+    const size_t nn = (size_t)n * n;
+    const double *dD = D;
+    if (o.where == RCHEM_HOST) {
+        CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+        dD = b->d_D;
+    }
+    bool any32 = false;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
+    const int th = 256;
+    if (any32) {
+        k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, dD, b->d_D32);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemsetAsync(b->d_Jh, 0, nn * sizeof(double), b->stream));
+    CK(cudaMemsetAsync(b->d_Kh, 0, nn * sizeof(double), b->stream));
+    EriArgs a = base_args(b);
+    a.D = dD;
+    a.D32 = b->d_D32;
+    a.J = b->d_Jh;
+    a.K = b->d_Kh;
+    // FP32 lists first: they are cheap and their atomics overlap the FP64 work
+    for (int prec = 1; prec >= 0; --prec)
+        for (int k = RCHEM_NCLASS - 1; k >= 0; --k) {
+            if (b->task_cnt[k][prec] == 0) continue;
+            a.tasks = b->d_tasks + b->task_off[k][prec];
+            a.ntasks = (int)b->task_cnt[k][prec];
+            rchem_eri_launchers[k](a, prec, EPI_JK, b->stream);
+        }
+    CK(cudaGetLastError());
+    double *Jd = (o.where == RCHEM_DEVICE) ? J : b->d_Jo;
+    double *Kd = (o.where == RCHEM_DEVICE) ? K : b->d_Ko;
+    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, b->d_Jh, b->d_Kh, Jd, Kd);
+    CK(cudaGetLastError());
+    if (o.where == RCHEM_HOST) {
+        CK(cudaMemcpyAsync(J, Jd, nn * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaMemcpyAsync(K, Kd, nn * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    b->last_stats = b->plan_stats;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out) {
+    if (!b || !out) return set_err(RCHEM_ERR_INVALID, "null argument");
+    *out = b->last_stats;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
+    if (!b || !I) return set_err(RCHEM_ERR_INVALID, "null argument");
+    if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
+    const size_t n = b->nbf, n4 = n * n * n * n;
+    if (n > 256) return set_err(RCHEM_ERR_UNSUPPORTED, "dense n^4 tensor for n=%zu", n);
+    CKR(plan_tasks(b, 0.0, 0.0));  // every quartet, FP64
+    double *d_I = I;
+    if (where == RCHEM_HOST) CK(cudaMalloc(&d_I, n4 * sizeof(double)));
+    CK(cudaMemsetAsync(d_I, 0, n4 * sizeof(double), b->stream));
+    EriArgs a = base_args(b);
+    a.eri = d_I;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) {
+        if (b->task_cnt[k][0] == 0) continue;
+        a.tasks = b->d_tasks + b->task_off[k][0];
+        a.ntasks = (int)b->task_cnt[k][0];
+        rchem_eri_launchers[k](a, 0, EPI_STORE, b->stream);
+    }
+    CK(cudaGetLastError());
+    int rc = RCHEM_OK;
+    if (where == RCHEM_HOST) {
+        rc = finish_out(b, d_I, I, n4, RCHEM_HOST);
+        cudaFree(d_I);
+    } else {
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    return rc;
+}
+
+extern "C" int rchem_jk_inmem(int n, const double *I, const double *D, double *J, double *K, int where) {
+    if (n <= 0 || !I || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "bad argument");
+    const size_t nn = (size_t)n * n, n4 = nn * nn;
+    const double *dI = I, *dD = D;
+    double *dJ = J, *dK = K;
+    std::vector<void *> tmp;
+    if (where == RCHEM_HOST) {
+        double *a, *b2, *c, *d;
+        CK(cudaMalloc(&a, n4 * sizeof(double)));
+        CK(cudaMalloc(&b2, nn * sizeof(double)));
+        CK(cudaMalloc(&c, nn * sizeof(double)));
+        CK(cudaMalloc(&d, nn * sizeof(double)));
+        tmp = {a, b2, c, d};
+        CK(cudaMemcpy(a, I, n4 * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(b2, D, nn * sizeof(double), cudaMemcpyHostToDevice));
+        dI = a;
+        dD = b2;
+        dJ = c;
+        dK = d;
+    }
+    k_jk_inmem<<<(unsigned)((nn + 127) / 128), 128>>>(n, dI, dD, dJ, dK);
+    CK(cudaGetLastError());
+    if (where == RCHEM_HOST) {
+        CK(cudaMemcpy(J, dJ, nn * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(K, dK, nn * sizeof(double), cudaMemcpyDeviceToHost));
+        for (void *p : tmp) cudaFree(p);
+    } else {
+        CK(cudaDeviceSynchronize());
+    }
+    return RCHEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// cints-compatible scalar and batched entry points
+// ---------------------------------------------------------------------------
+template <typename T>
+static int stage_in(const T *src, size_t n, int where, const T **dev, std::vector<void *> &tmp) {
+    if (where == RCHEM_DEVICE) {
+        *dev = src;
+        return RCHEM_OK;
+    }
+    T *d = nullptr;
+    CK(cudaMalloc(&d, std::max<size_t>(n, 1) * sizeof(T)));
+    tmp.push_back(d);
+    CK(cudaMemcpy(d, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    *dev = d;
+    return RCHEM_OK;
+}
+
+static void free_all(std::vector<void *> &tmp) {
+    for (void *p : tmp) cudaFree(p);
+    tmp.clear();
+}
+
+extern "C" int rchem_eri_prim_batch(int count, const rchem_prim *prims, double *out, int where) {
+    if (count < 0 || (count > 0 && (!prims || !out))) return set_err(RCHEM_ERR_INVALID, "bad argument");
+    if (count == 0) return RCHEM_OK;
+    if (where == RCHEM_HOST)
+        for (int i = 0; i < 4 * count; ++i)
+            if (prims[i].l < 0 || prims[i].m < 0 || prims[i].n < 0 || !(prims[i].alpha > 0.0))
+                return set_err(RCHEM_ERR_INVALID, "primitive %d", i);
+    if (where == RCHEM_HOST)
+        for (int i = 0; i < count; ++i) {
+            int L = 0;
+            for (int k = 0; k < 4; ++k) L += prims[4 * i + k].l + prims[4 * i + k].m + prims[4 * i + k].n;
+            if (L > MD_MAXL) return set_err(RCHEM_ERR_UNSUPPORTED, "quartet %d has total L=%d > %d", i, L, MD_MAXL);
+        }
+    const DevTables *t;
+    CKR(get_tables(&t));
+    std::vector<void *> tmp;
+    const rchem_prim *dp;
+    int rc = stage_in(prims, 4 * (size_t)count, where, &dp, tmp);
+    if (rc) { free_all(tmp); return rc; }
+    double *dout = out;
+    if (where == RCHEM_HOST) {
+        if (cudaMalloc(&dout, count * sizeof(double)) != cudaSuccess) { free_all(tmp); return set_err(RCHEM_ERR_NOMEM, "out"); }
+        tmp.push_back(dout);
+    }
+    k_eri_prim_batch<<<(count + 63) / 64, 64>>>(count, dp, t->boys64, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == RCHEM_HOST) e = cudaMemcpy(out, dout, count * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && where == RCHEM_DEVICE) e = cudaDeviceSynchronize();
+    free_all(tmp);
+    if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "eri batch: %s", cudaGetErrorString(e));
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_onee_prim_batch(int kind, int count, const rchem_prim *prims, const double *centers, double *out,
+                                     int where) {
+    if (kind < 0 || kind > 2) return set_err(RCHEM_ERR_INVALID, "kind=%d", kind);
+    if (count < 0 || (count > 0 && (!prims || !out || (kind == 2 && !centers))))
+        return set_err(RCHEM_ERR_INVALID, "bad argument");
+    if (count == 0) return RCHEM_OK;
+    if (where == RCHEM_HOST)
+        for (int i = 0; i < count; ++i) {
+            const rchem_prim &a = prims[2 * i], &c = prims[2 * i + 1];
+            if (a.l + a.m + a.n + c.l + c.m + c.n > MD_MAXL || a.l + c.l + 2 > MD_MAXE || a.m + c.m + 2 > MD_MAXE ||
+                a.n + c.n + 2 > MD_MAXE)
+                return set_err(RCHEM_ERR_UNSUPPORTED, "pair %d angular momentum too high", i);
+        }
+    const DevTables *t;
+    CKR(get_tables(&t));
+    std::vector<void *> tmp;
+    const rchem_prim *dp;
+    const double *dc = nullptr;
+    int rc = stage_in(prims, 2 * (size_t)count, where, &dp, tmp);
+    if (!rc && kind == 2) rc = stage_in(centers, 3 * (size_t)count, where, &dc, tmp);
+    if (rc) { free_all(tmp); return rc; }
+    double *dout = out;
+    if (where == RCHEM_HOST) {
+        if (cudaMalloc(&dout, count * sizeof(double)) != cudaSuccess) { free_all(tmp); return set_err(RCHEM_ERR_NOMEM, "out"); }
+        tmp.push_back(dout);
+    }
+    k_onee_prim_batch<<<(count + 63) / 64, 64>>>(kind, count, dp, dc, t->boys64, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == RCHEM_HOST) e = cudaMemcpy(out, dout, count * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && where == RCHEM_DEVICE) e = cudaDeviceSynchronize();
+    free_all(tmp);
+    if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "one-electron batch: %s", cudaGetErrorString(e));
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_boys_batch(int count, const int *m, const double *x, double *out, int precision, int where) {
+    if (count < 0 || (count > 0 && (!m || !x || !out))) return set_err(RCHEM_ERR_INVALID, "bad argument");
+    if (precision != 64 && precision != 32) return set_err(RCHEM_ERR_INVALID, "precision=%d", precision);
+    if (count == 0) return RCHEM_OK;
+    if (where == RCHEM_HOST)
+        for (int i = 0; i < count; ++i)
+            if (m[i] < 0 || m[i] > BOYS_NCOL - BoysPrec<double>::NTAY || !(x[i] >= 0.0))
+                return set_err(RCHEM_ERR_INVALID, "m=%d x=%g (0 <= m <= %d, x >= 0)", m[i], x[i],
+                               BOYS_NCOL - BoysPrec<double>::NTAY);
+    const DevTables *t;
+    CKR(get_tables(&t));
+    std::vector<void *> tmp;
+    const int *dm;
+    const double *dx;
+    int rc = stage_in(m, count, where, &dm, tmp);
+    if (!rc) rc = stage_in(x, count, where, &dx, tmp);
+    if (rc) { free_all(tmp); return rc; }
+    double *dout = out;
+    if (where == RCHEM_HOST) {
+        if (cudaMalloc(&dout, count * sizeof(double)) != cudaSuccess) { free_all(tmp); return set_err(RCHEM_ERR_NOMEM, "out"); }
+        tmp.push_back(dout);
+    }
+    k_boys_batch<<<(count + 127) / 128, 128>>>(count, dm, dx, t->boys64, t->boys32, precision, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == RCHEM_HOST) e = cudaMemcpy(out, dout, count * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && where == RCHEM_DEVICE) e = cudaDeviceSynchronize();
+    free_all(tmp);
+    if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "boys batch: %s", cudaGetErrorString(e));
+    return RCHEM_OK;
+}
+
+static rchem_prim mkprim(double x, double y, double z, double norm, int l, int m, int n, double alpha) {
+    rchem_prim p;
+    p.x = x; p.y = y; p.z = z; p.norm = norm; p.alpha = alpha; p.l = l; p.m = m; p.n = n; p.pad = 0;
+    return p;
+}
+
+extern "C" double coulomb_repulsion(double xa, double ya, double za, double norma, int la, int ma, int na,
+                                    double alphaa, double xb, double yb, double zb, double normb, int lb, int mb,
+                                    int nb, double alphab, double xc, double yc, double zc, double normc, int lc,
+                                    int mc, int nc, double alphac, double xd, double yd, double zd, double normd,
+                                    int ld, int md, int nd, double alphad) {
+    rchem_prim q[4] = {mkprim(xa, ya, za, norma, la, ma, na, alphaa), mkprim(xb, yb, zb, normb, lb, mb, nb, alphab),
+                       mkprim(xc, yc, zc, normc, lc, mc, nc, alphac), mkprim(xd, yd, zd, normd, ld, md, nd, alphad)};
+    double v = NAN;
+    if (rchem_eri_prim_batch(1, q, &v, RCHEM_HOST) != RCHEM_OK) return NAN;
+    return v;
+}
+
+extern "C" double overlap(double alpha1, int l1, int m1, int n1, double xa, double ya, double za, double alpha2,
+                          int l2, int m2, int n2, double xb, double yb, double zb) {
+    rchem_prim q[2] = {mkprim(xa, ya, za, 1.0, l1, m1, n1, alpha1), mkprim(xb, yb, zb, 1.0, l2, m2, n2, alpha2)};
+    double v = NAN;
+    if (rchem_onee_prim_batch(0, 1, q, nullptr, &v, RCHEM_HOST) != RCHEM_OK) return NAN;
+    return v;
+}
+
+extern "C" double kinetic(double alpha1, int l1, int m1, int n1, double xa, double ya, double za, double alpha2,
+                          int l2, int m2, int n2, double xb, double yb, double zb) {
+    rchem_prim q[2] = {mkprim(xa, ya, za, 1.0, l1, m1, n1, alpha1), mkprim(xb, yb, zb, 1.0, l2, m2, n2, alpha2)};
+    double v = NAN;
+    if (rchem_onee_prim_batch(1, 1, q, nullptr, &v, RCHEM_HOST) != RCHEM_OK) return NAN;
+    return v;
+}
+
+extern "C" double nuclear_attraction(double x1, double y1, double z1, double norm1, int l1, int m1, int n1,
+                                     double alpha1, double x2, double y2, double z2, double norm2, int l2, int m2,
+                                     int n2, double alpha2, double x3, double y3, double z3) {
+    rchem_prim q[2] = {mkprim(x1, y1, z1, norm1, l1, m1, n1, alpha1), mkprim(x2, y2, z2, norm2, l2, m2, n2, alpha2)};
+    const double c[3] = {x3, y3, z3};
+    double v = NAN;
+    if (rchem_onee_prim_batch(2, 1, q, c, &v, RCHEM_HOST) != RCHEM_OK) return NAN;
+    return v;
+}
+
+extern "C" double Fgamma(double m, double x) {
+    const int mi = (int)(m + 0.5);
+    double v = NAN;
+    if (rchem_boys_batch(1, &mi, &x, &v, 64, RCHEM_HOST) != RCHEM_OK) return NAN;
+    return v;
+}
+
+extern "C" double contr_coulomb(int ia, double *aexps, double *acoefs, double *anorms, double xa, double ya,
+                                double za, int la, int ma, int na, int ib, double *bexps, double *bcoefs,
+                                double *bnorms, double xb, double yb, double zb, int lb, int mb, int nb, int ic,
+                                double *cexps, double *ccoefs, double *cnorms, double xc, double yc, double zc,
+                                int lc, int mc, int nc, int id, double *dexps, double *dcoefs, double *dnorms,
+                                double xd, double yd, double zd, int ld, int md, int nd) {
+    if (ia <= 0 || ib <= 0 || ic <= 0 || id <= 0) {
+        set_err(RCHEM_ERR_INVALID, "empty contraction");
+        return NAN;
+    }
+    const int count = ia * ib * ic * id;
+    std::vector<rchem_prim> q((size_t)count * 4);
+    std::vector<double> w(count), v(count);
+    int k = 0;
+    for (int i = 0; i < ia; ++i)
+        for (int j = 0; j < ib; ++j)
+            for (int c = 0; c < ic; ++c)
+                for (int d = 0; d < id; ++d, ++k) {
+                    q[4 * k + 0] = mkprim(xa, ya, za, anorms[i], la, ma, na, aexps[i]);
+                    q[4 * k + 1] = mkprim(xb, yb, zb, bnorms[j], lb, mb, nb, bexps[j]);
+                    q[4 * k + 2] = mkprim(xc, yc, zc, cnorms[c], lc, mc, nc, cexps[c]);
+                    q[4 * k + 3] = mkprim(xd, yd, zd, dnorms[d], ld, md, nd, dexps[d]);
+                    w[k] = acoefs[i] * bcoefs[j] * ccoefs[c] * dcoefs[d];
+                }
+    if (rchem_eri_prim_batch(count, q.data(), v.data(), RCHEM_HOST) != RCHEM_OK) return NAN;
+    double s = 0.0;
+    for (int i = 0; i < count; ++i) s += w[i] * v[i];
+    return s;
+}

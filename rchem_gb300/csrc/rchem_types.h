@@ -1,0 +1,75 @@
+// rchem_types.h -- device data layout shared by the host planner and the kernels.
+//
+// A basis lives on the GPU as shells (pure l, reference AO order), shell pairs
+// and primitive pairs.  Everything the inner ERI loop reads per primitive
+// quartet is precomputed per primitive pair (product centre, P-A, 1/(2p), the
+// contraction/normalisation/Gaussian-product prefactor), so the loop itself
+// does no divisions and no exponentials.
+#pragma once
+
+#ifdef __CUDACC__
+#define RCHEM_HD __host__ __device__
+#else
+#define RCHEM_HD
+#endif
+
+#define RCHEM_LMAX 2          // s, p, d shells (Cartesian)
+#define RCHEM_MAX_NCART 6
+
+// One primitive pair (alpha_a on shell A, alpha_b on shell B), 80 bytes.
+struct PairPrim {
+    double p;      // alpha_a + alpha_b
+    double ohp;    // 1/(2p)
+    double P[3];   // (alpha_a A + alpha_b B)/p
+    double PA[3];  // P - A
+    double K;      // c_a c_b N_a N_b exp(-alpha_a alpha_b |AB|^2 / p) * sqrt(2) pi^(5/4) / p
+    double pad;
+};
+
+// The same in single precision, for the FP32 part of the mixed form, 48 bytes.
+struct PairPrim32 {
+    float p, ohp, P[3], PA[3], K, pad[3];
+};
+
+// One shell pair (A,B) with l_A >= l_B, 80 bytes.
+struct ShellPair {
+    int A, B;        // shell indices
+    int aoA, aoB;    // first basis function of A and of B
+    int prim0, npp;  // primitive pairs [prim0, prim0 + npp)
+    int group, diag; // pair group; 1 if A == B
+    double AB[3];    // A - B
+    double Q;        // Schwarz bound sqrt(max |(ab|ab)|) over the pair's functions
+    float AB32[3];   // A - B in single precision
+    int la_lb;       // 10*l_A + l_B
+};
+
+// One warp of work: the bra pair against up to 32 consecutive ket pairs of one
+// pair group (same angular momenta, same primitive-pair count).
+struct EriTask {
+    int bra, ket0, nket, flags;
+};
+
+// Arguments of every ERI class kernel.
+struct EriArgs {
+    const EriTask *tasks;
+    int ntasks;
+    int nbf;
+    const ShellPair *pairs;
+    const PairPrim *prims;
+    const PairPrim32 *prims32;
+    const double *boys64;  // F_m(T_i), BOYS_NGRID x BOYS_NCOL
+    const double *exp64;   // exp(-T_i)
+    const float *boys32;
+    const float *exp32;
+    const double *D;       // density, nbf x nbf row-major
+    const float *D32;      // the same in single precision (mixed form)
+    double *J;             // unsymmetrised accumulators (J-hat, K-hat)
+    double *K;
+    double *eri;           // dense nbf^4 output (ERI-tensor epilogue)
+};
+
+// Shell as the planner sees it.
+struct ShellInfo {
+    int atom, l, nprim, prim0, ao;
+    double R[3];
+};

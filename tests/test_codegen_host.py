@@ -1,0 +1,95 @@
+"""The generated HGP class code and the Boys evaluator, compiled for the host
+with g++ (tests/host_eri_check.cpp), against the oracle -- no GPU needed.
+
+This pins the code generator (csrc/gen_eri.py) and csrc/boys.cuh before any
+GPU run; the GPU tests then pin the kernels that wrap them.
+"""
+import ctypes as C
+import itertools
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "rchem_gb300", "csrc")
+
+CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 0, 1, 0), (1, 1, 0, 0), (1, 1, 1, 0), (1, 1, 1, 1), (2, 0, 0, 0),
+           (2, 0, 1, 0), (2, 0, 1, 1), (2, 0, 2, 0), (2, 1, 0, 0), (2, 1, 1, 0), (2, 1, 1, 1), (2, 1, 2, 0),
+           (2, 1, 2, 1), (2, 2, 0, 0), (2, 2, 1, 0), (2, 2, 1, 1), (2, 2, 2, 0), (2, 2, 2, 1), (2, 2, 2, 2)]
+
+
+@pytest.fixture(scope="module")
+def hostlib(tmp_path_factory):
+    d = tmp_path_factory.mktemp("hostcheck")
+    gen = d / "gen"
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("gen_eri", os.path.join(CSRC, "gen_eri.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.main(str(gen))
+    with open(d / "eri_all.inc", "w") as f:
+        for c in CLASSES:
+            f.write('#include "%s/eri_class_%d%d%d%d.inc"\n' % ((str(gen),) + c))
+    so = d / "libhost.so"
+    subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, "-I", str(d), "-o", str(so),
+                    os.path.join(ROOT, "tests", "host_eri_check.cpp")], check=True)
+    L = C.CDLL(str(so))
+    L.host_eri_block.argtypes = [C.c_int] * 5 + [C.c_void_p] * 5
+    L.host_boys.restype = C.c_double
+    L.host_boys.argtypes = [C.c_int, C.c_double, C.c_int]
+    return L
+
+
+def _block_oracle(port, oracle, cls, R, e, c):
+    na = [len(oracle.ijk_list(l)) for l in cls]
+    ref = np.zeros(na)
+    for idx in itertools.product(*[range(x) for x in na]):
+        pw = [oracle.ijk_list(cls[k])[idx[k]] for k in range(4)]
+        v = 0.0
+        for a, b, cc, d in itertools.product(*[range(len(x)) for x in e]):
+            ps = (a, b, cc, d)
+            args = []
+            for k in range(4):
+                args += [R[k], port.pgto_norm(e[k][ps[k]], *pw[k]), pw[k], e[k][ps[k]]]
+            v += c[0][a] * c[1][b] * c[2][cc] * c[3][d] * port.coulomb_repulsion(*args)
+        ref[idx] = v
+    return ref
+
+
+@pytest.mark.parametrize("cls", CLASSES)
+def test_generated_class_vs_oracle(hostlib, port, cls):
+    import oracle
+
+    rng = np.random.default_rng(sum(cls) * 7 + cls[0])
+    for trial in range(2):
+        R = rng.uniform(-1.5, 1.5, (4, 3))
+        if trial == 1:
+            R[1] = R[0]
+            R[3] = R[2]
+        n = rng.integers(1, 3, 4)
+        e = [rng.uniform(0.2, 3.0, k) for k in n]
+        c = [rng.uniform(0.2, 1.0, k) for k in n]
+        cs = np.concatenate([c[k] * np.array([port.pgto_norm(x, cls[k], 0, 0) for x in e[k]]) for k in range(4)])
+        es = np.concatenate(e)
+        ref = _block_oracle(port, oracle, cls, R, e, c)
+        for f32, tol in ((0, 1e-14), (1, 2e-5)):
+            res = np.zeros(ref.size)
+            rc = hostlib.host_eri_block(*cls, f32, np.ascontiguousarray(R).ctypes.data,
+                                        np.ascontiguousarray(n, dtype=np.int32).ctypes.data, es.ctypes.data,
+                                        cs.ctypes.data, res.ctypes.data)
+            assert rc == 0
+            res = res.reshape(ref.shape)
+            scale = 1.0 if f32 == 0 else np.abs(ref).max()
+            assert np.abs(res - ref).max() <= tol * scale, (cls, f32, np.abs(res - ref).max())
+
+
+def test_boys_evaluator(hostlib, port):
+    xs = [0.0, 1e-9, 0.01, 0.03125, 0.5, 1.0, 2.5, 5.0, 10.0, 20.0, 33.0, 39.99, 40.0, 41.0, 50.0, 100.0, 1e3]
+    for m in range(0, 12):
+        for x in xs:
+            ex = port.boys_exact(m, x)
+            assert abs(hostlib.host_boys(m, x, 0) - ex) <= 4e-15 * ex, (m, x)
+            assert abs(hostlib.host_boys(m, x, 1) - ex) <= 2e-6 * ex, (m, x)

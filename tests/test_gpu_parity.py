@@ -1,0 +1,293 @@
+"""GPU parity: librchem_gpu.so through its C ABI against the oracle.
+
+Tolerances: 1e-12 absolute per integral / matrix element for the FP64 path
+(the target the hot path is built to); the reference's own Boys function is
+only ~1e-7 accurate, so the as-shipped numbers are compared at that level.
+"""
+import itertools
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_npz
+
+pytestmark = pytest.mark.gpu
+
+
+# ---- cints-compatible scalar entry points ---------------------------------
+def test_scalar_eri_golden(gpu):
+    from rchem_gb300 import cints
+    from test_oracle import ERI_GEOM as g
+    from test_oracle import ERI_GOLDEN
+
+    for pw, ref in ERI_GOLDEN:
+        v = cints.coulomb(g["za"], g["zb"], g["zc"], g["zd"], g["ra"], g["rb"], g["rc"], g["rd"], pw)
+        assert abs(v - ref) < 1e-15, (pw, v, ref)
+
+
+def test_scalar_onee_golden(gpu):
+    from rchem_gb300 import cints
+    from test_oracle import KIN_GOLDEN, NUC_GOLDEN, OVL_GOLDEN, RA, RB, RC
+
+    for pw, ref in OVL_GOLDEN:
+        assert abs(cints.overlap(1.8, 2.8, RA, RB, pw) - ref) < 1e-16
+    for pw, ref in KIN_GOLDEN:
+        assert abs(cints.kinetic(1.8, 2.0, RA, RB, pw) - ref) < 1e-15
+    for pw, ref in NUC_GOLDEN:
+        assert abs(cints.nuclear(1.8, 2.0, RA, RB, RC, pw) - ref) < 1e-15
+
+
+def test_eri_batch_vs_reference_fixture(gpu, golden_eri):
+    from rchem_gb300 import cints
+
+    quartets = [[(it["R"][k], 1.0, it["alpha"][k], it["powers"][k]) for k in range(4)] for it in golden_eri]
+    v = cints.eri_batch(quartets)
+    ex = np.array([it["exact"] for it in golden_eri])
+    sh = np.array([it["shipped"] for it in golden_eri])
+    assert np.abs(v - ex).max() < 1e-12
+    # against the reference as shipped: its NR Boys function limits agreement
+    assert np.all(np.abs(v - sh) <= 2e-7 * np.maximum(np.abs(sh), 1e-3))
+
+
+def test_onee_batch_vs_reference_fixture(gpu, golden_onee):
+    from rchem_gb300 import cints
+
+    for it in golden_onee:
+        a, pw = it["alpha"], it["pa"] + it["pb"]
+        assert abs(cints.overlap(a[0], a[1], it["A"], it["B"], pw) - it["S_exact"]) < 1e-13
+        assert abs(cints.kinetic(a[0], a[1], it["A"], it["B"], pw) - it["T_exact"]) < 1e-12
+        assert abs(cints.nuclear(a[0], a[1], it["A"], it["B"], it["C"], pw) - it["V_exact"]) < 1e-12
+
+
+def test_boys_batch(gpu, port):
+    from rchem_gb300 import cints
+
+    ms, xs = [], []
+    for m in range(0, 13):
+        for x in (0.0, 1e-12, 1e-3, 0.0312, 0.7, 3.3, 9.9, 17.0, 29.0, 39.97, 40.0, 40.5, 55.0, 120.0, 5000.0):
+            ms.append(m)
+            xs.append(x)
+    ex = np.array([port.boys_exact(m, x) for m, x in zip(ms, xs)])
+    v64 = cints.boys_batch(ms, xs, 64)
+    v32 = cints.boys_batch(ms, xs, 32)
+    assert np.all(np.abs(v64 - ex) <= 4e-15 * ex)
+    assert np.all(np.abs(v32 - ex) <= 2e-6 * ex)
+    assert abs(cints.fgamma(2, 1.5) - port.boys_exact(2, 1.5)) < 1e-16
+
+
+def test_contr_coulomb(gpu, port):
+    import ctypes as C
+
+    from rchem_gb300 import _lib
+
+    L = _lib.lib()
+    e = np.array([1.3, 0.4])
+    c = np.array([0.6, 0.5])
+    nrm = np.array([port.pgto_norm(x, 1, 0, 0) for x in e])
+    args = []
+    for R in ([0, 0, 0], [0, 0, 1.4], [1.0, 0, 0], [0, 1.2, 0.3]):
+        args += [2, e.ctypes.data, c.ctypes.data, nrm.ctypes.data, *R, 1, 0, 0]
+    v = L.contr_coulomb(*args)
+    ref = 0.0
+    for i, j, k, l in itertools.product(range(2), repeat=4):
+        ref += c[i] * c[j] * c[k] * c[l] * port.coulomb_repulsion(
+            [0, 0, 0], nrm[i], [1, 0, 0], e[i], [0, 0, 1.4], nrm[j], [1, 0, 0], e[j],
+            [1.0, 0, 0], nrm[k], [1, 0, 0], e[k], [0, 1.2, 0.3], nrm[l], [1, 0, 0], e[l])
+    assert abs(v - ref) < 1e-13
+
+
+# ---- matrix API against the reference-generated fixtures ---------------------
+@pytest.mark.parametrize("tag,name", [("h2o_sto3g", "sto-3g-fit"), ("h2o_631g", "6-31g-fit"),
+                                      ("h2o_631gs", "6-31gs-fit")])
+def test_matrices_vs_reference_fixture(gpu, tag, name):
+    import rchem_gb300 as rc
+
+    g = load_npz(tag)
+    Z, R = rc.geometry.water_monomer()
+    with rc.Basis(Z, R, name) as b:
+        np.testing.assert_allclose(rc.S(b), g["S"], atol=1e-12, rtol=0)
+        np.testing.assert_allclose(rc.T(b), g["T"], atol=1e-12, rtol=0)
+        np.testing.assert_allclose(rc.V(b, R, Z), g["V"], atol=1e-12, rtol=0)
+        n = b.nbf
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, g["D"], schwarz_tau=0.0)  # no screening: exact semantics
+        np.testing.assert_allclose(J, g["J"], atol=1e-12, rtol=0)
+        np.testing.assert_allclose(K, g["K"], atol=1e-12, rtol=0)
+        rc.JK_direct(J, K, b, g["D"])  # Schwarz 1e-12
+        np.testing.assert_allclose(J, g["J"], atol=1e-11, rtol=0)
+        np.testing.assert_allclose(K, g["K"], atol=1e-11, rtol=0)
+        if "I" in g:
+            I = rc.build_I(b)
+            np.testing.assert_allclose(I, g["I"], atol=1e-12, rtol=0)
+            Ji, Ki = rc.JK_inmem(I, g["D"])
+            np.testing.assert_allclose(Ji, g["J"], atol=1e-12, rtol=0)
+            np.testing.assert_allclose(Ki, g["K"], atol=1e-12, rtol=0)
+
+
+def test_device_pointers_and_torch_stream(gpu):
+    torch = pytest.importorskip("torch")
+    import rchem_gb300 as rc
+
+    g = load_npz("h2o_631g")
+    Z, R = rc.geometry.water_monomer()
+    with rc.Basis(Z, R, "6-31g-fit") as b:
+        s = torch.cuda.Stream()
+        b.set_stream(s.cuda_stream)
+        D = torch.from_numpy(g["D"]).cuda()
+        J = torch.empty_like(D)
+        K = torch.empty_like(D)
+        with torch.cuda.stream(s):
+            rc.JK_direct(J, K, b, D, schwarz_tau=0.0)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(J.cpu().numpy(), g["J"], atol=1e-12, rtol=0)
+        np.testing.assert_allclose(K.cpu().numpy(), g["K"], atol=1e-12, rtol=0)
+        Sd = rc.S(b, device=True)
+        np.testing.assert_allclose(Sd.cpu().numpy(), g["S"], atol=1e-12, rtol=0)
+
+
+def _sym_density(rng, n, scale=0.2):
+    X = rng.normal(size=(n, n)) * scale
+    return X @ X.T / n
+
+
+@pytest.mark.parametrize("name,nw,box", [("6-31gss-fit", 2, 4.5), ("6-31gs-fit", 2, 5.0)])
+def test_jk_vs_oracle_dimer(gpu, oracle_mod, name, nw, box):
+    """All 21 classes in play (d on O, p on H): GPU vs the 8-fold oracle."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    Z, R = rc.geometry.water_cluster(nw, box, seed=11)
+    ob = O.expand_basis(Z, R, rc.load_bse(name))
+    D = _sym_density(np.random.default_rng(1), ob.n)
+    Jr, Kr = O.JK_sym(ob, D)
+    with rc.Basis(Z, R, name) as b:
+        n = b.nbf
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, D, schwarz_tau=0.0)
+        assert np.abs(J - Jr).max() < 1e-12
+        assert np.abs(K - Kr).max() < 1e-12
+        rc.JK_direct(J, K, b, D)
+        assert np.abs(J - Jr).max() < 1e-10
+        assert np.abs(K - Kr).max() < 1e-10
+        np.testing.assert_allclose(rc.S(b), O.S(ob), atol=1e-12, rtol=0)
+        np.testing.assert_allclose(rc.T(b), O.T(ob), atol=1e-12, rtol=0)
+        np.testing.assert_allclose(rc.V(b), O.V(ob, R, Z), atol=1e-11, rtol=0)
+
+
+def test_jk_full_size_h2o8_sampled(gpu, oracle_mod):
+    """(H2O)8 in the 6-31G-shaped basis (104 functions): sampled elements of J
+    and K straight from their definitions (basis.rs:406-417) on the CPU, plus
+    size-independent properties of the whole matrices."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    bname, Z, R = rc.geometry.config("h2o8_631g")
+    ob = O.expand_basis(Z, R, rc.load_bse(bname))
+    D = _sym_density(np.random.default_rng(2), ob.n)
+    with rc.Basis(Z, R, bname) as b:
+        n = b.nbf
+        assert n == 104
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, D)
+        st = b.stats()
+        # properties: symmetry, J linear in D, Tr(D J) = sum (mn|ls) D_mn D_ls >= 0
+        assert np.abs(J - J.T).max() == 0.0 and np.abs(K - K.T).max() == 0.0
+        assert float(np.sum(D * J)) > 0.0
+        J2, K2 = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J2, K2, b, 2.0 * D)
+        np.testing.assert_allclose(J2, 2.0 * J, atol=1e-11, rtol=0)
+        np.testing.assert_allclose(K2, 2.0 * K, atol=1e-11, rtol=0)
+        # sampled elements
+        mus = [0, 5, 40, 77, 103]
+        nus = [0, 17, 40, 3, 60]
+        Je, Ke = O.JK_elements(ob, D, mus, nus)
+        for k in range(len(mus)):
+            assert abs(J[mus[k], nus[k]] - Je[k]) < 1e-10
+            assert abs(K[mus[k], nus[k]] - Ke[k]) < 1e-10
+        assert st["quartets_fp64"] > 0 and st["quartets_fp32"] == 0
+
+
+def test_mixed_precision_close_to_fp64(gpu):
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o8_631g")
+    D = _sym_density(np.random.default_rng(2), 104)
+    with rc.Basis(Z, R, bname) as b:
+        n = b.nbf
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        Jm, Km = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, D)
+        rc.JK_direct(Jm, Km, b, D, fp32_tau=1e-6)
+        st = b.stats()
+        assert st["quartets_fp32"] > 0
+        # every FP32 quartet is bounded by 1e-6: per-element error well below 1e-8
+        assert np.abs(Jm - J).max() < 1e-8
+        assert np.abs(Km - K).max() < 1e-8
+        assert abs(float(np.sum(D * (Jm - J)))) < 1e-8
+
+
+def test_scf_energy_with_gpu_fock(gpu, oracle_mod):
+    """rchem.rs:40-89 driven by the GPU J/K and S/T/V: the fixture energy."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    g = load_npz("h2o_sto3g")
+    Z, R = rc.geometry.water_monomer()
+    with rc.Basis(Z, R, "sto-3g-fit") as b:
+        n = b.nbf
+        H = rc.T(b) + rc.V(b)
+        X = O.symm_orthog(rc.S(b))
+        _, Cp = np.linalg.eigh(X.T @ H @ X)
+        D = O.build_density(X @ Cp, 5)
+        e = O.elec_energy(D, H, H)
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        for _ in range(200):
+            rc.JK_direct(J, K, b, D)
+            F = H + 2 * J - K
+            _, Cp = np.linalg.eigh(X.T @ F @ X)
+            D = O.build_density(X @ Cp, 5)
+            e_old, e = e, O.elec_energy(D, H, F)
+            if abs(e - e_old) < 1e-12:
+                break
+        assert abs(e - float(g["e_elec"])) < 1e-10
+
+
+# ---- edge cases ---------------------------------------------------------
+def test_single_s_function_atom(gpu, port):
+    import rchem_gb300 as rc
+
+    Z = np.array([1])
+    R = np.zeros((1, 3))
+    doc = {"elements": {"1": {"electron_shells": [
+        {"function_type": "gto", "region": "", "angular_momentum": [0], "exponents": ["0.8"], "coefficients": [["1.0"]]}]}}}
+    with rc.Basis(Z, R, doc) as b:
+        assert b.nbf == 1
+        S = rc.S(b)
+        assert abs(S[0, 0] - 1.0) < 1e-14
+        J, K = np.zeros((1, 1)), np.zeros((1, 1))
+        rc.JK_direct(J, K, b, np.ones((1, 1)))
+        ssss = port.coulomb_repulsion([0, 0, 0], port.pgto_norm(0.8, 0, 0, 0), [0, 0, 0], 0.8, [0, 0, 0],
+                                      port.pgto_norm(0.8, 0, 0, 0), [0, 0, 0], 0.8, [0, 0, 0],
+                                      port.pgto_norm(0.8, 0, 0, 0), [0, 0, 0], 0.8, [0, 0, 0],
+                                      port.pgto_norm(0.8, 0, 0, 0), [0, 0, 0], 0.8)
+        assert abs(J[0, 0] - ssss) < 1e-14 and abs(K[0, 0] - ssss) < 1e-14
+
+
+def test_zero_density_and_errors(gpu):
+    import rchem_gb300 as rc
+
+    Z, R = rc.geometry.water_monomer()
+    with rc.Basis(Z, R, "6-31gs-fit") as b:
+        n = b.nbf
+        J, K = np.ones((n, n)), np.ones((n, n))
+        rc.JK_direct(J, K, b, np.zeros((n, n)))
+        assert not J.any() and not K.any()
+        with pytest.raises(ValueError):
+            rc.JK_direct(J, K, b, np.zeros((n + 1, n + 1)))
+    bad = {"elements": {"8": {"electron_shells": [
+        {"function_type": "gto", "region": "", "angular_momentum": [3], "exponents": ["1.0"], "coefficients": [["1.0"]]}]},
+        "1": {"electron_shells": [{"function_type": "gto", "region": "", "angular_momentum": [0], "exponents": ["1.0"],
+                                   "coefficients": [["1.0"]]}]}}}
+    with pytest.raises(rc.RchemError, match="l=3"):
+        rc.Basis(Z, R, bad)

@@ -1,0 +1,173 @@
+"""Host-side logic without a GPU: AO ordering, basis files, geometry, the
+C-ABI library's exported symbols."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_ijk_list_order():
+    """src/shell.rs:44-60."""
+    import oracle
+
+    assert oracle.ijk_list(3) == [(3, 0, 0), (2, 1, 0), (2, 0, 1), (1, 2, 0), (1, 1, 1), (1, 0, 2), (0, 3, 0),
+                                  (0, 2, 1), (0, 1, 2), (0, 0, 3)]
+
+
+def test_shell4_order():
+    """src/shell.rs:62-86: get_shell4(2,0,0,1) is the product order of get_ijk_list."""
+    import itertools
+
+    import oracle
+
+    comps = [list(a) + list(b) + list(c) + list(d) for a, b, c, d in
+             itertools.product(oracle.ijk_list(2), oracle.ijk_list(0), oracle.ijk_list(0), oracle.ijk_list(1))]
+    assert comps[0] == [2, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0]
+    assert comps[4] == [1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0]
+    assert comps[-1] == [0, 0, 2, 0, 0, 0, 0, 0, 0, 0, 0, 1]
+    assert len(comps) == 18
+
+
+def test_generator_cartesian_order_matches_reference():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("g", os.path.join(ROOT, "rchem_gb300", "csrc", "gen_eri.py"))
+    g = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(g)
+    import oracle
+
+    for l in range(5):
+        assert g.ijk_list(l) == oracle.ijk_list(l)
+    assert abs(g.comp_norm((1, 1, 0)) - 3 ** 0.5) < 1e-15
+    assert g.comp_norm((2, 0, 0)) == 1.0
+
+
+@pytest.mark.parametrize("name,nbf_h2o,nprim", [("sto-3g-fit", 7, 21), ("6-31g-fit", 13, 30), ("6-31gs-fit", 19, 36),
+                                                ("6-31gss-fit", 25, 42)])
+def test_basis_sets_shapes(name, nbf_h2o, nprim):
+    from rchem_gb300 import bse, geometry
+
+    Z, R = geometry.water_monomer()
+    sh = bse.expand_shells(Z, bse.load_bse(name))
+    assert sh.nbf == nbf_h2o
+    # P = sum over functions of primitives
+    P = sum(((l + 1) * (l + 2) // 2) * n for l, n in zip(sh.l, sh.nprim))
+    assert P == nprim
+
+
+def test_expand_shells_matches_oracle_expansion():
+    import oracle
+
+    from rchem_gb300 import bse, geometry
+
+    Z, R = geometry.water_cluster(2, 5.0, seed=3)
+    doc = bse.load_bse("6-31gss-fit")
+    sh = bse.expand_shells(Z, doc)
+    ob = oracle.expand_basis(Z, R, doc)
+    # AO-by-AO: same atom, same exponents
+    ao = 0
+    off = 0
+    for s in range(len(sh.l)):
+        for k in range((sh.l[s] + 1) * (sh.l[s] + 2) // 2):
+            assert ob.atom[ao] == sh.atom[s]
+            assert sum(ob.powers[ao]) == sh.l[s]
+            np.testing.assert_array_equal(ob.exps[ob.prim_off[ao]:ob.prim_off[ao] + ob.nprim[ao]],
+                                          sh.exps[off:off + sh.nprim[s]])
+            ao += 1
+        off += sh.nprim[s]
+    assert ao == ob.n
+
+
+def test_config_sizes():
+    from rchem_gb300 import bse, geometry
+
+    sizes = {"h2o_sto3g": 7, "h2o8_631g": 104, "h2o4_631gss": 100, "h2o32_631gs": 608}
+    for name, nbf in sizes.items():
+        b, Z, R = geometry.config(name)
+        assert bse.expand_shells(Z, bse.load_bse(b)).nbf == nbf
+        O = R[Z == 8]
+        d = np.linalg.norm(O[:, None] - O[None], axis=-1) + np.eye(len(O)) * 1e9
+        assert d.min() >= 2.7 * geometry.ANGSTROM_TO_BOHR - 1e-9
+
+
+def test_geometry_seeded_and_monomer():
+    from rchem_gb300 import geometry
+
+    Z, R = geometry.water_monomer()
+    r = np.linalg.norm(R[1] - R[0]) / geometry.ANGSTROM_TO_BOHR
+    assert abs(r - 0.957) < 1e-12
+    v1, v2 = R[1] - R[0], R[2] - R[0]
+    ang = np.degrees(np.arccos(v1 @ v2 / np.linalg.norm(v1) / np.linalg.norm(v2)))
+    assert abs(ang - 104.5) < 1e-9
+    a = geometry.water_cluster(8, 9.0, seed=1)[1]
+    b = geometry.water_cluster(8, 9.0, seed=1)[1]
+    np.testing.assert_array_equal(a, b)
+    batch = geometry.water_batch(512, seed=5)
+    sizes = [len(z) // 3 for z, _ in batch]
+    assert len(batch) == 512 and sizes.count(1) == 172 and sizes.count(2) == 170 and sizes.count(3) == 170
+
+
+def test_xyz_roundtrip(tmp_path):
+    from rchem_gb300 import bse, geometry
+
+    Z, R = geometry.water_monomer()
+    p = tmp_path / "w.xyz"
+    bse.write_xyz(p, Z, R)
+    Z2, R2 = bse.read_xyz(p)
+    np.testing.assert_array_equal(Z, Z2)
+    np.testing.assert_allclose(R, R2, atol=1e-11)
+    # the reference's own Crawford water file format (bohr, element symbols)
+    Z3, R3 = bse.read_xyz(str(p), angstrom=True)
+    np.testing.assert_allclose(R3, R2 * bse.ANGSTROM_TO_BOHR)
+
+
+def _declared_symbols():
+    names = set()
+    for h in sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?(?:int|double|char\s*\*|const char\s*\*)\s*\*?\s*(\w+)\s*\(", src,
+                             flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    """The C-ABI library loads on the host (no GPU calls) and exports every
+    entry point the headers declare."""
+    from rchem_gb300 import _lib, build
+
+    build.build()
+    declared = _declared_symbols()
+    assert declared == set(_lib.exported_symbols())
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True, check=True)
+    exported = {ln.split()[-1] for ln in out.stdout.splitlines() if " T " in ln}
+    missing = declared - exported
+    assert not missing, missing
+    L = _lib.lib()  # dlopen succeeds without a GPU
+    assert L.rchem_abi_version() == 1
+
+
+def test_invalid_arguments_rejected_without_gpu():
+    """Argument validation happens before any device call."""
+    import ctypes as C
+
+    from rchem_gb300 import _lib, build
+
+    build.build()
+    L = _lib.lib()
+    h = C.c_void_p()
+    Z = np.array([8], np.int32)
+    R = np.array([0.0, 0.0, np.nan])
+    one = np.array([0], np.int32)
+    e = np.array([1.0])
+    rc = L.rchem_basis_create(C.byref(h), 1, Z.ctypes.data, R.ctypes.data, 1, one.ctypes.data, one.ctypes.data,
+                              np.array([1], np.int32).ctypes.data, e.ctypes.data, e.ctypes.data)
+    assert rc == _lib.RCHEM_ERR_INVALID
+    assert b"not finite" in L.rchem_last_error()
+    rc = L.rchem_jk_direct(None, None, None, None, None)
+    assert rc == _lib.RCHEM_ERR_INVALID
