@@ -4,29 +4,40 @@
 // function (libpyquante2/cints.c:302-373, relative error ~1e-7).  Here:
 //   T < BOYS_TMAX: Taylor expansion about the nearest grid point T_i = i*h,
 //     F_m(T_i + d) = sum_k F_{m+k}(T_i) (-d)^k / k!,  |d| <= h/2,
-//     with NTAY terms (8 in FP64: remainder < 3e-17 F; 4 in FP32: < 5e-8 F);
-//     either for every m ("direct") or for m = L only, followed by the
-//     downward recursion F_m = (2T F_{m+1} + e^{-T}) / (2m+1), with
-//     e^{-T} = e^{-T_i} e^{-d} from the same Taylor multipliers;
+//     with NTAY terms (8 in FP64: remainder < 3e-17 F; 4 in FP32: < 5e-8 F).
+//     The tables hold the coefficients already divided by k!, one sub-table per
+//     m (and one for e^{-T} = e^{-T_i} e^{-d}), so an evaluation is a pure
+//     Horner chain in x = -d: NTAY-1 fused multiply-adds.  Small L evaluates
+//     every F_m that way ("direct"); larger L evaluates F_L and e^{-T} and runs
+//     the downward recursion F_m = (2T F_{m+1} + e^{-T}) / (2m+1).
 //   T >= BOYS_TMAX: F_0 = sqrt(pi/T)/2 (erfc(sqrt T) < 4e-19 there) and the
 //     upward recursion F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T), stable for T > m.
 // All F values come out multiplied by the caller's prefactor.
-// The grid tables are filled on the host (rchem_gpu.cu) from the exact power
-// series, in double, at exactly the T_i values used here.
+// The grid index uses the add-2^52+2^51 rounding, so no int<->double
+// conversions run on the (narrow) FP64 pipe.
 #pragma once
+#include <math.h>
+#include <string.h>
+
 #include "rchem_types.h"
 
 // h = 1/16 is exact in binary, so T_i = i*h and d = T - T_i are exact in both
 // precisions and the host tables are built at exactly the device's grid points.
 #define BOYS_NGRID 641   // rows i = 0..640 (nearest-point rounding reaches 640 just below T = 40)
-#define BOYS_NCOL 24
+#define BOYS_MMAX 16     // F_0 .. F_16
+#define BOYS_NSUB (BOYS_MMAX + 2)  // sub-table 0 = e^{-T}, sub-table m+1 = F_m
 #define BOYS_TMAX 40.0
 #define BOYS_INVH 16.0
 #define BOYS_H 0.0625
+#define BOYS_NT64 8
+#define BOYS_NT32 4
 
 template <typename R> struct BoysPrec;
-template <> struct BoysPrec<double> { static constexpr int NTAY = 8; };
-template <> struct BoysPrec<float> { static constexpr int NTAY = 4; };
+template <> struct BoysPrec<double> { static constexpr int NTAY = BOYS_NT64; };
+template <> struct BoysPrec<float> { static constexpr int NTAY = BOYS_NT32; };
+
+// table element (sub-table s, grid row i, Taylor order k)
+RCHEM_HD inline int boys_idx(int s, int i, int k, int nt) { return (s * BOYS_NGRID + i) * nt + k; }
 
 RCHEM_HD inline double rchem_rsqrt(double x) {
 #ifdef __CUDA_ARCH__
@@ -47,6 +58,9 @@ RCHEM_HD inline float rchem_rsqrt(float x) {
 // so single precision is ample there (and it underflows harmlessly past 87).
 RCHEM_HD inline float rchem_expf(float x) { return expf(x); }
 
+RCHEM_HD inline double rchem_fma(double a, double b, double c) { return fma(a, b, c); }
+RCHEM_HD inline float rchem_fma(float a, float b, float c) { return fmaf(a, b, c); }
+
 template <typename R>
 RCHEM_HD inline R rchem_ldg(const R *p) {
 #ifdef __CUDA_ARCH__
@@ -56,38 +70,62 @@ RCHEM_HD inline R rchem_ldg(const R *p) {
 #endif
 }
 
-// F[0..L] = pref * F_m(T).
-template <int L, bool DIRECT, typename R>
-RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, const R *__restrict__ etab, R *F) {
+// nearest grid row i and x = T_i - T, for 0 <= T < BOYS_TMAX
+RCHEM_HD inline void boys_grid(double T, int &i, double &x) {
+    const double magic = 6755399441055744.0;  // 2^52 + 2^51
+    const double t = fma(T, BOYS_INVH, magic);
+#ifdef __CUDA_ARCH__
+    i = __double2loint(t);
+#else
+    long long bits;
+    memcpy(&bits, &t, sizeof(bits));
+    i = (int)(bits & 0xffffffffLL);
+#endif
+    x = fma(t - magic, BOYS_H, -T);
+}
+RCHEM_HD inline void boys_grid(float T, int &i, float &x) {
+    const float magic = 12582912.0f;  // 2^23 + 2^22
+    const float t = fmaf(T, (float)BOYS_INVH, magic);
+#ifdef __CUDA_ARCH__
+    i = __float_as_int(t) - __float_as_int(magic);
+#else
+    int bits, mb;
+    memcpy(&bits, &t, sizeof(bits));
+    memcpy(&mb, &magic, sizeof(mb));
+    i = bits - mb;
+#endif
+    x = fmaf(t - magic, (float)BOYS_H, -T);
+}
+
+template <typename R>
+RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
     constexpr int NT = BoysPrec<R>::NTAY;
+    const R *c = tab + boys_idx(s, i, 0, NT);
+    R acc = rchem_ldg(c + NT - 1);
+#pragma unroll
+    for (int k = NT - 2; k >= 0; --k) acc = rchem_fma(acc, x, rchem_ldg(c + k));
+    return acc;
+}
+
+// Direct evaluation of every F_m is cheaper up to this L.
+#define BOYS_DIRECT_MAXL 1
+
+// F[0..L] = pref * F_m(T).
+template <int L, typename R>
+RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
     if (T < R(BOYS_TMAX)) {
-        const int i = (int)(T * R(BOYS_INVH) + R(0.5));
-        const R d = T - R(i) * R(BOYS_H);
-        const R *row = tab + i * BOYS_NCOL;
-        R mult[NT];
+        int i;
+        R x;
+        boys_grid(T, i, x);
+        if (L <= BOYS_DIRECT_MAXL) {
 #pragma unroll
-        for (int k = 1; k < NT; ++k) mult[k] = -d * (R(1) / R(k));
-        if (DIRECT) {
-#pragma unroll
-            for (int m = 0; m <= L; ++m) {
-                R acc = rchem_ldg(row + m + NT - 1);
-#pragma unroll
-                for (int k = NT - 1; k >= 1; --k) acc = rchem_ldg(row + m + k - 1) + acc * mult[k];
-                F[m] = acc * pref;
-            }
+            for (int m = 0; m <= L; ++m) F[m] = boys_horner(tab, m + 1, i, x) * pref;
         } else {
-            R acc = rchem_ldg(row + L + NT - 1);
-#pragma unroll
-            for (int k = NT - 1; k >= 1; --k) acc = rchem_ldg(row + L + k - 1) + acc * mult[k];
-            // e^{-T} = e^{-T_i} * e^{-d}; Taylor of e^{-d} with the multipliers mult[k] = -d/k
-            R ex = R(1);
-#pragma unroll
-            for (int k = NT - 1; k >= 1; --k) ex = R(1) + ex * mult[k];
-            ex *= rchem_ldg(etab + i) * pref;
-            F[L] = acc * pref;
+            const R ex = boys_horner(tab, 0, i, x) * pref;
+            F[L] = boys_horner(tab, L + 1, i, x) * pref;
             const R T2 = T + T;
 #pragma unroll
-            for (int m = L - 1; m >= 0; --m) F[m] = (T2 * F[m + 1] + ex) * (R(1) / R(2 * m + 1));
+            for (int m = L - 1; m >= 0; --m) F[m] = rchem_fma(T2, F[m + 1], ex) * (R(1) / R(2 * m + 1));
         }
     } else {
         const R rs = rchem_rsqrt(T);
@@ -99,26 +137,51 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, const R *
     }
 }
 
-// Runtime-L variant for the generic (non-class) kernels.
+// Runtime-L variant for the generic (non-class) kernels; L <= BOYS_MMAX.
 template <typename R>
 RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab, R *F) {
-    constexpr int NT = BoysPrec<R>::NTAY;
     if (T < R(BOYS_TMAX)) {
-        const int i = (int)(T * R(BOYS_INVH) + R(0.5));
-        const R d = T - R(i) * R(BOYS_H);
-        const R *row = tab + i * BOYS_NCOL;
-        R mult[NT];
-        for (int k = 1; k < NT; ++k) mult[k] = -d * (R(1) / R(k));
-        for (int m = 0; m <= L; ++m) {
-            R acc = rchem_ldg(row + m + NT - 1);
-            for (int k = NT - 1; k >= 1; --k) acc = rchem_ldg(row + m + k - 1) + acc * mult[k];
-            F[m] = acc * pref;
-        }
+        int i;
+        R x;
+        boys_grid(T, i, x);
+        for (int m = 0; m <= L; ++m) F[m] = boys_horner(tab, m + 1, i, x) * pref;
     } else {
         const R rs = rchem_rsqrt(T);
         const R inv2T = R(0.5) * rs * rs;
         const R ex = R(rchem_expf(-(float)T)) * pref;
         F[0] = R(0.88622692545275801365) * rs * pref;
         for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;
+    }
+}
+
+// Host: fill the FP64 and FP32 tables (sizes boys_table_size(nt)).
+inline size_t boys_table_size(int nt) { return (size_t)BOYS_NSUB * BOYS_NGRID * nt; }
+
+inline double boys_series_host(int m, double x) {
+    // F_m(x) = e^{-x} sum_k (2x)^k / prod_{i=0..k} (2m+2i+1): every term positive
+    double term = 1.0 / (2 * m + 1), sum = term;
+    for (int k = 1; k < 2000; ++k) {
+        term *= 2.0 * x / (2 * m + 2 * k + 1);
+        sum += term;
+        if (term < sum * 1e-18) break;
+    }
+    return exp(-x) * sum;
+}
+
+inline void boys_fill_tables(double *t64, float *t32) {
+    double fk[32];
+    fk[0] = 1.0;
+    for (int k = 1; k < 32; ++k) fk[k] = fk[k - 1] * k;
+    for (int i = 0; i < BOYS_NGRID; ++i) {
+        const double T = (double)i * BOYS_H;  // exact: h = 1/16
+        double F[BOYS_MMAX + BOYS_NT64 + 1];
+        for (int m = 0; m <= BOYS_MMAX + BOYS_NT64; ++m) F[m] = boys_series_host(m, T);
+        const double e = exp(-T);
+        for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(0, i, k, BOYS_NT64)] = e / fk[k];
+        for (int k = 0; k < BOYS_NT32; ++k) t32[boys_idx(0, i, k, BOYS_NT32)] = (float)(e / fk[k]);
+        for (int m = 0; m <= BOYS_MMAX; ++m) {
+            for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(m + 1, i, k, BOYS_NT64)] = F[m + k] / fk[k];
+            for (int k = 0; k < BOYS_NT32; ++k) t32[boys_idx(m + 1, i, k, BOYS_NT32)] = (float)(F[m + k] / fk[k]);
+        }
     }
 }

@@ -1,14 +1,14 @@
 // eri_kernel.cuh -- the HGP ERI class kernel and its fused epilogues.
 //
-// Work unit: one warp = one bra shell pair against up to 32 ket shell pairs
-// taken from one pair group (same l_C, l_D and primitive-pair count, sorted by
-// Schwarz bound), one ket pair per lane.  Every lane therefore runs the same
-// primitive loop trip counts.  Per primitive quartet: Boys function, the
-// generated Obara--Saika VRR into the [e0|f0] contraction accumulators (held in
+// Work unit: one warp = 32 consecutive quartets of one (bra pair group, ket
+// pair group) combination -- same angular momenta and primitive-pair counts on
+// both sides, so every lane runs the same primitive-loop trip counts; lanes
+// may straddle bra pairs.  Per primitive quartet: Boys function, the generated
+// Obara--Saika VRR into the [e0|f0] contraction accumulators (held in
 // registers); per contracted quartet: the generated HRR, then
 //   EPI_JK    -- the 8-fold-symmetric J/K scatter (contracted with D in
-//                registers, bra J block reduced across the warp with shuffles,
-//                everything else added with FP64 atomics into J-hat / K-hat),
+//                registers, then added with FP64 atomics into J-hat / K-hat:
+//                the additions run in L2, not on the SM's narrow FP64 pipe),
 //   EPI_STORE -- the dense ERI tensor (all 8 index permutations),
 //   EPI_DIAG  -- the Schwarz diagonal max |(ab|ab)| (bra = ket = lane's pair).
 //
@@ -45,22 +45,14 @@ template <> struct PrimLoad<float> {
 template <typename R> struct Tabs;
 template <> struct Tabs<double> {
     static __device__ __forceinline__ const double *boys(const EriArgs &a) { return a.boys64; }
-    static __device__ __forceinline__ const double *ex(const EriArgs &a) { return a.exp64; }
     static __device__ __forceinline__ double dens(const EriArgs &a, int i) { return __ldg(a.D + i); }
     static __device__ __forceinline__ void ab(const ShellPair &s, double *v) { v[0] = s.AB[0]; v[1] = s.AB[1]; v[2] = s.AB[2]; }
 };
 template <> struct Tabs<float> {
     static __device__ __forceinline__ const float *boys(const EriArgs &a) { return a.boys32; }
-    static __device__ __forceinline__ const float *ex(const EriArgs &a) { return a.exp32; }
     static __device__ __forceinline__ float dens(const EriArgs &a, int i) { return __ldg(a.D32 + i); }
     static __device__ __forceinline__ void ab(const ShellPair &s, float *v) { v[0] = s.AB32[0]; v[1] = s.AB32[1]; v[2] = s.AB32[2]; }
 };
-
-template <typename R> __device__ __forceinline__ R warp_sum(R v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 template <int LA, int LB, int LC, int LD, typename R, int EPI>
 __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
@@ -70,9 +62,18 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
     if (w >= a.ntasks) return;  // warp-uniform
     const EriTask t = a.tasks[w];
-    const bool active = lane < t.nket;
-    const int kidx = t.ket0 + (active ? lane : 0);
-    const int bidx = (EPI == EPI_DIAG) ? kidx : t.bra;
+    const int lg = (t.nq_lg >> 8) & 7, nq = t.nq_lg & 255;
+    const int G = 1 << lg, r = lane & (G - 1), qi = lane >> lg;
+    const bool active = qi < nq;
+    // walk the segment chain to this lane's quartet (inactive lanes repeat lane 0's)
+    int sg = t.seg, off = t.off + (active ? qi : 0);
+    EriSeg seg = a.segs[sg];
+    while (off >= seg.count) {
+        off -= seg.count;
+        seg = a.segs[++sg];
+    }
+    const int bidx = seg.bra;
+    const int kidx = seg.ket0 + off;
     const ShellPair bp = a.pairs[bidx];
     const ShellPair kp = a.pairs[kidx];
 
@@ -81,26 +82,36 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     for (int i = 0; i < C::NE * C::NF; ++i) acc[i] = R(0);
 
     const R *btab = Tabs<R>::boys(a);
-    const R *etab = Tabs<R>::ex(a);
-    for (int ia = 0; ia < bp.npp; ++ia) {
-        R p, ohp, P[3], PA[3], Kab;
+    // one primitive quartet: Boys function, then the VRR into acc
+    auto prim = [&](const R p, const R ohp, const R *P, const R *PA, const R Kab, const R q, const R ohq,
+                    const R *Q, const R *QC, const R Kcd) {
+        const R pq = p + q;
+        const R rs = rchem_rsqrt(pq);
+        const R ipq = rs * rs;
+        const R PQx = P[0] - Q[0], PQy = P[1] - Q[1], PQz = P[2] - Q[2];
+        const R qi_ = q * ipq, pi_ = p * ipq;
+        const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
+        const R pref = Kab * Kcd * rs;
+        R F[L + 1];
+        boys_eval<L, R>(T, pref, btab, F);
+        C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi_ * PQx, -qi_ * PQy, -qi_ * PQz, QC[0], QC[1], QC[2],
+                           pi_ * PQx, pi_ * PQy, pi_ * PQz, ohp, ohq, R(0.5) * ipq, qi_, pi_);
+    };
+    // the G lanes of a quartet split its npp_bra x npp_ket primitive quartets
+    // (one flat loop: a single inlined copy of the VRR), then reduce
+    const int nk = kp.npp, ntot = bp.npp * nk;
+    for (int tq = r; tq < ntot; tq += G) {
+        const int ia = tq / nk, ic = tq - ia * nk;
+        R p, ohp, P[3], PA[3], Kab, q, ohq, Q[3], QC[3], Kcd;
         PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, P, PA, Kab);
-        for (int ic = 0; ic < kp.npp; ++ic) {
-            R q, ohq, Q[3], QC[3], Kcd;
-            PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Q, QC, Kcd);
-            const R pq = p + q;
-            const R rs = rchem_rsqrt(pq);
-            const R ipq = rs * rs;
-            const R PQx = P[0] - Q[0], PQy = P[1] - Q[1], PQz = P[2] - Q[2];
-            const R qi = q * ipq, pi = p * ipq;
-            const R T = p * qi * (PQx * PQx + PQy * PQy + PQz * PQz);
-            const R pref = Kab * Kcd * rs;
-            R F[L + 1];
-            boys_eval<L, C::BOYS_DIRECT, R>(T, pref, btab, etab, F);
-            C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi * PQx, -qi * PQy, -qi * PQz, QC[0], QC[1], QC[2],
-                               pi * PQx, pi * PQy, pi * PQz, ohp, ohq, R(0.5) * ipq, qi, pi);
-        }
+        PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Q, QC, Kcd);
+        prim(p, ohp, P, PA, Kab, q, ohq, Q, QC, Kcd);
     }
+    for (int o = G >> 1; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < C::NE * C::NF; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    // one lane per quartet finishes it
+    const bool lead = active && r == 0;
 
     R AB[3], CD[3];
     Tabs<R>::ab(bp, AB);
@@ -111,7 +122,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #define IDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
     if constexpr (EPI == EPI_DIAG) {
         if constexpr (LA == LC && LB == LD) {
-            if (active) {
+            if (lead) {
                 double m = 0.0;
 #pragma unroll
                 for (int ia = 0; ia < NA; ++ia)
@@ -125,7 +136,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     const int n = a.nbf;
     const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
     if constexpr (EPI == EPI_STORE) {
-        if (active) {
+        if (lead) {
             const size_t N1 = (size_t)n, N2 = N1 * n, N3 = N2 * n;
 #pragma unroll
             for (int ia = 0; ia < NA; ++ia)
@@ -151,12 +162,13 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     }
 
     // ---- EPI_JK: degeneracy-weighted 8-fold scatter -------------------------
-    R deg = active ? R(1) : R(0);
+    R deg = R(1);
     if (bp.diag) deg *= R(0.5);
     if (kp.diag) deg *= R(0.5);
     if (bidx == kidx) deg *= R(0.5);
 
-    // J-hat bra block: sum over the ket of 2 (ab|cd) D_cd, reduced over the warp
+    if (!lead) return;
+    // J-hat bra block: 2 (ab|cd) D_cd
     {
         R Dcd[NC * ND];
 #pragma unroll
@@ -172,11 +184,9 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dcd[ic * ND + id];
-                s = warp_sum<R>(s * deg);
-                if (lane == 0) atomicAdd(a.J + (m0 + ia) * n + n0 + ib, 2.0 * (double)s);
+                atomicAdd(a.J + (m0 + ia) * n + n0 + ib, 2.0 * (double)(s * deg));
             }
     }
-    if (!active) return;
     // J-hat ket block: 2 (ab|cd) D_ab
     {
         R Dab[NA * NB];

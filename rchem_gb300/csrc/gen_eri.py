@@ -273,17 +273,19 @@ def best_hrr(la, lb, lc, ld, targets):
     return best
 
 
-# Boys-function cost model of boys.cuh (must stay in sync with it):
-#   Taylor about the nearest grid point with NTAY terms for each m (direct)
-#   or for F_L and exp(-T) followed by the downward recursion.
+# Boys-function cost model of boys.cuh (must stay in sync with it): a Horner
+# chain of NTAY-1 FMAs per evaluated function; every F_m for L <= 1, else F_L
+# and e^{-T} followed by the downward recursion (one FMA + one multiply per m);
+# the prefactor multiplies (L+1 or 2); the grid index (one FMA + one add + one FMA).
 NTAY64 = 8
 NTAY32 = 4
 
 
 def boys_ops(L, ntay=NTAY64):
-    direct = (ntay - 1) * (L + 1) + (ntay - 1)  # Horner per m + the (-d/k) multipliers
-    downward = (ntay - 1) + 2 * (ntay - 1) + 2 * L + 2
-    return min(direct, downward), (direct <= downward)
+    """(fma, other) FP64 operations of one Boys evaluation."""
+    if L <= 1:
+        return (ntay - 1) * (L + 1) + 2, (L + 1) + 1
+    return 2 * (ntay - 1) + L + 2, L + 2 + 1
 
 
 def main(outdir):
@@ -297,18 +299,18 @@ def main(outdir):
         NE = len(comps_range(la, la + lb))
         NF = len(comps_range(lc, lc + ld))
         NA, NB, NC, ND = ncart(la), ncart(lb), ncart(lc), ncart(ld)
-        bops, direct = boys_ops(L)
-        # per primitive quartet: set-up (pq, rsqrt via library, rho, PQ, T, pref,
-        # WP/WQ, rho_p, rho_q, ohpq): counted as 24 FP64 ops + rsqrt (~6)
-        setup = 30
-        prim_flops = 2 * (vem.nfma + bops) + (vem.nmul + setup + (L + 1))
+        bf, bo = boys_ops(L)
+        # per primitive quartet set-up: p+q, rsqrt (library: ~4 FP64 ops), 1/(p+q),
+        # P-Q, q/(p+q), p/(p+q), T (3 FMA-type), prefactor (2), W-P and W-Q (6),
+        # 1/(2(p+q)): 12 multiply/add + 3 FMA + rsqrt
+        setup_fma, setup_other = 3, 16
+        prim_flops = 2 * (vem.nfma + bf + setup_fma) + (vem.nmul + bo + setup_other)
         # per contracted quartet: HRR + scatter (6 FMA per integral)
         contr_flops = 2 * hem.nfma + hem.nmul + 2 * 6 * NA * NB * NC * ND
         lines = []
         lines.append("// class (%d%d|%d%d): VRR %s-choice %d ops, HRR %s-choice %d ops" % (la, lb, lc, ld, chv, cost_v, chh, cost_h))
         lines.append("template <> struct EriClass<%d,%d,%d,%d> {" % (la, lb, lc, ld))
         lines.append("  static constexpr int L = %d, NE = %d, NF = %d, NA = %d, NB = %d, NC = %d, ND = %d;" % (L, NE, NF, NA, NB, NC, ND))
-        lines.append("  static constexpr bool BOYS_DIRECT = %s;" % ("true" if direct else "false"))
         lines.append("  static constexpr double PRIM_FLOPS = %d.0, CONTR_FLOPS = %d.0;" % (prim_flops, contr_flops))
         lines.append("  template <typename R> __host__ __device__ static __forceinline__ void vrr(R* __restrict__ acc, const R* __restrict__ F,")
         lines.append("      R PAx, R PAy, R PAz, R WPx, R WPy, R WPz, R QCx, R QCy, R QCz, R WQx, R WQy, R WQz,")

