@@ -103,6 +103,29 @@ typedef struct {
 int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
 int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
 
+/*
+ * The Fock build of rchem_jk_direct without any device allocation (this entry
+ * point has no counterpart in the reference, which runs on the CPU).  It is
+ * for callers that cannot allocate GPU memory where they need the build:
+ * programs whose device memory is owned by an external pooled allocator that
+ * forbids cudaMalloc after start-up, or long-running services whose
+ * steady-state loop must never allocate.
+ *  - D, J and K are device arrays (opts->where must be RCHEM_DEVICE); opts is
+ *    required.  Results equal rchem_jk_direct's up to summation order.
+ *  - The scratch (J-hat, K-hat, the FP32 copy of D) is a static device array
+ *    inside the library sized for at most 640 basis functions (about 8 MiB,
+ *    held by every GPU that loads the library until the process exits);
+ *    larger bases get RCHEM_ERR_UNSUPPORTED.
+ *  - The basis must already be planned for the same thresholds: call
+ *    rchem_jk_direct once with the same options first (planning may allocate).
+ *  - The first call on a device looks up the array's device address; make
+ *    that first call before any stream capture.
+ *  - Every call on a device shares the one array: calls whose GPU work
+ *    overlaps (different threads, streams or handles at the same time) race.
+ *    Each call clears the accumulators it uses.
+ */
+int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
+
 /* build_I (src/basis.rs:430-460): the dense n^4 ERI tensor I[m][n][l][s]. */
 int rchem_build_I(rchem_basis b, double *I, int where);
 /* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */

@@ -1133,3 +1133,87 @@ extern "C" double contr_coulomb(int ia, double *aexps, double *acoefs, double *a
     for (int i = 0; i < count; ++i) s += w[i] * v[i];
     return s;
 }
+
+// ---------------------------------------------------------------------------
+// Fock build that allocates nothing
+// ---------------------------------------------------------------------------
+// rchem_jk_direct keeps its J-hat/K-hat accumulators in buffers the basis
+// handle allocated when it was created, and may allocate again when the work
+// plan changes.  Some callers cannot allocate device memory at the point where
+// they need a Fock build: code running under an external memory manager that
+// owns the whole device (a pooled allocator that forbids cudaMalloc after
+// start-up), or a long-running service whose steady-state loop must never
+// allocate.  rchem_jk_direct_noalloc serves them: its scratch (J-hat, K-hat and the
+// single-precision copy of D of the mixed form) lives in the file-scope device
+// array below, sized for up to RCHEM_NOALLOC_MAX_NBF basis functions
+// (2*640^2 doubles + 640^2 floats, about 8 MiB); every GPU that loads this
+// library holds that array until the process exits.
+#define RCHEM_NOALLOC_MAX_NBF 640
+#define RCHEM_NOALLOC_DOUBLES (2 * RCHEM_NOALLOC_MAX_NBF * RCHEM_NOALLOC_MAX_NBF + \
+                               RCHEM_NOALLOC_MAX_NBF * RCHEM_NOALLOC_MAX_NBF / 2)
+static __device__ __align__(256) double g_noalloc_scratch[RCHEM_NOALLOC_DOUBLES];
+
+// The array's device address, looked up once per device.  On the host the
+// symbol g_noalloc_scratch is only a stand-in: a kernel given it would fault,
+// or silently touch the wrong memory where the GPU can reach host memory, so
+// kernels are always handed this looked-up address.
+static double *g_noalloc_ptr[64];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_err(RCHEM_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            return set_err(RCHEM_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch): %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = (double *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K,
+                                       const rchem_jk_opts *opts) {
+    if (!b || !D || !J || !K || !opts) return set_err(RCHEM_ERR_INVALID, "null argument");
+    if (opts->where != RCHEM_DEVICE)
+        return set_err(RCHEM_ERR_INVALID, "rchem_jk_direct_noalloc takes device arrays only (opts->where = RCHEM_DEVICE)");
+    const int n = b->nbf;
+    if (n > RCHEM_NOALLOC_MAX_NBF)
+        return set_err(RCHEM_ERR_UNSUPPORTED, "nbf=%d exceeds the no-allocation limit of %d basis functions", n,
+                       RCHEM_NOALLOC_MAX_NBF);
+    const double tau = (opts->schwarz_tau == 0.0) ? 1e-12 : (opts->schwarz_tau < 0.0 ? 0.0 : opts->schwarz_tau);
+    const double tau32 = (opts->fp32_tau > 0.0) ? opts->fp32_tau : 0.0;
+    if (!b->planned || tau != b->plan_tau || tau32 != b->plan_tau32)
+        return set_err(RCHEM_ERR_INVALID,
+                       "the basis has no work plan for these thresholds: call rchem_jk_direct once with the same "
+                       "options first (planning may allocate)");
+    double *scratch = nullptr;
+    CKR(noalloc_scratch(&scratch));
+    const size_t nn = (size_t)n * n;
+    double *Jh = scratch, *Kh = scratch + nn;
+    float *D32 = (float *)(scratch + 2 * nn);
+    // the array keeps the previous call's contents: clear the accumulators
+    CK(cudaMemsetAsync(Jh, 0, 2 * nn * sizeof(double), b->stream));
+    bool any32 = false;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
+    const int th = 256;
+    if (any32) {
+        k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, D, D32);
+        CK(cudaGetLastError());
+    }
+    EriArgs a = base_args(b);
+    a.D = D;
+    a.D32 = D32;
+    a.J = Jh;
+    a.K = Kh;
+    CKR(launch_lists(b, a, EPI_JK, any32));
+    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, Jh, Kh, J, K);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(b->stream));
+    b->last_stats = b->plan_stats;
+    return RCHEM_OK;
+}
