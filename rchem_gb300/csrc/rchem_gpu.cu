@@ -291,9 +291,13 @@ struct rchem_basis_s {
     long long task_off[RCHEM_NCLASS][2], task_cnt[RCHEM_NCLASS][2];
     double list_flops[RCHEM_NCLASS][2];
     // concurrent class kernels: fork/join over auxiliary streams
-    static const int NAUX = 8;
+    static const int NAUX = 16;
     cudaStream_t aux[NAUX] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[NAUX] = {};
+    // the device part of a Fock build, captured once per work plan
+    int plan_version = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_version = -1;
     rchem_jk_stats plan_stats;
     rchem_jk_stats last_stats;
     // Fock-build work buffers
@@ -312,6 +316,7 @@ static void free_basis(rchem_basis b) {
         if (b->ev_join[i]) cudaEventDestroy(b->ev_join[i]);
     }
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -613,32 +618,39 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
     CK(cudaStreamSynchronize(b->stream));
     b->plan_stats = st;
     b->planned = true;
+    b->plan_version += 1;
     b->plan_tau = tau;
     b->plan_tau32 = tau32;
     return RCHEM_OK;
 }
 
-// Launch every non-empty class list of an epilogue, the heaviest first, spread
-// over the auxiliary streams so the class kernels run concurrently; the
-// handle's stream waits for all of them.
+// Launch every non-empty class list of an epilogue over the auxiliary streams
+// so the class kernels run concurrently: longest-processing-time-first onto
+// the least-loaded stream (cost = algorithmic FLOPs; FP32 ones weighted by the
+// FP32/FP64 throughput gap); the handle's stream waits for all of them.
 static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32) {
     struct L {
         int k, p;
-        double fl;
+        double cost;
     };
     std::vector<L> ls;
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < (with32 ? 2 : 1); ++p)
-            if (b->task_cnt[k][p] > 0) ls.push_back(L{k, p, b->list_flops[k][p] / (p ? 32.0 : 1.0)});
-    std::stable_sort(ls.begin(), ls.end(), [](const L &x, const L &y) { return x.fl > y.fl; });
+            if (b->task_cnt[k][p] > 0) ls.push_back(L{k, p, b->list_flops[k][p] / (p ? 16.0 : 1.0)});
+    std::stable_sort(ls.begin(), ls.end(), [](const L &x, const L &y) { return x.cost > y.cost; });
     a.segs = b->d_segs;
-    CK(cudaEventRecord(b->ev_fork, b->stream));
     const int nuse = std::min<int>((int)ls.size(), rchem_basis_s::NAUX);
+    CK(cudaEventRecord(b->ev_fork, b->stream));
     for (int i = 0; i < nuse; ++i) CK(cudaStreamWaitEvent(b->aux[i], b->ev_fork, 0));
+    double load[rchem_basis_s::NAUX] = {0};
     for (size_t i = 0; i < ls.size(); ++i) {
+        int best = 0;
+        for (int j = 1; j < nuse; ++j)
+            if (load[j] < load[best]) best = j;
+        load[best] += ls[i].cost;
         a.tasks = b->d_tasks + b->task_off[ls[i].k][ls[i].p];
         a.ntasks = (int)b->task_cnt[ls[i].k][ls[i].p];
-        rchem_eri_launchers[ls[i].k](a, ls[i].p, epi, b->aux[i % rchem_basis_s::NAUX]);
+        rchem_eri_launchers[ls[i].k](a, ls[i].p, epi, b->aux[best]);
     }
     CK(cudaGetLastError());
     for (int i = 0; i < nuse; ++i) {
@@ -780,7 +792,7 @@ extern "C" int rchem_basis_set_stream(rchem_basis b, void *stream) {
     if (b->own_stream) cudaStreamDestroy(b->stream);
     b->own_stream = false;
     b->stream = (cudaStream_t)stream;
-    return RCHEM_OK;
+    return RCHEM_OK;  // a captured graph stays valid: it is launched onto whatever stream is current
 }
 
 // ---------------------------------------------------------------------------
@@ -828,6 +840,29 @@ extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy,
 // ---------------------------------------------------------------------------
 // Fock build
 // ---------------------------------------------------------------------------
+// The device part of a Fock build on the handle's internal buffers:
+// d_D -> (d_D32) -> class kernels -> J-hat, K-hat -> d_Jo, d_Ko.
+static int record_build(rchem_basis b, bool any32) {
+    const int n = b->nbf;
+    const size_t nn = (size_t)n * n;
+    const int th = 256;
+    if (any32) {
+        k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_D32);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemsetAsync(b->d_Jh, 0, nn * sizeof(double), b->stream));
+    CK(cudaMemsetAsync(b->d_Kh, 0, nn * sizeof(double), b->stream));
+    EriArgs a = base_args(b);
+    a.D = b->d_D;
+    a.D32 = b->d_D32;
+    a.J = b->d_Jh;
+    a.K = b->d_Kh;
+    CKR(launch_lists(b, a, EPI_JK, any32));
+    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko);
+    CK(cudaGetLastError());
+    return RCHEM_OK;
+}
+
 extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts) {
     if (!b || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "null argument");
     rchem_jk_opts o;
@@ -839,34 +874,37 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     CKR(plan_tasks(b, tau, tau32));
     const int n = b->nbf;
     const size_t nn = (size_t)n * n;
-    const double *dD = D;
-    if (o.where == RCHEM_HOST) {
-        CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-        dD = b->d_D;
-    }
+    CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double),
+                       o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, b->stream));
     bool any32 = false;
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
-    const int th = 256;
-    if (any32) {
-        k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, dD, b->d_D32);
-        CK(cudaGetLastError());
+    // replay the captured build; capture it again when the plan has changed.
+    // The legacy default stream cannot be captured: run the launches directly there.
+    const bool capturable = b->stream != nullptr && b->stream != cudaStreamLegacy;
+    if (!capturable) {
+        CKR(record_build(b, any32));
+    } else if (b->graph_version != b->plan_version) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_version = -1;
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = record_build(b, any32);
+        const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc != RCHEM_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "capturing the Fock build: %s", cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "instantiating the Fock build: %s", cudaGetErrorString(ei));
+        b->graph_version = b->plan_version;
     }
-    CK(cudaMemsetAsync(b->d_Jh, 0, nn * sizeof(double), b->stream));
-    CK(cudaMemsetAsync(b->d_Kh, 0, nn * sizeof(double), b->stream));
-    EriArgs a = base_args(b);
-    a.D = dD;
-    a.D32 = b->d_D32;
-    a.J = b->d_Jh;
-    a.K = b->d_Kh;
-    CKR(launch_lists(b, a, EPI_JK, any32));
-    double *Jd = (o.where == RCHEM_DEVICE) ? J : b->d_Jo;
-    double *Kd = (o.where == RCHEM_DEVICE) ? K : b->d_Ko;
-    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, b->d_Jh, b->d_Kh, Jd, Kd);
-    CK(cudaGetLastError());
-    if (o.where == RCHEM_HOST) {
-        CK(cudaMemcpyAsync(J, Jd, nn * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
-        CK(cudaMemcpyAsync(K, Kd, nn * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
-    }
+    if (capturable) CK(cudaGraphLaunch(b->graph, b->stream));
+    const cudaMemcpyKind out = o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpyAsync(J, b->d_Jo, nn * sizeof(double), out, b->stream));
+    CK(cudaMemcpyAsync(K, b->d_Ko, nn * sizeof(double), out, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     b->last_stats = b->plan_stats;
     return RCHEM_OK;
