@@ -126,6 +126,19 @@ int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
  */
 int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
 
+/*
+ * Nuclear gradient dE/dR (hartree/bohr, grad[3*natoms]) of the RHF energy the
+ * reference computes, E = sum (H + F) o D + E_nuc (src/bin/rchem.rs:106-108,
+ * plus the nuclear repulsion it does not print), at a converged density
+ * D = C_occ C_occ^T and energy-weighted density W = sum_i eps_i C_i C_i^T
+ * (both without the factor 2, as in src/bin/rchem.rs:101-104).  Adjoint
+ * kernels: derivative ERIs contracted on the fly with the density products,
+ * derivative S/T/V contracted with W and D, Hellmann-Feynman term included.
+ * No counterpart in the reference, which has no gradients.  opts: schwarz_tau
+ * and where (for D, W and grad); fp32_tau is ignored (FP64).
+ */
+int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
+
 /* build_I (src/basis.rs:430-460): the dense n^4 ERI tensor I[m][n][l][s]. */
 int rchem_build_I(rchem_basis b, double *I, int where);
 /* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */

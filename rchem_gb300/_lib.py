@@ -67,6 +67,7 @@ def lib():
     L.rchem_moment.argtypes = [vp, vp, i, i, i, vp, i]
     L.rchem_jk_direct.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_jk_direct_noalloc.argtypes = [vp, vp, vp, vp, p(JKOpts)]
+    L.rchem_gradient.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
     L.rchem_jk_inmem.argtypes = [i, vp, vp, vp, vp, i]
@@ -101,5 +102,5 @@ def exported_symbols():
         "rchem_basis_set_stream", "rchem_S", "rchem_T", "rchem_V", "rchem_moment", "rchem_jk_direct",
         "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
-        "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc",
+        "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient",
     ]

@@ -42,6 +42,19 @@ template <> struct PrimLoad<float> {
     }
 };
 
+// Widen a contribution to double for the FP64 atomic.  float -> double by
+// rebuilding the bit pattern with integer operations, so the FP32 kernels put
+// nothing on the narrow FP64 pipe (subnormal floats, below 1.2e-38, flush to 0).
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu, sgn = u & 0x80000000u;
+    const unsigned ed = (e == 0xffu) ? 0x7ffu : e + 896u;  // rebias 127 -> 1023 (inf/nan kept)
+    const unsigned hi = (e == 0u) ? sgn : (sgn | (ed << 20) | (m >> 3));
+    const unsigned lo = (e == 0u) ? 0u : (m << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 template <typename R> struct Tabs;
 template <> struct Tabs<double> {
     static __device__ __forceinline__ const double *boys(const EriArgs &a) { return a.boys64; }
@@ -166,6 +179,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     if (bp.diag) deg *= R(0.5);
     if (kp.diag) deg *= R(0.5);
     if (bidx == kidx) deg *= R(0.5);
+    const R deg2 = deg + deg;  // J carries the factor 2
 
     if (!lead) return;
     // J-hat bra block: 2 (ab|cd) D_cd
@@ -184,7 +198,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dcd[ic * ND + id];
-                atomicAdd(a.J + (m0 + ia) * n + n0 + ib, 2.0 * (double)(s * deg));
+                atomicAdd(a.J + (m0 + ia) * n + n0 + ib, widen(s * deg2));
             }
     }
     // J-hat ket block: 2 (ab|cd) D_ab
@@ -203,7 +217,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ib = 0; ib < NB; ++ib) s += out[IDX(ia, ib, ic, id)] * Dab[ia * NB + ib];
-                atomicAdd(a.J + (l0 + ic) * n + s0 + id, 2.0 * (double)(s * deg));
+                atomicAdd(a.J + (l0 + ic) * n + s0 + id, widen(s * deg2));
             }
     }
     // K-hat[a][c] += (ab|cd) D_bd
@@ -222,7 +236,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dbd[ib * ND + id];
-                atomicAdd(a.K + (m0 + ia) * n + l0 + ic, (double)(s * deg));
+                atomicAdd(a.K + (m0 + ia) * n + l0 + ic, widen(s * deg));
             }
     }
     // K-hat[b][c] += (ab|cd) D_ad
@@ -241,7 +255,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dad[ia * ND + id];
-                atomicAdd(a.K + (n0 + ib) * n + l0 + ic, (double)(s * deg));
+                atomicAdd(a.K + (n0 + ib) * n + l0 + ic, widen(s * deg));
             }
     }
     // K-hat[a][d] += (ab|cd) D_bc
@@ -260,7 +274,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dbc[ib * NC + ic];
-                atomicAdd(a.K + (m0 + ia) * n + s0 + id, (double)(s * deg));
+                atomicAdd(a.K + (m0 + ia) * n + s0 + id, widen(s * deg));
             }
     }
     // K-hat[b][d] += (ab|cd) D_ac
@@ -279,7 +293,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dac[ia * NC + ic];
-                atomicAdd(a.K + (n0 + ib) * n + s0 + id, (double)(s * deg));
+                atomicAdd(a.K + (n0 + ib) * n + s0 + id, widen(s * deg));
             }
     }
 #undef IDX

@@ -25,6 +25,7 @@
 #include "_gen/eri_dispatch.h"
 #include "boys.cuh"
 #include "eri_kernel.cuh"
+#include "grad.cuh"
 #include "md.cuh"
 #include "rchem_types.h"
 
@@ -303,12 +304,19 @@ struct rchem_basis_s {
     // Fock-build work buffers
     double *d_D = nullptr, *d_Jh = nullptr, *d_Kh = nullptr, *d_Jo = nullptr, *d_Ko = nullptr;
     float *d_D32 = nullptr;
+    // gradient: shell atoms / angular momenta, surviving quartets, W, result
+    int *d_shell_atom = nullptr, *d_shell_l = nullptr;
+    int2 *d_gq = nullptr;
+    long long gq_n = 0;
+    double gq_tau = -1.0;
+    double *d_W = nullptr, *d_grad = nullptr;
 };
 
 static void free_basis(rchem_basis b) {
     if (!b) return;
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
-                    b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32};
+                    b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
+                    b->d_shell_atom, b->d_shell_l, b->d_gq, b->d_W, b->d_grad};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
@@ -415,7 +423,7 @@ static int build_pairs(rchem_basis b) {
                         q.PA[d] = q.P[d] - sa.R[d];
                     }
                     q.K = b->pcoef[sa.prim0 + i] * b->pcoef[sb.prim0 + j] * E * c_pref / p;
-                    q.pad = 0.0;
+                    q.pad = aa;  // exponent on shell A (the gradient kernels need it)
                     c.pp.push_back(q);
                 }
             if (c.pp.empty()) continue;
@@ -751,6 +759,16 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
         shd[s].atom = b->shells[s].atom;
     }
     std::vector<double> Zd(b->Z.begin(), b->Z.end());
+    std::vector<int> sh_atom(nshells), sh_l(nshells);
+    for (int s2 = 0; s2 < nshells; ++s2) {
+        sh_atom[s2] = b->shells[s2].atom;
+        sh_l[s2] = b->shells[s2].l;
+    }
+    if ((rc = upload(&b->d_shell_atom, sh_atom, b->stream)) != RCHEM_OK ||
+        (rc = upload(&b->d_shell_l, sh_l, b->stream)) != RCHEM_OK) {
+        free_basis(b);
+        return rc;
+    }
     const size_t nn = (size_t)b->nbf * b->nbf;
     if ((rc = upload(&b->d_sh, shd, b->stream)) != RCHEM_OK || (rc = upload(&b->d_ao, b->aos, b->stream)) != RCHEM_OK ||
         (rc = upload(&b->d_pexp, b->pexp, b->stream)) != RCHEM_OK ||
@@ -764,7 +782,9 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
         cudaMalloc(&b->d_Kh, nn * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->d_Jo, nn * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->d_Ko, nn * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&b->d_D32, nn * sizeof(float)) != cudaSuccess) {
+        cudaMalloc(&b->d_D32, nn * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b->d_W, nn * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->d_grad, 3 * (size_t)natoms * sizeof(double)) != cudaSuccess) {
         free_basis(b);
         return set_err(RCHEM_ERR_NOMEM, "work buffers for nbf=%d", ao);
     }
@@ -907,6 +927,90 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     CK(cudaMemcpyAsync(K, b->d_Ko, nn * sizeof(double), out, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     b->last_stats = b->plan_stats;
+    return RCHEM_OK;
+}
+
+// every unique surviving quartet (bra pair >= ket pair in the class order), as
+// for the Fock build, for the one-thread-per-quartet gradient kernel
+static int plan_gradient(rchem_basis b, double tau) {
+    if (b->d_gq && b->gq_tau == tau) return RCHEM_OK;
+    std::vector<int2> q;
+    const std::vector<ShellPair> &P = b->pairs;
+    for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
+        const PairGroup &gb = b->groups[gbi];
+        for (int gki = 0; gki < (int)b->groups.size(); ++gki) {
+            const PairGroup &gk = b->groups[gki];
+            if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
+            for (int ib = gb.begin; ib < gb.end; ++ib) {
+                const double Qb = P[ib].Q;
+                if (!(Qb > 0.0)) continue;
+                int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
+                if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
+                for (int j = 0; j < nk; ++j) q.push_back(make_int2(ib, gk.begin + j));
+            }
+        }
+    }
+    if (b->d_gq) cudaFree(b->d_gq);
+    b->d_gq = nullptr;
+    b->gq_n = 0;
+    CKR(upload(&b->d_gq, q, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    b->gq_n = (long long)q.size();
+    b->gq_tau = tau;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad,
+                              const rchem_jk_opts *opts) {
+    if (!b || !D || !W || !grad) return set_err(RCHEM_ERR_INVALID, "null argument");
+    rchem_jk_opts o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
+    const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
+    CKR(plan_gradient(b, tau));
+    const int n = b->nbf, na = b->natoms;
+    const size_t nn = (size_t)n * n;
+    const cudaMemcpyKind in = o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double), in, b->stream));
+    CK(cudaMemcpyAsync(b->d_W, W, nn * sizeof(double), in, b->stream));
+    // nuclear repulsion: dE/dR_A = -sum_C Z_A Z_C (R_A - R_C) / |R_A - R_C|^3
+    std::vector<double> gnuc(3 * (size_t)na, 0.0);
+    for (int a = 0; a < na; ++a)
+        for (int c = 0; c < na; ++c) {
+            if (a == c) continue;
+            double d[3], r2 = 0.0;
+            for (int x = 0; x < 3; ++x) {
+                d[x] = b->R[3 * a + x] - b->R[3 * c + x];
+                r2 += d[x] * d[x];
+            }
+            const double f = -(double)b->Z[a] * b->Z[c] / (r2 * std::sqrt(r2));
+            for (int x = 0; x < 3; ++x) gnuc[3 * a + x] += f * d[x];
+        }
+    CK(cudaMemcpyAsync(b->d_grad, gnuc.data(), 3 * (size_t)na * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    if (b->gq_n > 0) {
+        GradArgs g;
+        g.quartets = b->d_gq;
+        g.nq = (int)b->gq_n;
+        g.nbf = n;
+        g.pairs = b->d_pairs;
+        g.prims = b->d_prims;
+        g.shell_atom = b->d_shell_atom;
+        g.shell_l = b->d_shell_l;
+        g.boys64 = b->tabs->boys64;
+        g.D = b->d_D;
+        g.grad = b->d_grad;
+        k_grad2e<<<(unsigned)((b->gq_n + 63) / 64), 64, 0, b->stream>>>(g);
+        CK(cudaGetLastError());
+    }
+    const int th = 128;
+    k_grad1e<<<(unsigned)((nn + th - 1) / th), th, 3 * (size_t)na * sizeof(double), b->stream>>>(
+        n, reinterpret_cast<const AOGrad *>(b->d_ao), reinterpret_cast<const ShellGrad *>(b->d_sh), b->d_pexp,
+        b->d_pcoef, na, b->d_Z, b->d_R, b->tabs->boys64, b->d_D, b->d_W, b->d_grad);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(grad, b->d_grad, 3 * (size_t)na * sizeof(double),
+                       o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
     return RCHEM_OK;
 }
 
