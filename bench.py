@@ -50,6 +50,7 @@ def _args():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-sample", type=int, default=0, help="J/K elements timed for the CPU baseline (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-north-star", action="store_true", help="skip the (H2O)32 / gradient measurements")
     return ap.parse_args()
 
 
@@ -155,6 +156,67 @@ def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True):
         rates.append(m / (dt * n * n))
     port.set_boys(True)
     return rates, threads, m, n
+
+
+def _timed_builds(rc, torch, b, D, tau32, reps=3):
+    s = torch.cuda.Stream()
+    b.set_stream(s.cuda_stream)
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    for _ in range(2):
+        rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.median(ms)), b.stats()
+
+
+def north_star(rc, torch):
+    """The targets stated on the larger workloads: mixed vs FP64 Fock build on
+    (H2O)32 in the 6-31G*-shaped basis (608 functions) at converged-SCF
+    |dE| <= 1 uEh, and the adjoint gradient time per geometry on (H2O)4 in the
+    6-31G**-shaped basis (100 functions)."""
+    out = {}
+    bname, Z, R = rc.geometry.config("h2o32_631gs")
+    with rc.Basis(Z, R, bname) as b:
+        t0 = time.perf_counter()
+        r64 = rc.scf.rhf(b, thresh_e=1e-10)
+        t_scf64 = time.perf_counter() - t0
+        D = r64["D"].contiguous()
+        ms64, st64 = _timed_builds(rc, torch, b, D, 0.0)
+        rec = {"nbf": b.nbf, "fp64_ms": ms64, "fp64_builds_per_s": 1000.0 / ms64, "eris_fp64": st64["eris_fp64"],
+               "fp64_flops": st64["flops_fp64"], "scf_fp64_s": t_scf64, "scf_iterations": r64["iterations"],
+               "e_total_fp64": r64["e_total"], "mixed": {}}
+        for tau32 in (1e-6, 1e-4):
+            ms, st = _timed_builds(rc, torch, b, D, tau32)
+            t0 = time.perf_counter()
+            r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32)
+            t_scf = time.perf_counter() - t0
+            rec["mixed"]["%g" % tau32] = {
+                "ms": ms, "builds_per_s": 1000.0 / ms, "speedup_vs_fp64": ms64 / ms,
+                "fp32_quartet_fraction": st["quartets_fp32"] / max(1, st["quartets_fp32"] + st["quartets_fp64"]),
+                "scf_dE_Eh": r["e_total"] - r64["e_total"], "scf_max_dD": float((r["D"] - r64["D"]).abs().max()),
+                "scf_s": t_scf, "scf_iterations": r["iterations"]}
+        out["h2o32_631gs_fock"] = rec
+    bname, Z, R = rc.geometry.config("h2o4_631gss")
+    with rc.Basis(Z, R, bname) as b:
+        rc.scf.gradient(b, rc.scf.rhf(b))  # warm-up (plans, graphs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = rc.scf.rhf(b, thresh_e=1e-10)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = rc.scf.gradient(b, res)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out["h2o4_631gss_gradient"] = {"nbf": b.nbf, "scf_s": t1 - t0, "gradient_s": t2 - t1,
+                                       "s_per_geometry": t2 - t0, "max_abs_grad": float(g.abs().max()),
+                                       "check": "central finite differences to 1e-6 Eh/bohr in tests/test_gpu_gradient.py"}
+    return out
 
 
 def run_reference(a):
@@ -292,6 +354,11 @@ def main():
                "sample": "%d J/K elements by the JK_direct loops (src/basis.rs:392-425) with THO ERIs and the "
                          "shipped NR Boys function, extrapolated to the %d^2 elements of a build" % (m, n)}
 
+    # ---- spec workloads (outside the headline timed region) -----------
+    north = None
+    if rank == 0 and not a.no_north_star:
+        north = north_star(rc, torch)
+
     clocks = clk.summary()
     launches = st64["kernels"] + 1  # class kernels + symmetrise
     line = {
@@ -320,6 +387,7 @@ def main():
         "clocks": clocks,
         "wall_s_timed": wall,
         "cpu_baseline": cpu,
+        "north_star": north,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -59,8 +59,24 @@ int rchem_abi_version(void);
 int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords, int nshells,
                        const int *shell_atom, const int *shell_l, const int *shell_nprim, const double *exps,
                        const double *coefs);
+/*
+ * Many geometries in one handle (no counterpart in the reference, which builds
+ * one molecule at a time): every Fock build, S/T/V and gradient call then
+ * covers all of them in one set of kernel launches.  Geometry g owns the next
+ * geom_natoms[g] atoms of atomnos/coords; shell_atom indexes the concatenated
+ * atoms and the shells must come in geometry order.  Matrices are packed:
+ * geometry g's n_g x n_g block (row-major) starts at element geom_offset[g]
+ * (rchem_basis_layout); blocks never couple.
+ */
+int rchem_batch_create(rchem_basis *out, int ngeom, const int *geom_natoms, int natoms, const int *atomnos,
+                       const double *coords, int nshells, const int *shell_atom, const int *shell_l,
+                       const int *shell_nprim, const double *exps, const double *coefs);
+/* Number of geometries, total packed matrix elements, and per geometry (arrays
+ * of ngeom, may be NULL) its basis size and block offset. */
+int rchem_basis_layout(rchem_basis b, int *ngeom, long long *packed, int *geom_nbf, long long *geom_offset);
 int rchem_basis_destroy(rchem_basis b);
-/* Number of contracted Cartesian functions (the reference's cgtos.len()). */
+/* Number of contracted Cartesian functions (the reference's cgtos.len());
+ * summed over the geometries of a batched handle. */
 int rchem_basis_nbf(rchem_basis b);
 /* Use the caller's CUDA stream (a cudaStream_t) instead of the handle's own. */
 int rchem_basis_set_stream(rchem_basis b, void *stream);

@@ -9,9 +9,9 @@ from . import geometry
 from ._lib import RchemError
 from .basis import JK_direct, JK_inmem, S, T, V, Basis, build_I, moment
 from .bse import available_basis_sets, expand_shells, load_bse, read_xyz
-from . import cints, scf
+from . import batch, cints, scf
 
 __all__ = [
     "Basis", "S", "T", "V", "JK_direct", "build_I", "JK_inmem", "moment", "RchemError", "load_bse",
-    "expand_shells", "read_xyz", "available_basis_sets", "geometry", "cints", "scf",
+    "expand_shells", "read_xyz", "available_basis_sets", "geometry", "cints", "scf", "batch",
 ]

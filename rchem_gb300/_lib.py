@@ -60,6 +60,8 @@ def lib():
     L.rchem_abi_version.restype = i
     L.rchem_basis_create.argtypes = [p(vp), i, vp, vp, i, vp, vp, vp, vp, vp]
     L.rchem_basis_destroy.argtypes = [vp]
+    L.rchem_batch_create.argtypes = [p(vp), i, vp, i, vp, vp, i, vp, vp, vp, vp, vp]
+    L.rchem_basis_layout.argtypes = [vp, vp, vp, vp, vp]
     L.rchem_basis_nbf.argtypes = [vp]
     L.rchem_basis_set_stream.argtypes = [vp, vp]
     for f in ("rchem_S", "rchem_T", "rchem_V"):
@@ -102,5 +104,6 @@ def exported_symbols():
         "rchem_basis_set_stream", "rchem_S", "rchem_T", "rchem_V", "rchem_moment", "rchem_jk_direct",
         "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
-        "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient",
+        "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
+        "rchem_basis_layout",
     ]

@@ -146,8 +146,10 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
         }
         return;
     }
-    const int n = a.nbf;
+    // bra and ket belong to one geometry: its block of the packed matrices
+    const int n = bp.mn;
     const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
+    const int mo = bp.moff;
     if constexpr (EPI == EPI_STORE) {
         if (lead) {
             const size_t N1 = (size_t)n, N2 = N1 * n, N3 = N2 * n;
@@ -188,7 +190,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-            for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = Tabs<R>::dens(a, (l0 + ic) * n + s0 + id);
+            for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id);
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dcd[ic * ND + id];
-                atomicAdd(a.J + (m0 + ia) * n + n0 + ib, widen(s * deg2));
+                atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, widen(s * deg2));
             }
     }
     // J-hat ket block: 2 (ab|cd) D_ab
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
-            for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = Tabs<R>::dens(a, (m0 + ia) * n + n0 + ib);
+            for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib);
 #pragma unroll
         for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ib = 0; ib < NB; ++ib) s += out[IDX(ia, ib, ic, id)] * Dab[ia * NB + ib];
-                atomicAdd(a.J + (l0 + ic) * n + s0 + id, widen(s * deg2));
+                atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, widen(s * deg2));
             }
     }
     // K-hat[a][c] += (ab|cd) D_bd
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
-            for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = Tabs<R>::dens(a, (n0 + ib) * n + s0 + id);
+            for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id);
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -236,7 +238,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dbd[ib * ND + id];
-                atomicAdd(a.K + (m0 + ia) * n + l0 + ic, widen(s * deg));
+                atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, widen(s * deg));
             }
     }
     // K-hat[b][c] += (ab|cd) D_ad
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
-            for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = Tabs<R>::dens(a, (m0 + ia) * n + s0 + id);
+            for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id);
 #pragma unroll
         for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dad[ia * ND + id];
-                atomicAdd(a.K + (n0 + ib) * n + l0 + ic, widen(s * deg));
+                atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, widen(s * deg));
             }
     }
     // K-hat[a][d] += (ab|cd) D_bc
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
-            for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = Tabs<R>::dens(a, (n0 + ib) * n + l0 + ic);
+            for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic);
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dbc[ib * NC + ic];
-                atomicAdd(a.K + (m0 + ia) * n + s0 + id, widen(s * deg));
+                atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, widen(s * deg));
             }
     }
     // K-hat[b][d] += (ab|cd) D_ac
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
         for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
-            for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = Tabs<R>::dens(a, (m0 + ia) * n + l0 + ic);
+            for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic);
 #pragma unroll
         for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dac[ia * NC + ic];
-                atomicAdd(a.K + (n0 + ib) * n + s0 + id, widen(s * deg));
+                atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, widen(s * deg));
             }
     }
 #undef IDX

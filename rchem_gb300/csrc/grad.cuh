@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     const int la = g.shell_l[bp.A], lb = g.shell_l[bp.B], lc = g.shell_l[kp.A], ld = g.shell_l[kp.B];
     const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2, nc = (lc + 1) * (lc + 2) / 2,
               nd = (ld + 1) * (ld + 2) / 2;
-    const int n = g.nbf;
+    const int n = bp.mn;  // the quartet's geometry block of the packed D
+    const double *Dg = g.D + bp.moff;
     double deg = 8.0;
     if (bp.diag) deg *= 0.5;
     if (kp.diag) deg *= 0.5;
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
                     gr_comp(lb, kb, B);
                     const double cnb = cna * gr_cnorm(B);
                     const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    const double Dmn = g.D[mu * n + nu];
+                    const double Dmn = Dg[mu * n + nu];
                     for (int kc = 0; kc < nc; ++kc) {
                         gr_comp(lc, kc, Cc);
                         const double cnc = cnb * gr_cnorm(Cc);
@@ -192,9 +193,9 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
                             gr_comp(ld, kd, Dd);
                             const int sg = kp.aoB + kd;
                             const double Gam = deg * cnc * gr_cnorm(Dd) *
-                                               (2.0 * Dmn * g.D[la_ * n + sg] -
-                                                0.5 * (g.D[mu * n + la_] * g.D[nu * n + sg] +
-                                                       g.D[mu * n + sg] * g.D[nu * n + la_]));
+                                               (2.0 * Dmn * Dg[la_ * n + sg] -
+                                                0.5 * (Dg[mu * n + la_] * Dg[nu * n + sg] +
+                                                       Dg[mu * n + sg] * Dg[nu * n + la_]));
                             if (Gam == 0.0) continue;
                             for (int x = 0; x < 3; ++x) {
                                 int s[3];
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     }
 }
 
-// One-electron part, one thread per ordered function pair (mu, nu):
+// One-electron part, one thread per ordered function pair (mu, nu) of a geometry:
 //   4 D_mn d_mu H_mn - 4 W_mn d_mu S_mn on the atom of mu,
 //   and the Hellmann-Feynman term -4 D_mn Z_C d_mu V_mn(C) on each nucleus C
 // (d_mu = derivative with respect to the centre of mu; 2-centre translational
@@ -256,50 +257,56 @@ struct ShellGrad {
     int l, nprim, prim0, atom;
 };
 
-__global__ void k_grad1e(int nbf, const AOGrad *ao, const ShellGrad *sh, const double *pexp, const double *pcoef,
-                         int natoms, const double *Z, const double *Ratoms, const double *boys, const double *D,
-                         const double *W, double *grad) {
-    extern __shared__ double sg[];  // 3 * natoms block-local gradient
-    for (int i = threadIdx.x; i < 3 * natoms; i += blockDim.x) sg[i] = 0.0;
-    __syncthreads();
+__device__ __forceinline__ int geom_of(const GeomDev *geo, int ngeom, long long idx) {
+    int lo = 0, hi = ngeom - 1;  // last geometry whose block starts at or before idx
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (geo[mid].moff <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const AOGrad *ao, const ShellGrad *sh,
+                         const double *pexp, const double *pcoef, int natoms_total, const double *Z,
+                         const double *Ratoms, const double *boys, const double *D, const double *W, double *grad) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (idx < (long long)nbf * nbf) {
-        const int mu = (int)(idx / nbf), nu = (int)(idx % nbf);
-        const double Dmn = D[(size_t)mu * nbf + nu], Wmn = W[(size_t)mu * nbf + nu];
-        const AOGrad a = ao[mu], b = ao[nu];
-        const ShellGrad sa = sh[a.shell], sb = sh[b.shell];
-        double gH[3] = {0, 0, 0}, gS[3] = {0, 0, 0};
-        for (int j = 0; j < sb.nprim; ++j) {
-            const double eb = pexp[sb.prim0 + j], cb = pcoef[sb.prim0 + j];
-            for (int i = 0; i < sa.nprim; ++i) {
-                const double ea = pexp[sa.prim0 + i], cc = pcoef[sa.prim0 + i] * cb * a.cn * b.cn;
-                for (int x = 0; x < 3; ++x) {
-                    int up[3] = {a.lmn[0], a.lmn[1], a.lmn[2]}, dn[3] = {a.lmn[0], a.lmn[1], a.lmn[2]};
-                    up[x] += 1;
-                    dn[x] -= 1;
-                    const bool has_dn = a.lmn[x] > 0;
-                    // overlap and kinetic
-                    double s = 2.0 * ea * md_onee_prim(0, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
-                    double t = 2.0 * ea * md_onee_prim(1, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
-                    if (has_dn) {
-                        s -= a.lmn[x] * md_onee_prim(0, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
-                        t -= a.lmn[x] * md_onee_prim(1, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
-                    }
-                    gS[x] += cc * s;
-                    gH[x] += cc * t;
-                    // nuclear attraction, each nucleus
-                    for (int c = 0; c < natoms; ++c) {
-                        double v = 2.0 * ea * md_onee_prim(2, sa.R, up, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
-                        if (has_dn) v -= a.lmn[x] * md_onee_prim(2, sa.R, dn, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
-                        v *= cc * Z[c];
-                        gH[x] += v;
-                        atomicAdd(sg + 3 * c + x, -4.0 * Dmn * v);
-                    }
+    if (idx >= packed) return;
+    const GeomDev gm = geo[geom_of(geo, ngeom, idx)];
+    const int loc = (int)(idx - gm.moff), mu = gm.ao0 + loc / gm.n, nu = gm.ao0 + loc % gm.n;
+    const double Dmn = D[idx], Wmn = W[idx];
+    const AOGrad a = ao[mu], b = ao[nu];
+    const ShellGrad sa = sh[a.shell], sb = sh[b.shell];
+    double gH[3] = {0, 0, 0}, gS[3] = {0, 0, 0};
+    for (int j = 0; j < sb.nprim; ++j) {
+        const double eb = pexp[sb.prim0 + j], cb = pcoef[sb.prim0 + j];
+        for (int i = 0; i < sa.nprim; ++i) {
+            const double ea = pexp[sa.prim0 + i], cc = pcoef[sa.prim0 + i] * cb * a.cn * b.cn;
+            for (int x = 0; x < 3; ++x) {
+                int up[3] = {a.lmn[0], a.lmn[1], a.lmn[2]}, dn[3] = {a.lmn[0], a.lmn[1], a.lmn[2]};
+                up[x] += 1;
+                dn[x] -= 1;
+                const bool has_dn = a.lmn[x] > 0;
+                // overlap and kinetic
+                double s = 2.0 * ea * md_onee_prim(0, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
+                double t = 2.0 * ea * md_onee_prim(1, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
+                if (has_dn) {
+                    s -= a.lmn[x] * md_onee_prim(0, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
+                    t -= a.lmn[x] * md_onee_prim(1, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
+                }
+                gS[x] += cc * s;
+                gH[x] += cc * t;
+                // nuclear attraction, each nucleus of this geometry
+                for (int c = gm.atom0; c < gm.atom0 + gm.natoms; ++c) {
+                    double v = 2.0 * ea * md_onee_prim(2, sa.R, up, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
+                    if (has_dn) v -= a.lmn[x] * md_onee_prim(2, sa.R, dn, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
+                    v *= cc * Z[c];
+                    gH[x] += v;
+                    atomicAdd(grad + 3 * c + x, -4.0 * Dmn * v);
                 }
             }
         }
-        for (int x = 0; x < 3; ++x) atomicAdd(sg + 3 * sa.atom + x, 4.0 * Dmn * gH[x] - 4.0 * Wmn * gS[x]);
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 3 * natoms; i += blockDim.x) atomicAdd(grad + i, sg[i]);
+    for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * sa.atom + x, 4.0 * Dmn * gH[x] - 4.0 * Wmn * gS[x]);
+    (void)natoms_total;
 }

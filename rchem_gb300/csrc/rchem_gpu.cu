@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -187,15 +188,18 @@ struct ShellDev {
     int l, nprim, prim0, atom;
 };
 
-// kind: 0 S, 1 T, 2 V (sum over atoms, Z-weighted), 3 moment
-__global__ void k_onee_matrix(int kind, int nbf, const AODev *ao, const ShellDev *sh, const double *pexp,
-                              const double *pcoef, int natoms, const double *Z, const double *Ratoms,
-                              const double *boys, const double *center, int ox, int oy, int oz, double *out) {
+// kind: 0 S, 1 T, 2 V (sum over the geometry's atoms, Z-weighted), 3 moment.
+// One thread per element of the packed per-geometry blocks.
+__global__ void k_onee_matrix(int kind, long long packed, int ngeom, const GeomDev *geo, const AODev *ao,
+                              const ShellDev *sh, const double *pexp, const double *pcoef, const double *Z,
+                              const double *Ratoms, const double *boys, const double *center, int ox, int oy, int oz,
+                              double *out) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (idx >= (long long)nbf * nbf) return;
-    const int mu = (int)(idx / nbf), nu = (int)(idx % nbf);
-    if (nu > mu) return;  // lower triangle + mirror, src/basis.rs:237-248
-    const AODev a = ao[mu], b = ao[nu];
+    if (idx >= packed) return;
+    const GeomDev gm = geo[geom_of(geo, ngeom, idx)];
+    const int loc = (int)(idx - gm.moff), r = loc / gm.n, c = loc % gm.n;
+    if (c > r) return;  // lower triangle + mirror, src/basis.rs:237-248
+    const AODev a = ao[gm.ao0 + r], b = ao[gm.ao0 + c];
     const ShellDev sa = sh[a.shell], sb = sh[b.shell];
     const int ord[3] = {ox, oy, oz};
     double v = 0.0;
@@ -206,8 +210,8 @@ __global__ void k_onee_matrix(int kind, int nbf, const AODev *ao, const ShellDev
             double x;
             if (kind == 2) {
                 x = 0.0;
-                for (int c = 0; c < natoms; ++c)
-                    x += Z[c] * md_onee_prim(2, sa.R, a.lmn, eai, sb.R, b.lmn, ebj, Ratoms + 3 * c, boys);
+                for (int at = gm.atom0; at < gm.atom0 + gm.natoms; ++at)
+                    x += Z[at] * md_onee_prim(2, sa.R, a.lmn, eai, sb.R, b.lmn, ebj, Ratoms + 3 * at, boys);
             } else if (kind == 3) {
                 x = md_moment_prim(sa.R, a.lmn, eai, sb.R, b.lmn, ebj, center, ord);
             } else {
@@ -217,18 +221,20 @@ __global__ void k_onee_matrix(int kind, int nbf, const AODev *ao, const ShellDev
         }
     }
     v *= a.cn * b.cn;
-    out[(size_t)mu * nbf + nu] = v;
-    out[(size_t)nu * nbf + mu] = v;
+    out[gm.moff + (size_t)r * gm.n + c] = v;
+    out[gm.moff + (size_t)c * gm.n + r] = v;
 }
 
-// J = Jhat + Jhat^T, K = Khat + Khat^T
-__global__ void k_symmetrize(int n, const double *Jh, const double *Kh, double *J, double *K) {
+// J = Jhat + Jhat^T, K = Khat + Khat^T, block by block
+__global__ void k_symmetrize(long long packed, int ngeom, const GeomDev *geo, const double *Jh, const double *Kh,
+                             double *J, double *K) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (idx >= (long long)n * n) return;
-    const int i = (int)(idx / n), j = (int)(idx % n);
-    const size_t ij = (size_t)i * n + j, ji = (size_t)j * n + i;
-    J[ij] = Jh[ij] + Jh[ji];
-    K[ij] = Kh[ij] + Kh[ji];
+    if (idx >= packed) return;
+    const GeomDev gm = geo[geom_of(geo, ngeom, idx)];
+    const int loc = (int)(idx - gm.moff), r = loc / gm.n, c = loc % gm.n;
+    const size_t ji = gm.moff + (size_t)c * gm.n + r;
+    J[idx] = Jh[idx] + Jh[ji];
+    K[idx] = Kh[idx] + Kh[ji];
 }
 
 __global__ void k_to_f32(long long n, const double *x, float *y) {
@@ -258,7 +264,7 @@ __global__ void k_jk_inmem(int n, const double *I, const double *D, double *J, d
 // basis handle
 // ---------------------------------------------------------------------------
 struct PairGroup {
-    int cls, la, lb, npp, begin, end;
+    int cls, la, lb, npp, begin, end, geom;
 };
 
 struct rchem_basis_s {
@@ -266,6 +272,13 @@ struct rchem_basis_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int natoms = 0, nbf = 0, nshells = 0;
+    // geometries (one for rchem_basis_create): packed n_g x n_g matrix blocks
+    int ngeom = 1;
+    long long packed = 0;
+    std::vector<GeomDev> geoms;
+    std::vector<int> atom_geom;
+    std::vector<int> geom_group_begin, geom_group_end;
+    GeomDev *d_geom = nullptr;
     std::vector<int> Z;
     std::vector<double> R;
     std::vector<ShellInfo> shells;
@@ -316,7 +329,7 @@ static void free_basis(rchem_basis b) {
     if (!b) return;
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
                     b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
-                    b->d_shell_atom, b->d_shell_l, b->d_gq, b->d_W, b->d_grad};
+                    b->d_shell_atom, b->d_shell_l, b->d_gq, b->d_W, b->d_grad, b->d_geom};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
@@ -404,6 +417,8 @@ static int build_pairs(rchem_basis b) {
         for (int B = 0; B < b->nshells; ++B) {
             const ShellInfo &sa = b->shells[A], &sb = b->shells[B];
             if (!(sa.l > sb.l || (sa.l == sb.l && A >= B))) continue;
+            const int gA = b->atom_geom[sa.atom];
+            if (b->atom_geom[sb.atom] != gA) continue;  // pairs never span two geometries
             Cand c;
             double AB[3], r2 = 0.0;
             for (int d = 0; d < 3; ++d) {
@@ -431,8 +446,10 @@ static int build_pairs(rchem_basis b) {
             memset(&s, 0, sizeof(s));
             s.A = A;
             s.B = B;
-            s.aoA = sa.ao;
-            s.aoB = sb.ao;
+            s.aoA = sa.ao - b->geoms[gA].ao0;  // basis-function index within the geometry
+            s.aoB = sb.ao - b->geoms[gA].ao0;
+            s.moff = b->geoms[gA].moff;
+            s.mn = b->geoms[gA].n;
             s.npp = (int)c.pp.size();
             s.diag = (A == B) ? 1 : 0;
             for (int d = 0; d < 3; ++d) {
@@ -443,16 +460,22 @@ static int build_pairs(rchem_basis b) {
             c.cls = pair_cls(sa.l, sb.l);
             cands.push_back(std::move(c));
         }
-    // groups keyed by (class, npp)
-    std::map<std::pair<int, int>, std::vector<int>> gm;
-    for (int i = 0; i < (int)cands.size(); ++i) gm[{cands[i].cls, cands[i].sp.npp}].push_back(i);
+    // groups keyed by (geometry, class, npp), geometries in order
+    std::map<std::tuple<int, int, int>, std::vector<int>> gm;
+    for (int i = 0; i < (int)cands.size(); ++i)
+        gm[std::make_tuple(b->atom_geom[b->shells[cands[i].sp.A].atom], cands[i].cls, cands[i].sp.npp)].push_back(i);
     b->pairs.clear();
     b->groups.clear();
     std::vector<PairPrim> prims;
+    b->geom_group_begin.assign(b->ngeom, 0);
+    b->geom_group_end.assign(b->ngeom, 0);
     for (auto &kv : gm) {
         PairGroup g;
-        g.cls = kv.first.first;
-        g.npp = kv.first.second;
+        g.geom = std::get<0>(kv.first);
+        g.cls = std::get<1>(kv.first);
+        g.npp = std::get<2>(kv.first);
+        if (b->geom_group_end[g.geom] == 0) b->geom_group_begin[g.geom] = (int)b->groups.size();
+        b->geom_group_end[g.geom] = (int)b->groups.size() + 1;
         const ShellPair &s0 = cands[kv.second[0]].sp;
         g.la = s0.la_lb / 10;
         g.lb = s0.la_lb % 10;
@@ -517,7 +540,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
-        for (int gki = 0; gki < (int)b->groups.size(); ++gki) {
+        for (int gki = b->geom_group_begin[gb.geom]; gki < b->geom_group_end[gb.geom]; ++gki) {
             const PairGroup &gk = b->groups[gki];
             if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
             const int k = quartet_kernel(gb.cls, gk.cls);
@@ -668,25 +691,57 @@ static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32) {
     return RCHEM_OK;
 }
 
-extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords,
-                                  int nshells, const int *shell_atom, const int *shell_l, const int *shell_nprim,
-                                  const double *exps, const double *coefs) {
+// Shared by rchem_basis_create (one geometry) and rchem_batch_create: geometry
+// g owns atoms [atom0_g, atom0_g + geom_natoms[g]) and the shells on them,
+// which must come in geometry order.
+static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int natoms, const int *atomnos,
+                       const double *coords, int nshells, const int *shell_atom, const int *shell_l,
+                       const int *shell_nprim, const double *exps, const double *coefs) {
     if (!out) return set_err(RCHEM_ERR_INVALID, "out is null");
     *out = nullptr;
-    if (natoms <= 0 || nshells <= 0) return set_err(RCHEM_ERR_INVALID, "natoms=%d nshells=%d", natoms, nshells);
-    if (!atomnos || !coords || !shell_atom || !shell_l || !shell_nprim || !exps || !coefs)
+    if (natoms <= 0 || nshells <= 0 || ngeom <= 0)
+        return set_err(RCHEM_ERR_INVALID, "natoms=%d nshells=%d ngeom=%d", natoms, nshells, ngeom);
+    if (!atomnos || !coords || !shell_atom || !shell_l || !shell_nprim || !exps || !coefs || !geom_natoms)
         return set_err(RCHEM_ERR_INVALID, "null array argument");
     for (int i = 0; i < 3 * natoms; ++i)
         if (!std::isfinite(coords[i])) return set_err(RCHEM_ERR_INVALID, "coordinate %d is not finite", i);
+    {
+        long long tot = 0;
+        for (int g = 0; g < ngeom; ++g) {
+            if (geom_natoms[g] <= 0) return set_err(RCHEM_ERR_INVALID, "geometry %d has %d atoms", g, geom_natoms[g]);
+            tot += geom_natoms[g];
+        }
+        if (tot != natoms) return set_err(RCHEM_ERR_INVALID, "geometry atom counts sum to %lld, not %d", tot, natoms);
+    }
     rchem_basis b = new rchem_basis_s();
     CK(cudaGetDevice(&b->dev));
     b->natoms = natoms;
     b->Z.assign(atomnos, atomnos + natoms);
     b->R.assign(coords, coords + 3 * natoms);
     b->nshells = nshells;
-    int pos = 0, ao = 0;
+    b->ngeom = ngeom;
+    b->geoms.assign(ngeom, GeomDev{0, 0, 0, 0, 0, 0});
+    b->atom_geom.assign(natoms, 0);
+    for (int g = 0, a0 = 0; g < ngeom; ++g) {
+        b->geoms[g].atom0 = a0;
+        b->geoms[g].natoms = geom_natoms[g];
+        for (int k = 0; k < geom_natoms[g]; ++k) b->atom_geom[a0 + k] = g;
+        a0 += geom_natoms[g];
+    }
+    int pos = 0, ao = 0, gprev = 0;
     for (int s = 0; s < nshells; ++s) {
         const int l = shell_l[s], np = shell_nprim[s], at = shell_atom[s];
+        if (at >= 0 && at < natoms) {
+            const int g = b->atom_geom[at];
+            if (g < gprev) {
+                free_basis(b);
+                return set_err(RCHEM_ERR_INVALID, "shell %d: shells must come in geometry order", s);
+            }
+            for (int gg = gprev + (s == 0 ? 0 : 1); gg <= g; ++gg) b->geoms[gg].ao0 = ao;
+            if (s == 0)
+                for (int gg = 0; gg <= g; ++gg) b->geoms[gg].ao0 = 0;
+            gprev = g;
+        }
         if (l < 0 || l > RCHEM_MAX_L) {
             free_basis(b);
             return set_err(RCHEM_ERR_UNSUPPORTED, "shell %d has l=%d (supported: 0..%d)", s, l, RCHEM_MAX_L);
@@ -729,6 +784,25 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
         b->shells.push_back(si);
     }
     b->nbf = ao;
+    for (int gg = gprev + 1; gg < ngeom; ++gg) b->geoms[gg].ao0 = ao;
+    {
+        long long moff = 0;
+        for (int g = 0; g < ngeom; ++g) {
+            const int end = (g + 1 < ngeom) ? b->geoms[g + 1].ao0 : ao;
+            b->geoms[g].n = end - b->geoms[g].ao0;
+            if (b->geoms[g].n <= 0) {
+                free_basis(b);
+                return set_err(RCHEM_ERR_INVALID, "geometry %d has no basis functions", g);
+            }
+            b->geoms[g].moff = (int)moff;
+            moff += (long long)b->geoms[g].n * b->geoms[g].n;
+            if (moff >= (1LL << 31)) {
+                free_basis(b);
+                return set_err(RCHEM_ERR_UNSUPPORTED, "packed matrices exceed 2^31 elements");
+            }
+        }
+        b->packed = moff;
+    }
     int rc;
     if ((rc = get_tables(&b->tabs)) != RCHEM_OK) {
         free_basis(b);
@@ -769,7 +843,11 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
         free_basis(b);
         return rc;
     }
-    const size_t nn = (size_t)b->nbf * b->nbf;
+    const size_t nn = (size_t)b->packed;
+    if ((rc = upload(&b->d_geom, b->geoms, b->stream)) != RCHEM_OK) {
+        free_basis(b);
+        return rc;
+    }
     if ((rc = upload(&b->d_sh, shd, b->stream)) != RCHEM_OK || (rc = upload(&b->d_ao, b->aos, b->stream)) != RCHEM_OK ||
         (rc = upload(&b->d_pexp, b->pexp, b->stream)) != RCHEM_OK ||
         (rc = upload(&b->d_pcoef, b->pcoef, b->stream)) != RCHEM_OK ||
@@ -794,6 +872,31 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
     }
     memset(&b->last_stats, 0, sizeof(b->last_stats));
     *out = b;
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords,
+                                  int nshells, const int *shell_atom, const int *shell_l, const int *shell_nprim,
+                                  const double *exps, const double *coefs) {
+    return create_impl(out, 1, &natoms, natoms, atomnos, coords, nshells, shell_atom, shell_l, shell_nprim, exps,
+                       coefs);
+}
+
+extern "C" int rchem_batch_create(rchem_basis *out, int ngeom, const int *geom_natoms, int natoms, const int *atomnos,
+                                  const double *coords, int nshells, const int *shell_atom, const int *shell_l,
+                                  const int *shell_nprim, const double *exps, const double *coefs) {
+    return create_impl(out, ngeom, geom_natoms, natoms, atomnos, coords, nshells, shell_atom, shell_l, shell_nprim,
+                       exps, coefs);
+}
+
+extern "C" int rchem_basis_layout(rchem_basis b, int *ngeom, long long *packed, int *geom_nbf, long long *geom_offset) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    if (ngeom) *ngeom = b->ngeom;
+    if (packed) *packed = b->packed;
+    for (int g = 0; g < b->ngeom; ++g) {
+        if (geom_nbf) geom_nbf[g] = b->geoms[g].n;
+        if (geom_offset) geom_offset[g] = b->geoms[g].moff;
+    }
     return RCHEM_OK;
 }
 
@@ -837,10 +940,10 @@ static int onee(rchem_basis b, int kind, const double *center, int ox, int oy, i
         CK(cudaMalloc(&d_c, 3 * sizeof(double)));
         CK(cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     }
-    const long long n2 = (long long)b->nbf * b->nbf;
+    const long long n2 = b->packed;
     const int th = 128;
-    k_onee_matrix<<<(unsigned)((n2 + th - 1) / th), th, 0, b->stream>>>(kind, b->nbf, b->d_ao, b->d_sh, b->d_pexp,
-                                                                         b->d_pcoef, b->natoms, b->d_Z, b->d_R,
+    k_onee_matrix<<<(unsigned)((n2 + th - 1) / th), th, 0, b->stream>>>(kind, n2, b->ngeom, b->d_geom, b->d_ao, b->d_sh,
+                                                                         b->d_pexp, b->d_pcoef, b->d_Z, b->d_R,
                                                                          b->tabs->boys64, d_c, ox, oy, oz, dst);
     CK(cudaGetLastError());
     int rc = finish_out(b, dst, out, (size_t)n2, where);
@@ -863,8 +966,7 @@ extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy,
 // The device part of a Fock build on the handle's internal buffers:
 // d_D -> (d_D32) -> class kernels -> J-hat, K-hat -> d_Jo, d_Ko.
 static int record_build(rchem_basis b, bool any32) {
-    const int n = b->nbf;
-    const size_t nn = (size_t)n * n;
+    const size_t nn = (size_t)b->packed;
     const int th = 256;
     if (any32) {
         k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_D32);
@@ -878,7 +980,8 @@ static int record_build(rchem_basis b, bool any32) {
     a.J = b->d_Jh;
     a.K = b->d_Kh;
     CKR(launch_lists(b, a, EPI_JK, any32));
-    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko);
+    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->ngeom, b->d_geom, b->d_Jh,
+                                                                        b->d_Kh, b->d_Jo, b->d_Ko);
     CK(cudaGetLastError());
     return RCHEM_OK;
 }
@@ -892,8 +995,7 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     CKR(plan_tasks(b, tau, tau32));
-    const int n = b->nbf;
-    const size_t nn = (size_t)n * n;
+    const size_t nn = (size_t)b->packed;
     CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double),
                        o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, b->stream));
     bool any32 = false;
@@ -938,7 +1040,7 @@ static int plan_gradient(rchem_basis b, double tau) {
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
-        for (int gki = 0; gki < (int)b->groups.size(); ++gki) {
+        for (int gki = b->geom_group_begin[gb.geom]; gki < b->geom_group_end[gb.geom]; ++gki) {
             const PairGroup &gk = b->groups[gki];
             if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
             for (int ib = gb.begin; ib < gb.end; ++ib) {
@@ -969,8 +1071,8 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
     if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     CKR(plan_gradient(b, tau));
-    const int n = b->nbf, na = b->natoms;
-    const size_t nn = (size_t)n * n;
+    const int na = b->natoms;
+    const size_t nn = (size_t)b->packed;
     const cudaMemcpyKind in = o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double), in, b->stream));
     CK(cudaMemcpyAsync(b->d_W, W, nn * sizeof(double), in, b->stream));
@@ -978,7 +1080,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
     std::vector<double> gnuc(3 * (size_t)na, 0.0);
     for (int a = 0; a < na; ++a)
         for (int c = 0; c < na; ++c) {
-            if (a == c) continue;
+            if (a == c || b->atom_geom[a] != b->atom_geom[c]) continue;
             double d[3], r2 = 0.0;
             for (int x = 0; x < 3; ++x) {
                 d[x] = b->R[3 * a + x] - b->R[3 * c + x];
@@ -992,7 +1094,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         GradArgs g;
         g.quartets = b->d_gq;
         g.nq = (int)b->gq_n;
-        g.nbf = n;
+        g.nbf = 0;
         g.pairs = b->d_pairs;
         g.prims = b->d_prims;
         g.shell_atom = b->d_shell_atom;
@@ -1004,9 +1106,10 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         CK(cudaGetLastError());
     }
     const int th = 128;
-    k_grad1e<<<(unsigned)((nn + th - 1) / th), th, 3 * (size_t)na * sizeof(double), b->stream>>>(
-        n, reinterpret_cast<const AOGrad *>(b->d_ao), reinterpret_cast<const ShellGrad *>(b->d_sh), b->d_pexp,
-        b->d_pcoef, na, b->d_Z, b->d_R, b->tabs->boys64, b->d_D, b->d_W, b->d_grad);
+    k_grad1e<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(
+        (long long)nn, b->ngeom, b->d_geom, reinterpret_cast<const AOGrad *>(b->d_ao),
+        reinterpret_cast<const ShellGrad *>(b->d_sh), b->d_pexp, b->d_pcoef, na, b->d_Z, b->d_R, b->tabs->boys64,
+        b->d_D, b->d_W, b->d_grad);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(grad, b->d_grad, 3 * (size_t)na * sizeof(double),
                        o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, b->stream));
@@ -1023,6 +1126,7 @@ extern "C" int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out) {
 extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
     if (!b || !I) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
+    if (b->ngeom != 1) return set_err(RCHEM_ERR_UNSUPPORTED, "build_I takes a single-geometry basis");
     const size_t n = b->nbf, n4 = n * n * n * n;
     if (n > 256) return set_err(RCHEM_ERR_UNSUPPORTED, "dense n^4 tensor for n=%zu", n);
     CKR(plan_tasks(b, 0.0, 0.0));  // every quartet, FP64
@@ -1323,6 +1427,7 @@ extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J
     if (!b || !D || !J || !K || !opts) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (opts->where != RCHEM_DEVICE)
         return set_err(RCHEM_ERR_INVALID, "rchem_jk_direct_noalloc takes device arrays only (opts->where = RCHEM_DEVICE)");
+    if (b->ngeom != 1) return set_err(RCHEM_ERR_UNSUPPORTED, "rchem_jk_direct_noalloc takes a single-geometry basis");
     const int n = b->nbf;
     if (n > RCHEM_NOALLOC_MAX_NBF)
         return set_err(RCHEM_ERR_UNSUPPORTED, "nbf=%d exceeds the no-allocation limit of %d basis functions", n,
@@ -1353,7 +1458,7 @@ extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J
     a.J = Jh;
     a.K = Kh;
     CKR(launch_lists(b, a, EPI_JK, any32));
-    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(n, Jh, Kh, J, K);
+    k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, 1, b->d_geom, Jh, Kh, J, K);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(b->stream));
     b->last_stats = b->plan_stats;

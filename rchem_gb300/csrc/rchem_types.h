@@ -41,6 +41,13 @@ struct ShellPair {
     double Q;        // Schwarz bound sqrt(max |(ab|ab)|) over the pair's functions
     float AB32[3];   // A - B in single precision
     int la_lb;       // 10*l_A + l_B
+    int moff, mn;    // the pair's geometry: offset of its n x n block in the packed matrices, n
+};
+
+// One geometry of a (possibly batched) basis: its block of the packed
+// matrices, its first basis function and its atoms.
+struct GeomDev {
+    int moff, n, ao0, atom0, natoms, pad;
 };
 
 // A run of quartets sharing one bra pair: (bra | ket0 .. ket0+count-1), kets

@@ -1,0 +1,64 @@
+"""Batched geometries: one basis handle, one Fock-build launch set for all of
+them.  Each geometry's block must equal what a single-geometry handle gives."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _geoms(count=9, seed=3):
+    import rchem_gb300 as rc
+
+    return rc.geometry.water_batch(count, seed=seed)
+
+
+def test_batched_fock_and_onee_match_single(gpu):
+    import torch
+
+    import rchem_gb300 as rc
+
+    geoms = _geoms()
+    bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
+    assert bb.ngeom == len(geoms)
+    rng = np.random.default_rng(0)
+    D = torch.zeros(bb.packed, dtype=torch.float64, device="cuda")
+    blocks = []
+    for g in range(bb.ngeom):
+        n = int(bb.geom_nbf[g])
+        X = rng.normal(size=(n, n)) * 0.2
+        Dg = X @ X.T / n
+        blocks.append(Dg)
+        o = int(bb.offsets[g])
+        D[o:o + n * n] = torch.from_numpy(Dg.reshape(-1)).cuda()
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    rc.batch.jk(bb, D, J, K)
+    S = rc.batch._packed_matrix(rc._lib.lib().rchem_S, bb)
+    V = rc.batch._packed_matrix(rc._lib.lib().rchem_V, bb)
+    for g, (Z, R) in enumerate(geoms):
+        with rc.Basis(Z, R, "6-31g-fit") as b:
+            n = b.nbf
+            assert n == int(bb.geom_nbf[g])
+            Js, Ks = np.zeros((n, n)), np.zeros((n, n))
+            rc.JK_direct(Js, Ks, b, blocks[g])
+            np.testing.assert_allclose(bb.block(J, g).cpu().numpy(), Js, atol=1e-12, rtol=0)
+            np.testing.assert_allclose(bb.block(K, g).cpu().numpy(), Ks, atol=1e-12, rtol=0)
+            np.testing.assert_allclose(bb.block(S, g).cpu().numpy(), rc.S(b), atol=1e-13, rtol=0)
+            np.testing.assert_allclose(bb.block(V, g).cpu().numpy(), rc.V(b), atol=1e-12, rtol=0)
+    bb.close()
+
+
+def test_batched_rhf_and_gradient_match_single(gpu):
+    import rchem_gb300 as rc
+
+    geoms = _geoms(6, seed=5)
+    bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
+    res = rc.batch.rhf_batch(bb, thresh_e=1e-11, thresh_d=1e-8)
+    grads = rc.batch.gradient_batch(bb, res)
+    assert res["converged"]
+    for g, (Z, R) in enumerate(geoms):
+        with rc.Basis(Z, R, "6-31g-fit") as b:
+            r1 = rc.scf.rhf(b, thresh_e=1e-11, thresh_d=1e-8)
+            g1 = rc.scf.gradient(b, r1).cpu().numpy()
+        assert abs(res["e_total"][g] - r1["e_total"]) < 1e-9, g
+        np.testing.assert_allclose(grads[g], g1, atol=1e-7, rtol=0)
+    bb.close()
