@@ -7,9 +7,10 @@ step, every unique shell quartet computed once.  Synthetic, seeded geometry
 density of that system.
 
 Timing: W warm-up builds, then K timed builds, each bracketed by CUDA events
-on the stream the kernels run on; a 256 MiB buffer is written between timed
-builds (outside the events) so L2 (~126 MB) holds nothing of the previous
-build.  ``value`` is FP64 Fock builds/s with D, J and K resident on the device;
+that the library records on the stream its kernels run on (from the copy of D
+in to the copies of J and K out, so host submission latency is excluded); a
+256 MiB buffer is written between timed builds (outside the events) so L2
+(~126 MB) holds nothing of the previous build.  ``value`` is FP64 Fock builds/s with D, J and K resident on the device;
 ``e2e`` is the same through the C ABI with host arrays (H2D of D and D2H of J
 and K inside the timed region).  The mixed FP32/FP64 form is reported under
 ``forms``.
@@ -183,6 +184,8 @@ def north_star(rc, torch):
     out = {}
     bname, Z, R = rc.geometry.config("h2o32_631gs")
     with rc.Basis(Z, R, bname) as b:
+        rc.scf.rhf(b, max_iter=2)  # warm-up: work plan, graph, cuSOLVER initialisation
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         r64 = rc.scf.rhf(b, thresh_e=1e-10)
         t_scf64 = time.perf_counter() - t0
@@ -202,6 +205,39 @@ def north_star(rc, torch):
                 "scf_dE_Eh": r["e_total"] - r64["e_total"], "scf_max_dD": float((r["D"] - r64["D"]).abs().max()),
                 "scf_s": t_scf, "scf_iterations": r["iterations"]}
         out["h2o32_631gs_fock"] = rec
+    # 512 geometries of uneven size (monomer/dimer/trimer, 13/26/39 functions)
+    # in one handle: every Fock build is one graph launch over all of them
+    geoms = rc.geometry.water_batch(512, seed=7)
+    bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
+    rc.batch.rhf_batch(bb, max_iter=2)  # warm-up (plans, graphs)
+    rec = {"geometries": bb.ngeom, "packed_elements": bb.packed, "sizes": sorted(set(bb.geom_nbf.tolist()))}
+    for tag, tau32 in (("fp64", 0.0), ("mixed", 1e-6)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = rc.batch.gradient_batch(bb, r)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        rec[tag] = {"scf_s": t1 - t0, "gradient_s": t2 - t1, "s_per_geometry": (t2 - t0) / bb.ngeom,
+                    "iterations": r["iterations"], "converged": r["converged"], "e_total": r["e_total"]}
+    D = torch.zeros(bb.packed, dtype=torch.float64, device="cuda")
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    rc.batch.jk(bb, D, J, K)
+    for tag, tau32 in (("fp64", 0.0), ("mixed", 1e-6)):
+        rc.batch.jk(bb, D, J, K, fp32_tau=tau32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            rc.batch.jk(bb, D, J, K, fp32_tau=tau32)
+        torch.cuda.synchronize()
+        rec[tag]["fock_build_all_geometries_ms"] = (time.perf_counter() - t0) / 3 * 1e3
+    dE = np.abs(np.asarray(rec["mixed"].pop("e_total")) - np.asarray(rec["fp64"].pop("e_total")))
+    rec["mixed_vs_fp64_max_abs_dE_Eh"] = float(dE.max())
+    out["batch512_631g"] = rec
+    bb.close()
+
     bname, Z, R = rc.geometry.config("h2o4_631gss")
     with rc.Basis(Z, R, bname) as b:
         rc.scf.gradient(b, rc.scf.rhf(b))  # warm-up (plans, graphs)
@@ -274,20 +310,19 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def run(tau32, steps, warmup):
+        # device time of each build from the library's own CUDA events on the
+        # stream its kernels run on (bracketing the copy of D in, the class
+        # kernels and the copies of J and K out); the L2 flush runs before.
         for _ in range(warmup):
             rc.JK_direct(J, K, b, D, fp32_tau=tau32)
-        evs = []
+        ms = []
         for _ in range(steps):
             with torch.cuda.stream(stream):
                 flush.fill_(1)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
             rc.JK_direct(J, K, b, D, fp32_tau=tau32)
-            e1.record(stream)
-            evs.append((e0, e1))
+            ms.append(b.stats()["gpu_ms"])
         torch.cuda.synchronize()
-        return [e0.elapsed_time(e1) for e0, e1 in evs]
+        return ms
 
     # ---- timed region: FP64 form -----------------------------------------
     if world > 1:

@@ -108,6 +108,8 @@ typedef struct {
     long long warp_tasks;                   /* warps launched */
     int kernels;                            /* class kernels launched */
     int reserved;
+    double gpu_ms;                          /* device time of the last rchem_jk_direct (CUDA events on its
+                                               stream, from the copy of D in to the copies of J and K out) */
 } rchem_jk_stats;
 
 /*

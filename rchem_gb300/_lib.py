@@ -31,7 +31,7 @@ class JKStats(C.Structure):
         ("prim_quartets_fp64", C.c_longlong), ("prim_quartets_fp32", C.c_longlong),
         ("eris_fp64", C.c_longlong), ("eris_fp32", C.c_longlong),
         ("flops_fp64", C.c_double), ("flops_fp32", C.c_double),
-        ("warp_tasks", C.c_longlong), ("kernels", C.c_int), ("reserved", C.c_int),
+        ("warp_tasks", C.c_longlong), ("kernels", C.c_int), ("reserved", C.c_int), ("gpu_ms", C.c_double),
     ]
 
     def as_dict(self):

@@ -91,35 +91,6 @@ __device__ __forceinline__ void gr_R(int L, double a, double X, double Y, double
     for (int i = 0; i < cnt; ++i) out[i] = cur[i];
 }
 
-// one Hermite-expanded integral from the per-direction tables
-__device__ __forceinline__ double gr_int(const double (*Eb)[GR_NI][GR_NI][GR_NT], const double (*Ek)[GR_NI][GR_NI][GR_NT],
-                                         const int *a, const int *b, const int *c, const int *d, const double *R) {
-    double s = 0.0;
-    for (int t = 0; t <= a[0] + b[0]; ++t) {
-        const double ex = Eb[0][a[0]][b[0]][t];
-        if (ex == 0.0) continue;
-        for (int u = 0; u <= a[1] + b[1]; ++u) {
-            const double ey = ex * Eb[1][a[1]][b[1]][u];
-            if (ey == 0.0) continue;
-            for (int v = 0; v <= a[2] + b[2]; ++v) {
-                const double ez = ey * Eb[2][a[2]][b[2]][v];
-                if (ez == 0.0) continue;
-                double k = 0.0;
-                for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
-                    const double fx = Ek[0][c[0]][d[0]][tt];
-                    for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
-                        const double fy = fx * Ek[1][c[1]][d[1]][uu];
-                        for (int vv = 0; vv <= c[2] + d[2]; ++vv)
-                            k += fy * Ek[2][c[2]][d[2]][vv] * R[md_tuv(t + tt, u + uu, v + vv)];
-                    }
-                }
-                s += ez * k;
-            }
-        }
-    }
-    return s;
-}
-
 __device__ __forceinline__ void gr_comp(int l, int k, int *lmn) {
     int idx = 0;
     for (int a = 1; a <= l + 1; ++a)
@@ -137,6 +108,46 @@ __device__ __forceinline__ double gr_cnorm(const int *p) {
     const double f2[7] = {1.0, 1.0, 3.0, 15.0, 105.0, 945.0, 10395.0};  // (2k-1)!! for k = 0..6
     return sqrt(f2[p[0] + p[1] + p[2]] / (f2[p[0]] * f2[p[1]] * f2[p[2]]));
 }
+
+// Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
+// Hermite index with t+u+v <= bmax (box of side zd): the ket of one component
+// contracted with the Coulomb integrals once, reused by every bra component.
+__device__ __forceinline__ void gr_zvec(const double (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d,
+                                        const double *R, int zd, int bmax, double *Z) {
+    for (int t = 0; t < zd; ++t)
+        for (int u = 0; u < zd; ++u)
+            for (int v = 0; v < zd; ++v) {
+                double z = 0.0;
+                if (t + u + v <= bmax)
+                    for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
+                        const double fx = Ek[0][c[0]][d[0]][tt];
+                        for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
+                            const double fy = fx * Ek[1][c[1]][d[1]][uu];
+                            for (int vv = 0; vv <= c[2] + d[2]; ++vv)
+                                z += fy * Ek[2][c[2]][d[2]][vv] * R[md_tuv(t + tt, u + uu, v + vv)];
+                        }
+                    }
+                Z[(t * zd + u) * zd + v] = z;
+            }
+}
+
+// sum_{tuv} E^{ab}_{tuv} Z_{tuv}
+__device__ __forceinline__ double gr_dot(const double (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b,
+                                         const double *Z, int zd) {
+    double s = 0.0;
+    for (int t = 0; t <= a[0] + b[0]; ++t) {
+        const double ex = Eb[0][a[0]][b[0]][t];
+        for (int u = 0; u <= a[1] + b[1]; ++u) {
+            const double ey = ex * Eb[1][a[1]][b[1]][u];
+            const double *Zr = Z + (t * zd + u) * zd;
+            for (int v = 0; v <= a[2] + b[2]; ++v) s += ey * Eb[2][a[2]][b[2]][v] * Zr[v];
+        }
+    }
+    return s;
+}
+
+#define GR_ZD 6                           // bra Hermite box side: la+lb+2 <= 6
+#define GR_ZN (GR_ZD * GR_ZD * GR_ZD)
 
 // One thread per contracted shell quartet (unique, 8-fold): 9 centre derivatives
 // of sum Gamma (ab|cd), weighted by the degeneracy factor, added to the gradient.
@@ -156,7 +167,9 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     if (q.x == q.y) deg *= 0.5;
     double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
     const int L1 = la + lb + lc + ld + 1;
+    const int zd = la + lb + 2;
     double Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], R[GR_NR], F[GR_LMAX + 1];
+    double Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
     for (int ia = 0; ia < bp.npp; ++ia) {
         const PairPrim pa = g.prims[bp.prim0 + ia];
         const double aa = pa.pad, ab = pa.p - pa.pad;  // pad holds the exponent on the first shell
@@ -164,67 +177,71 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
             const PairPrim pc = g.prims[kp.prim0 + ic];
             const double ac = pc.pad;
             const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
-            const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Z = pa.P[2] - pc.P[2];
-            const double T = rho * (X * X + Y * Y + Z * Z);
+            const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
+            const double T = rho * (X * X + Y * Y + Zc * Zc);
             boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
-            gr_R(L1, rho, X, Y, Z, F, R);
+            gr_R(L1, rho, X, Y, Zc, F, R);
             for (int dd = 0; dd < 3; ++dd) {
                 gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
                 gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
-                // ket sign (-1)^t folded in
-                for (int i = 0; i <= lc + 1; ++i)
+                for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
                     for (int j = 0; j <= ld; ++j)
                         for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
             }
-            int A[3], B[3], Cc[3], Dd[3];
-            for (int ka = 0; ka < na; ++ka) {
-                gr_comp(la, ka, A);
-                const double cna = gr_cnorm(A);
-                for (int kb = 0; kb < nb; ++kb) {
-                    gr_comp(lb, kb, B);
-                    const double cnb = cna * gr_cnorm(B);
-                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    const double Dmn = Dg[mu * n + nu];
-                    for (int kc = 0; kc < nc; ++kc) {
-                        gr_comp(lc, kc, Cc);
-                        const double cnc = cnb * gr_cnorm(Cc);
-                        const int la_ = kp.aoA + kc;
-                        for (int kd = 0; kd < nd; ++kd) {
-                            gr_comp(ld, kd, Dd);
-                            const int sg = kp.aoB + kd;
-                            const double Gam = deg * cnc * gr_cnorm(Dd) *
-                                               (2.0 * Dmn * Dg[la_ * n + sg] -
-                                                0.5 * (Dg[mu * n + la_] * Dg[nu * n + sg] +
-                                                       Dg[mu * n + sg] * Dg[nu * n + la_]));
+            int A[3], B[3], Cc[3], Dd[3], s[3];
+            for (int kc = 0; kc < nc; ++kc) {
+                gr_comp(lc, kc, Cc);
+                const double cnc = gr_cnorm(Cc);
+                const int l_ = kp.aoA + kc;
+                for (int kd = 0; kd < nd; ++kd) {
+                    gr_comp(ld, kd, Dd);
+                    const double cncd = cnc * gr_cnorm(Dd);
+                    const int s_ = kp.aoB + kd;
+                    // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
+                    gr_zvec(Ek, Cc, Dd, R, zd, la + lb + 1, Z0);
+                    for (int x = 0; x < 3; ++x) {
+                        s[0] = Cc[0]; s[1] = Cc[1]; s[2] = Cc[2];
+                        s[x] += 1;
+                        gr_zvec(Ek, s, Dd, R, zd, la + lb, Zp[x]);
+                        if (Cc[x] > 0) {
+                            s[x] -= 2;
+                            gr_zvec(Ek, s, Dd, R, zd, la + lb, Zm[x]);
+                        }
+                    }
+                    for (int ka = 0; ka < na; ++ka) {
+                        gr_comp(la, ka, A);
+                        const double cna = gr_cnorm(A) * cncd;
+                        const int mu = bp.aoA + ka;
+                        for (int kb = 0; kb < nb; ++kb) {
+                            gr_comp(lb, kb, B);
+                            const int nu = bp.aoB + kb;
+                            const double Gam = deg * cna * gr_cnorm(B) *
+                                               (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
+                                                0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] +
+                                                       Dg[mu * n + s_] * Dg[nu * n + l_]));
                             if (Gam == 0.0) continue;
                             for (int x = 0; x < 3; ++x) {
-                                int s[3];
-                                // centre A
+                                // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
                                 s[0] = A[0]; s[1] = A[1]; s[2] = A[2];
                                 s[x] += 1;
-                                double v = 2.0 * aa * gr_int(Eb, Ek, s, B, Cc, Dd, R);
+                                double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
                                 if (A[x] > 0) {
                                     s[x] -= 2;
-                                    v -= A[x] * gr_int(Eb, Ek, s, B, Cc, Dd, R);
+                                    v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
                                 }
                                 gA[x] += Gam * v;
                                 // centre B
                                 s[0] = B[0]; s[1] = B[1]; s[2] = B[2];
                                 s[x] += 1;
-                                v = 2.0 * ab * gr_int(Eb, Ek, A, s, Cc, Dd, R);
+                                v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
                                 if (B[x] > 0) {
                                     s[x] -= 2;
-                                    v -= B[x] * gr_int(Eb, Ek, A, s, Cc, Dd, R);
+                                    v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
                                 }
                                 gB[x] += Gam * v;
                                 // centre C
-                                s[0] = Cc[0]; s[1] = Cc[1]; s[2] = Cc[2];
-                                s[x] += 1;
-                                v = 2.0 * ac * gr_int(Eb, Ek, A, B, s, Dd, R);
-                                if (Cc[x] > 0) {
-                                    s[x] -= 2;
-                                    v -= Cc[x] * gr_int(Eb, Ek, A, B, s, Dd, R);
-                                }
+                                v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
+                                if (Cc[x] > 0) v -= Cc[x] * gr_dot(Eb, A, B, Zm[x], zd);
                                 gC[x] += Gam * v;
                             }
                         }

@@ -312,6 +312,7 @@ struct rchem_basis_s {
     int plan_version = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_version = -1;
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // device time of a Fock build
     rchem_jk_stats plan_stats;
     rchem_jk_stats last_stats;
     // Fock-build work buffers
@@ -337,6 +338,8 @@ static void free_basis(rchem_basis b) {
         if (b->ev_join[i]) cudaEventDestroy(b->ev_join[i]);
     }
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_t0) cudaEventDestroy(b->ev_t0);
+    if (b->ev_t1) cudaEventDestroy(b->ev_t1);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -820,7 +823,8 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
             return set_err(RCHEM_ERR_CUDA, "auxiliary stream creation failed");
         }
     }
-    if (cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->ev_t0) != cudaSuccess || cudaEventCreate(&b->ev_t1) != cudaSuccess) {
         free_basis(b);
         return set_err(RCHEM_ERR_CUDA, "event creation failed");
     }
@@ -996,6 +1000,7 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     CKR(plan_tasks(b, tau, tau32));
     const size_t nn = (size_t)b->packed;
+    CK(cudaEventRecord(b->ev_t0, b->stream));
     CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double),
                        o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, b->stream));
     bool any32 = false;
@@ -1027,8 +1032,11 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     const cudaMemcpyKind out = o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     CK(cudaMemcpyAsync(J, b->d_Jo, nn * sizeof(double), out, b->stream));
     CK(cudaMemcpyAsync(K, b->d_Ko, nn * sizeof(double), out, b->stream));
+    CK(cudaEventRecord(b->ev_t1, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     b->last_stats = b->plan_stats;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) == cudaSuccess) b->last_stats.gpu_ms = ms;
     return RCHEM_OK;
 }
 
