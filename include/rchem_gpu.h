@@ -157,6 +157,16 @@ int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K
  */
 int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
 
+/*
+ * Autotune the Fock build's tile shapes for this basis and these thresholds
+ * (no counterpart in the reference): for every integral class list (21
+ * classes x {FP64, FP32}) time the list alone under each candidate number of
+ * lanes per shell quartet and keep the fastest.  chosen (may be NULL) receives
+ * 2*21 ints: the minimum primitive quartets per lane picked for each list
+ * (2^30 = never split).  Later rchem_jk_direct calls use the choices.
+ */
+int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen);
+
 /* build_I (src/basis.rs:430-460): the dense n^4 ERI tensor I[m][n][l][s]. */
 int rchem_build_I(rchem_basis b, double *I, int where);
 /* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */

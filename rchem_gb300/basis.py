@@ -82,6 +82,16 @@ class Basis:
         """Run this basis' work on a caller-owned CUDA stream (e.g. torch's)."""
         _lib.check(_lib.lib().rchem_basis_set_stream(self.handle, C.c_void_p(stream_ptr)))
 
+    def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0):
+        """Pick the Fock build's tile shape per integral class for this basis
+        (rchem_autotune); returns {(class, precision): min primitive quartets per lane}."""
+        import numpy as _np
+
+        chosen = _np.zeros(2 * 21, dtype=_np.int32)
+        o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau)
+        _lib.check(_lib.lib().rchem_autotune(self.handle, C.byref(o), chosen.ctypes.data))
+        return {(k, p): int(chosen[2 * k + p]) for k in range(21) for p in range(2)}
+
     def stats(self) -> dict:
         st = _lib.JKStats()
         _lib.check(_lib.lib().rchem_jk_stats_get(self.handle, C.byref(st)))

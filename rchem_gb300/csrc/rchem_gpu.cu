@@ -304,6 +304,9 @@ struct rchem_basis_s {
     size_t tasks_cap = 0, segs_cap = 0;
     long long task_off[RCHEM_NCLASS][2], task_cnt[RCHEM_NCLASS][2];
     double list_flops[RCHEM_NCLASS][2];
+    // tile shape per class list: lanes share a quartet while each keeps at
+    // least this many primitive quartets (rchem_autotune chooses them)
+    int ppl[RCHEM_NCLASS][2];
     // concurrent class kernels: fork/join over auxiliary streams
     static const int NAUX = 16;
     cudaStream_t aux[NAUX] = {};
@@ -530,7 +533,8 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
     return (int)(it - (p.begin() + g.begin));
 }
 
-// lanes share a quartet only while each keeps at least this many primitive quartets
+// default tile shape: lanes share a quartet only while each keeps at least
+// this many primitive quartets
 static const int kMinPrimPerLane = 16;
 
 static int plan_tasks(rchem_basis b, double tau, double tau32) {
@@ -568,7 +572,8 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 // G = 2^lg lanes per quartet: at least kMinPrimPerLane primitive
                 // quartets per lane, at most 32 lanes
                 int lg = 0;
-                while (lg < 5 && nprimq >= (long long)kMinPrimPerLane << (lg + 1)) ++lg;
+                const long long ppl = b->ppl[k][prec];
+                while (lg < 5 && nprimq >= ppl << (lg + 1)) ++lg;
                 const int perwarp = 32 >> lg;
                 // pack the run of segments into full warps
                 int sg = s0, off = 0;
@@ -718,6 +723,7 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
     }
     rchem_basis b = new rchem_basis_s();
     CK(cudaGetDevice(&b->dev));
+    for (int k = 0; k < RCHEM_NCLASS; ++k) b->ppl[k][0] = b->ppl[k][1] = kMinPrimPerLane;
     b->natoms = natoms;
     b->Z.assign(atomnos, atomnos + natoms);
     b->R.assign(coords, coords + 3 * natoms);
@@ -1122,6 +1128,67 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
     CK(cudaMemcpyAsync(grad, b->d_grad, 3 * (size_t)na * sizeof(double),
                        o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
+}
+
+// Autotuner: for every class list of the Fock build, time the list alone under
+// each candidate tile shape and keep the fastest.
+extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    rchem_jk_opts o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
+    const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
+    static const int cand[] = {4, 8, 16, 32, 64, 1 << 30};
+    const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+    float best_ms[RCHEM_NCLASS][2];
+    int best[RCHEM_NCLASS][2];
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p) {
+            best_ms[k][p] = 1e30f;
+            best[k][p] = kMinPrimPerLane;
+        }
+    const size_t nn = (size_t)b->packed;
+    CK(cudaMemsetAsync(b->d_D, 0, nn * sizeof(double), b->stream));
+    CK(cudaMemsetAsync(b->d_D32, 0, nn * sizeof(float), b->stream));
+    for (int c = 0; c < ncand; ++c) {
+        for (int k = 0; k < RCHEM_NCLASS; ++k) b->ppl[k][0] = b->ppl[k][1] = cand[c];
+        b->planned = false;
+        CKR(plan_tasks(b, tau, tau32));
+        EriArgs a = base_args(b);
+        a.segs = b->d_segs;
+        a.D = b->d_D;
+        a.D32 = b->d_D32;
+        a.J = b->d_Jh;
+        a.K = b->d_Kh;
+        for (int k = 0; k < RCHEM_NCLASS; ++k)
+            for (int p = 0; p < 2; ++p) {
+                if (b->task_cnt[k][p] == 0) continue;
+                a.tasks = b->d_tasks + b->task_off[k][p];
+                a.ntasks = (int)b->task_cnt[k][p];
+                float ms = 0.f;
+                for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
+                    CK(cudaEventRecord(b->ev_t0, b->stream));
+                    rchem_eri_launchers[k](a, p, EPI_JK, b->stream);
+                    CK(cudaEventRecord(b->ev_t1, b->stream));
+                    CK(cudaEventSynchronize(b->ev_t1));
+                    CK(cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1));
+                }
+                CK(cudaGetLastError());
+                if (ms < best_ms[k][p]) {
+                    best_ms[k][p] = ms;
+                    best[k][p] = cand[c];
+                }
+            }
+    }
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p) {
+            b->ppl[k][p] = best[k][p];
+            if (chosen) chosen[2 * k + p] = best[k][p];
+        }
+    b->planned = false;
+    CKR(plan_tasks(b, tau, tau32));
     return RCHEM_OK;
 }
 

@@ -293,3 +293,21 @@ def test_zero_density_and_errors(gpu):
                                    "coefficients": [["1.0"]]}]}}}
     with pytest.raises(rc.RchemError, match="l=3"):
         rc.Basis(Z, R, bad)
+
+
+def test_autotune_keeps_results(gpu):
+    """The autotuner only changes how quartets map onto lanes, never what is
+    computed."""
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o8_631g")
+    D = _sym_density(np.random.default_rng(4), 104)
+    with rc.Basis(Z, R, bname) as b:
+        J0, K0 = np.zeros((104, 104)), np.zeros((104, 104))
+        rc.JK_direct(J0, K0, b, D)
+        chosen = b.autotune()
+        assert len(chosen) == 42 and all(v >= 4 for v in chosen.values())
+        J1, K1 = np.zeros((104, 104)), np.zeros((104, 104))
+        rc.JK_direct(J1, K1, b, D)
+        np.testing.assert_allclose(J1, J0, atol=1e-12, rtol=0)
+        np.testing.assert_allclose(K1, K0, atol=1e-12, rtol=0)
