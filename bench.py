@@ -380,7 +380,7 @@ def main():
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get(a.workload)
+            traffic = json.load(open(tpath)).get(a.workload)  # bytes per build, all class kernels
         except (ValueError, OSError):
             traffic = None
 

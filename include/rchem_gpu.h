@@ -120,6 +120,10 @@ typedef struct {
  */
 int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
 int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
+/* Per integral class (21 classes, arrays of 21*4 / 21*2 entries, any may be
+ * NULL) of the current work plan: the class (l_a,l_b,l_c,l_d), and for {FP64,
+ * FP32} the shell quartets, primitive quartets and algorithmic FLOPs. */
+int rchem_jk_class_stats(rchem_basis b, int *class_l, long long *quartets, long long *prim_quartets, double *flops);
 
 /*
  * The Fock build of rchem_jk_direct without any device allocation (this entry

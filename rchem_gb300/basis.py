@@ -92,6 +92,21 @@ class Basis:
         _lib.check(_lib.lib().rchem_autotune(self.handle, C.byref(o), chosen.ctypes.data))
         return {(k, p): int(chosen[2 * k + p]) for k in range(21) for p in range(2)}
 
+    def class_stats(self) -> list:
+        """Per integral class of the current work plan: (l_a,l_b,l_c,l_d) with the
+        FP64 / FP32 shell quartets, primitive quartets and algorithmic FLOPs."""
+        import numpy as _np
+
+        cl = _np.zeros(84, dtype=_np.int32)
+        q = _np.zeros(42, dtype=_np.int64)
+        pq = _np.zeros(42, dtype=_np.int64)
+        fl = _np.zeros(42)
+        _lib.check(_lib.lib().rchem_jk_class_stats(self.handle, cl.ctypes.data, q.ctypes.data, pq.ctypes.data,
+                                                   fl.ctypes.data))
+        return [{"class": tuple(int(x) for x in cl[4 * k:4 * k + 4]), "quartets": (int(q[2 * k]), int(q[2 * k + 1])),
+                 "prim_quartets": (int(pq[2 * k]), int(pq[2 * k + 1])), "flops": (float(fl[2 * k]), float(fl[2 * k + 1]))}
+                for k in range(21)]
+
     def stats(self) -> dict:
         st = _lib.JKStats()
         _lib.check(_lib.lib().rchem_jk_stats_get(self.handle, C.byref(st)))

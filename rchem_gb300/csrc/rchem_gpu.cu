@@ -304,6 +304,7 @@ struct rchem_basis_s {
     size_t tasks_cap = 0, segs_cap = 0;
     long long task_off[RCHEM_NCLASS][2], task_cnt[RCHEM_NCLASS][2];
     double list_flops[RCHEM_NCLASS][2];
+    long long class_quartets[RCHEM_NCLASS][2], class_prims[RCHEM_NCLASS][2];
     // tile shape per class list: lanes share a quartet while each keeps at
     // least this many primitive quartets (rchem_autotune chooses them)
     int ppl[RCHEM_NCLASS][2];
@@ -544,6 +545,8 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
     rchem_jk_stats st;
     memset(&st, 0, sizeof(st));
     memset(b->list_flops, 0, sizeof(b->list_flops));
+    memset(b->class_quartets, 0, sizeof(b->class_quartets));
+    memset(b->class_prims, 0, sizeof(b->class_prims));
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
@@ -598,6 +601,8 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 }
                 const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
                 b->list_flops[k][prec] += fl;
+                b->class_quartets[k][prec] += total;
+                b->class_prims[k][prec] += total * nprimq;
                 if (prec) {
                     st.quartets_fp32 += total;
                     st.prim_quartets_fp32 += total * nprimq;
@@ -1189,6 +1194,22 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         }
     b->planned = false;
     CKR(plan_tasks(b, tau, tau32));
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_jk_class_stats(rchem_basis b, int *class_l, long long *quartets, long long *prim_quartets,
+                                    double *flops) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    if (!b->planned) return set_err(RCHEM_ERR_INVALID, "no Fock build has been planned yet");
+    for (int k = 0; k < RCHEM_NCLASS; ++k) {
+        for (int d = 0; d < 4; ++d)
+            if (class_l) class_l[4 * k + d] = rchem_class_l[k][d];
+        for (int p = 0; p < 2; ++p) {
+            if (quartets) quartets[2 * k + p] = b->class_quartets[k][p];
+            if (prim_quartets) prim_quartets[2 * k + p] = b->class_prims[k][p];
+            if (flops) flops[2 * k + p] = b->list_flops[k][p];
+        }
+    }
     return RCHEM_OK;
 }
 
