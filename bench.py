@@ -159,17 +159,17 @@ def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True):
     return rates, threads, m, n
 
 
-def _timed_builds(rc, torch, b, D, tau32, reps=3):
+def _timed_builds(rc, torch, b, D, tau32, reps=3, emulated=False):
     s = torch.cuda.Stream()
     b.set_stream(s.cuda_stream)
     J, K = torch.empty_like(D), torch.empty_like(D)
     for _ in range(2):
-        rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+        rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
     ms = []
     for _ in range(reps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+        rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
         e1.record(s)
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
@@ -204,6 +204,15 @@ def north_star(rc, torch):
                 "fp32_quartet_fraction": st["quartets_fp32"] / max(1, st["quartets_fp32"] + st["quartets_fp64"]),
                 "scf_dE_Eh": r["e_total"] - r64["e_total"], "scf_max_dD": float((r["D"] - r64["D"]).abs().max()),
                 "scf_s": t_scf, "scf_iterations": r["iterations"]}
+        # emulated FP64 (double-float on the FP32 pipe), alone and under the mixed form
+        rec["emulated"] = {}
+        for tau32 in (0.0, 1e-6):
+            ms, st = _timed_builds(rc, torch, b, D, tau32, emulated=True)
+            r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=True)
+            rec["emulated"]["fp32_tau=%g" % tau32] = {
+                "ms": ms, "builds_per_s": 1000.0 / ms, "speedup_vs_fp64": ms64 / ms,
+                "scf_dE_Eh": r["e_total"] - r64["e_total"], "scf_max_dD": float((r["D"] - r64["D"]).abs().max()),
+                "scf_iterations": r["iterations"]}
         out["h2o32_631gs_fock"] = rec
     # 512 geometries of uneven size (monomer/dimer/trimer, 13/26/39 functions)
     # in one handle: every Fock build is one graph launch over all of them
@@ -310,17 +319,17 @@ def main():
     K = torch.empty_like(D)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def run(tau32, steps, warmup):
+    def run(tau32, steps, warmup, emulated=False):
         # device time of each build from the library's own CUDA events on the
         # stream its kernels run on (bracketing the copy of D in, the class
         # kernels and the copies of J and K out); the L2 flush runs before.
         for _ in range(warmup):
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
         ms = []
         for _ in range(steps):
             with torch.cuda.stream(stream):
                 flush.fill_(1)
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
             ms.append(b.stats()["gpu_ms"])
         torch.cuda.synchronize()
         return ms
@@ -350,6 +359,13 @@ def main():
     Jm, Km = J.cpu().numpy(), K.cpu().numpy()
     dE = float(np.sum(Dh * (2 * (Jm - J64) - (Km - K64))))  # energy change at fixed D, sum (H+F) o D
     ms_mixed = float(np.mean(ms32))
+
+    # ---- emulated FP64 form (double-float on the FP32 pipe, same timing) ----
+    tuned["emulated"] = b.autotune(1e-12, 0.0, emulated=True)
+    msem = run(0.0, a.steps, a.warmup, emulated=True)
+    stem = b.stats()
+    Je, Ke = J.cpu().numpy(), K.cpu().numpy()
+    ms_emul = float(np.mean(msem))
 
     # ---- end to end through the C ABI with host arrays ---------------------
     b.autotune(1e-12, 0.0)
@@ -415,6 +431,11 @@ def main():
                       "quartets_fp64": st32["quartets_fp64"], "quartets_fp32": st32["quartets_fp32"],
                       "speedup_vs_fp64": ms / ms_mixed, "dE_fixed_density_Eh": dE,
                       "max_abs_dJ": float(np.abs(Jm - J64).max()), "max_abs_dK": float(np.abs(Km - K64).max())},
+            "emulated": {"builds_per_s": 1000.0 / ms_emul, "ms": ms_emul, "speedup_vs_fp64": ms / ms_emul,
+                         "arithmetic": "double-float (hi+lo float pairs) for classes up to total L 4, FP64 above",
+                         "quartets": stem["quartets_fp64"],
+                         "dE_fixed_density_Eh": float(np.sum(Dh * (2 * (Je - J64) - (Ke - K64)))),
+                         "max_abs_dJ": float(np.abs(Je - J64).max()), "max_abs_dK": float(np.abs(Ke - K64).max())},
         },
         "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": 2 * n * n * 8},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",

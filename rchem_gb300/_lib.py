@@ -22,7 +22,7 @@ class RchemError(RuntimeError):
 
 
 class JKOpts(C.Structure):
-    _fields_ = [("schwarz_tau", C.c_double), ("fp32_tau", C.c_double), ("where", C.c_int), ("reserved", C.c_int)]
+    _fields_ = [("schwarz_tau", C.c_double), ("fp32_tau", C.c_double), ("where", C.c_int), ("emulated", C.c_int)]
 
 
 class JKStats(C.Structure):

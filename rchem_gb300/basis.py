@@ -82,13 +82,14 @@ class Basis:
         """Run this basis' work on a caller-owned CUDA stream (e.g. torch's)."""
         _lib.check(_lib.lib().rchem_basis_set_stream(self.handle, C.c_void_p(stream_ptr)))
 
-    def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0):
+    def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
         """Pick the Fock build's tile shape per integral class for this basis
         (rchem_autotune); returns {(class, precision): min primitive quartets per lane}."""
         import numpy as _np
 
         chosen = _np.zeros(2 * 21, dtype=_np.int32)
-        o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau)
+        o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
+                        emulated=1 if emulated else 0)
         _lib.check(_lib.lib().rchem_autotune(self.handle, C.byref(o), chosen.ctypes.data))
         return {(k, p): int(chosen[2 * k + p]) for k in range(21) for p in range(2)}
 
@@ -160,8 +161,10 @@ def moment(basis: Basis, center, order, device=False):
     return out
 
 
-def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0):
-    """Fill J and K (in place, like the reference) from the density D."""
+def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
+    """Fill J and K (in place, like the reference) from the density D.
+    ``fp32_tau`` > 0 selects the mixed form; ``emulated`` computes the FP64
+    quartets in double-float arithmetic on the FP32 pipe."""
     dev = _is_cuda(D)
     if dev != _is_cuda(J) or dev != _is_cuda(K):
         raise ValueError("D, J and K must all be host arrays or all CUDA tensors")
@@ -177,7 +180,7 @@ def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0):
         if tuple(X.shape) != (n, n):
             raise ValueError("expected %dx%d matrices" % (n, n))
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
-                    where=_lib.DEVICE if dev else _lib.HOST)
+                    where=_lib.DEVICE if dev else _lib.HOST, emulated=1 if emulated else 0)
     _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
                                           C.c_void_p(_ptr(K)), C.byref(o)))
 

@@ -85,9 +85,10 @@ def _packed_matrix(fn, bb: BatchBasis):
     return out
 
 
-def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0):
+def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
     """One Fock build over every geometry: packed device vectors D -> J, K."""
-    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE)
+    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
+                    emulated=1 if emulated else 0)
     _lib.check(_lib.lib().rchem_jk_direct(bb.handle, C.c_void_p(D.data_ptr()), C.c_void_p(J.data_ptr()),
                                           C.c_void_p(K.data_ptr()), C.byref(o)))
 

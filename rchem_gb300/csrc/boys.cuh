@@ -32,9 +32,16 @@
 #define BOYS_NT64 8
 #define BOYS_NT32 4
 
-template <typename R> struct BoysPrec;
-template <> struct BoysPrec<double> { static constexpr int NTAY = BOYS_NT64; };
+template <typename R> struct BoysPrec { static constexpr int NTAY = BOYS_NT64; };  // double, double-float
 template <> struct BoysPrec<float> { static constexpr int NTAY = BOYS_NT32; };
+
+// 1/k for a small integer k, as a compile-time constant of type R
+template <typename R> RCHEM_HD constexpr R rchem_recip(int k) { return R(1.0 / (double)k); }
+template <> RCHEM_HD constexpr float rchem_recip<float>(int k) { return 1.0f / (float)k; }
+RCHEM_HD inline bool rchem_lt(double a, double b) { return a < b; }
+RCHEM_HD inline bool rchem_lt(float a, float b) { return a < b; }
+RCHEM_HD inline float rchem_tofloat(double a) { return (float)a; }
+RCHEM_HD inline float rchem_tofloat(float a) { return a; }
 
 // table element (sub-table s, grid row i, Taylor order k)
 RCHEM_HD inline int boys_idx(int s, int i, int k, int nt) { return (s * BOYS_NGRID + i) * nt + k; }
@@ -113,7 +120,7 @@ RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
 // F[0..L] = pref * F_m(T).
 template <int L, typename R>
 RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
-    if (T < R(BOYS_TMAX)) {
+    if (rchem_lt(T, R(BOYS_TMAX))) {
         int i;
         R x;
         boys_grid(T, i, x);
@@ -125,12 +132,12 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
             F[L] = boys_horner(tab, L + 1, i, x) * pref;
             const R T2 = T + T;
 #pragma unroll
-            for (int m = L - 1; m >= 0; --m) F[m] = rchem_fma(T2, F[m + 1], ex) * (R(1) / R(2 * m + 1));
+            for (int m = L - 1; m >= 0; --m) F[m] = rchem_fma(T2, F[m + 1], ex) * rchem_recip<R>(2 * m + 1);
         }
     } else {
         const R rs = rchem_rsqrt(T);
         const R inv2T = R(0.5) * rs * rs;
-        const R ex = R(rchem_expf(-(float)T)) * pref;
+        const R ex = R(rchem_expf(-rchem_tofloat(T))) * pref;
         F[0] = R(0.88622692545275801365) * rs * pref;
 #pragma unroll
         for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;

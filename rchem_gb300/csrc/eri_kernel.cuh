@@ -18,6 +18,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "rchem_types.h"
+#include "df64.cuh"
 #include "boys.cuh"
 
 template <int LA, int LB, int LC, int LD> struct EriClass;
@@ -55,11 +56,38 @@ __device__ __forceinline__ double widen(float x) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+template <> struct PrimLoad<df64> {
+    static __device__ __forceinline__ void get(const EriArgs &a, int idx, df64 &p, df64 &ohp, df64 *P, df64 *PA,
+                                               df64 &K) {
+        const float4 *q = reinterpret_cast<const float4 *>(a.primsdf + idx);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2), v3 = __ldg(q + 3), v4 = __ldg(q + 4);
+        p = df64(v0.x, v0.y); ohp = df64(v0.z, v0.w);
+        P[0] = df64(v1.x, v1.y); P[1] = df64(v1.z, v1.w); P[2] = df64(v2.x, v2.y);
+        PA[0] = df64(v2.z, v2.w); PA[1] = df64(v3.x, v3.y); PA[2] = df64(v3.z, v3.w);
+        K = df64(v4.x, v4.y);
+    }
+};
+
+// double-float to double: both words widened exactly, one FP64 add per atomic
+__device__ __forceinline__ double widen(df64 x) { return widen(x.hi) + widen(x.lo); }
+
 template <typename R> struct Tabs;
 template <> struct Tabs<double> {
     static __device__ __forceinline__ const double *boys(const EriArgs &a) { return a.boys64; }
     static __device__ __forceinline__ double dens(const EriArgs &a, int i) { return __ldg(a.D + i); }
     static __device__ __forceinline__ void ab(const ShellPair &s, double *v) { v[0] = s.AB[0]; v[1] = s.AB[1]; v[2] = s.AB[2]; }
+};
+template <> struct Tabs<df64> {
+    static __device__ __forceinline__ const df64 *boys(const EriArgs &a) {
+        return reinterpret_cast<const df64 *>(a.boysdf);
+    }
+    static __device__ __forceinline__ df64 dens(const EriArgs &a, int i) {
+        const float2 v = __ldg(a.Ddf + i);
+        return df64(v.x, v.y);
+    }
+    static __device__ __forceinline__ void ab(const ShellPair &s, df64 *v) {
+        v[0] = df64(s.AB32[0], s.ABlo[0]); v[1] = df64(s.AB32[1], s.ABlo[1]); v[2] = df64(s.AB32[2], s.ABlo[2]);
+    }
 };
 template <> struct Tabs<float> {
     static __device__ __forceinline__ const float *boys(const EriArgs &a) { return a.boys32; }
@@ -301,15 +329,22 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #undef IDX
 }
 
+// prec: 0 = FP64, 1 = FP32 (mixed form), 2 = double-float on the FP32 pipe
+// (emulated FP64; instantiated up to l_a+l_b+l_c+l_d = 4, FP64 above)
 template <int LA, int LB, int LC, int LD>
-void launch_eri_class(const EriArgs &a, int fp32, int epi, cudaStream_t s) {
+void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
     if (a.ntasks <= 0) return;
     const int threads = 128;
     const long long nthreads = (long long)a.ntasks * 32;
     const int blocks = (int)((nthreads + threads - 1) / threads);
     if (epi == EPI_JK) {
-        if (fp32) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
-        else eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+        if (prec == 1) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
+        else if constexpr (LA + LB + LC + LD <= 4) {
+            if (prec == 2) eri_class_kernel<LA, LB, LC, LD, df64, EPI_JK><<<blocks, threads, 0, s>>>(a);
+            else eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+        } else {
+            eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+        }
     } else if (epi == EPI_STORE) {
         eri_class_kernel<LA, LB, LC, LD, double, EPI_STORE><<<blocks, threads, 0, s>>>(a);
     } else if constexpr (LA == LC && LB == LD) {

@@ -66,6 +66,7 @@ extern "C" int rchem_abi_version(void) { return 1; }
 struct DevTables {
     double *boys64 = nullptr;
     float *boys32 = nullptr;
+    float2 *boysdf = nullptr;  // the FP64 table split into (hi, lo) float pairs
 };
 static DevTables g_tabs[64];
 static std::mutex g_tab_mu;
@@ -80,11 +81,18 @@ static int get_tables(const DevTables **out) {
         std::vector<double> b64(boys_table_size(BOYS_NT64));
         std::vector<float> b32(boys_table_size(BOYS_NT32));
         boys_fill_tables(b64.data(), b32.data());
+        std::vector<float2> bdf(b64.size());
+        for (size_t i = 0; i < b64.size(); ++i) {
+            const float hi = (float)b64[i];
+            bdf[i] = make_float2(hi, (float)(b64[i] - (double)hi));
+        }
         DevTables n;
         CK(cudaMalloc(&n.boys64, b64.size() * sizeof(double)));
         CK(cudaMalloc(&n.boys32, b32.size() * sizeof(float)));
+        CK(cudaMalloc(&n.boysdf, bdf.size() * sizeof(float2)));
         CK(cudaMemcpy(n.boys64, b64.data(), b64.size() * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boys32, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(n.boysdf, bdf.data(), bdf.size() * sizeof(float2), cudaMemcpyHostToDevice));
         t = n;
     }
     *out = &t;
@@ -237,6 +245,14 @@ __global__ void k_symmetrize(long long packed, int ngeom, const GeomDev *geo, co
     K[idx] = Kh[idx] + Kh[ji];
 }
 
+__global__ void k_to_df64(long long n, const double *x, float2 *y) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float hi = (float)x[i];
+        y[i] = make_float2(hi, (float)(x[i] - (double)hi));
+    }
+}
+
 __global__ void k_to_f32(long long n, const double *x, float *y) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) y[i] = (float)x[i];
@@ -292,6 +308,8 @@ struct rchem_basis_s {
     ShellPair *d_pairs = nullptr;
     PairPrim *d_prims = nullptr;
     PairPrim32 *d_prims32 = nullptr;
+    PairPrimDF *d_primsdf = nullptr;
+    float2 *d_Ddf = nullptr;
     AODev *d_ao = nullptr;
     ShellDev *d_sh = nullptr;
     double *d_pexp = nullptr, *d_pcoef = nullptr, *d_Z = nullptr, *d_R = nullptr;
@@ -316,6 +334,7 @@ struct rchem_basis_s {
     int plan_version = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_version = -1;
+    int graph_emul = -1;
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // device time of a Fock build
     rchem_jk_stats plan_stats;
     rchem_jk_stats last_stats;
@@ -332,7 +351,7 @@ struct rchem_basis_s {
 
 static void free_basis(rchem_basis b) {
     if (!b) return;
-    void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
+    void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_primsdf, b->d_Ddf, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
                     b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
                     b->d_shell_atom, b->d_shell_l, b->d_gq, b->d_W, b->d_grad, b->d_geom};
     for (void *p : ptrs)
@@ -368,6 +387,9 @@ static EriArgs base_args(rchem_basis b) {
     a.prims32 = b->d_prims32;
     a.boys64 = b->tabs->boys64;
     a.boys32 = b->tabs->boys32;
+    a.boysdf = b->tabs->boysdf;
+    a.primsdf = b->d_primsdf;
+    a.Ddf = b->d_Ddf;
     return a;
 }
 
@@ -462,6 +484,7 @@ static int build_pairs(rchem_basis b) {
             for (int d = 0; d < 3; ++d) {
                 s.AB[d] = AB[d];
                 s.AB32[d] = (float)AB[d];
+                s.ABlo[d] = (float)(AB[d] - (double)s.AB32[d]);
             }
             s.la_lb = 10 * sa.l + sb.l;
             c.cls = pair_cls(sa.l, sb.l);
@@ -511,8 +534,26 @@ static int build_pairs(rchem_basis b) {
         r.K = (float)q.K;
         r.pad[0] = r.pad[1] = r.pad[2] = 0.f;
     }
+    std::vector<PairPrimDF> pdf(prims.size());
+    auto split = [](double v, float *hl) {
+        hl[0] = (float)v;
+        hl[1] = (float)(v - (double)hl[0]);
+    };
+    for (size_t i = 0; i < prims.size(); ++i) {
+        const PairPrim &q = prims[i];
+        PairPrimDF &r = pdf[i];
+        split(q.p, r.p);
+        split(q.ohp, r.ohp);
+        for (int d = 0; d < 3; ++d) {
+            split(q.P[d], r.P[d]);
+            split(q.PA[d], r.PA[d]);
+        }
+        split(q.K, r.K);
+        r.pad[0] = r.pad[1] = 0.f;
+    }
     CKR(upload(&b->d_prims, prims, b->stream));
     CKR(upload(&b->d_prims32, p32, b->stream));
+    CKR(upload(&b->d_primsdf, pdf, b->stream));
     CKR(upload(&b->d_pairs, b->pairs, b->stream));
     // Schwarz bounds, then sort each group by Q descending
     std::vector<double> Q;
@@ -672,7 +713,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
 // so the class kernels run concurrently: longest-processing-time-first onto
 // the least-loaded stream (cost = algorithmic FLOPs; FP32 ones weighted by the
 // FP32/FP64 throughput gap); the handle's stream waits for all of them.
-static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32) {
+static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32, bool emul = false) {
     struct L {
         int k, p;
         double cost;
@@ -694,7 +735,7 @@ static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32) {
         load[best] += ls[i].cost;
         a.tasks = b->d_tasks + b->task_off[ls[i].k][ls[i].p];
         a.ntasks = (int)b->task_cnt[ls[i].k][ls[i].p];
-        rchem_eri_launchers[ls[i].k](a, ls[i].p, epi, b->aux[best]);
+        rchem_eri_launchers[ls[i].k](a, ls[i].p == 1 ? 1 : (emul ? 2 : 0), epi, b->aux[best]);
     }
     CK(cudaGetLastError());
     for (int i = 0; i < nuse; ++i) {
@@ -876,6 +917,7 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
         cudaMalloc(&b->d_Jo, nn * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->d_Ko, nn * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->d_D32, nn * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&b->d_Ddf, nn * sizeof(float2)) != cudaSuccess ||
         cudaMalloc(&b->d_W, nn * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->d_grad, 3 * (size_t)natoms * sizeof(double)) != cudaSuccess) {
         free_basis(b);
@@ -980,11 +1022,15 @@ extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy,
 // ---------------------------------------------------------------------------
 // The device part of a Fock build on the handle's internal buffers:
 // d_D -> (d_D32) -> class kernels -> J-hat, K-hat -> d_Jo, d_Ko.
-static int record_build(rchem_basis b, bool any32) {
+static int record_build(rchem_basis b, bool any32, bool emul) {
     const size_t nn = (size_t)b->packed;
     const int th = 256;
     if (any32) {
         k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_D32);
+        CK(cudaGetLastError());
+    }
+    if (emul) {
+        k_to_df64<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_Ddf);
         CK(cudaGetLastError());
     }
     CK(cudaMemsetAsync(b->d_Jh, 0, nn * sizeof(double), b->stream));
@@ -994,7 +1040,7 @@ static int record_build(rchem_basis b, bool any32) {
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
-    CKR(launch_lists(b, a, EPI_JK, any32));
+    CKR(launch_lists(b, a, EPI_JK, any32, emul));
     k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->ngeom, b->d_geom, b->d_Jh,
                                                                         b->d_Kh, b->d_Jo, b->d_Ko);
     CK(cudaGetLastError());
@@ -1018,16 +1064,17 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
     // replay the captured build; capture it again when the plan has changed.
     // The legacy default stream cannot be captured: run the launches directly there.
+    const bool emul = o.emulated != 0;
     const bool capturable = b->stream != nullptr && b->stream != cudaStreamLegacy;
     if (!capturable) {
-        CKR(record_build(b, any32));
-    } else if (b->graph_version != b->plan_version) {
+        CKR(record_build(b, any32, emul));
+    } else if (b->graph_version != b->plan_version || b->graph_emul != (int)emul) {
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
         b->graph_version = -1;
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = record_build(b, any32);
+        const int rc = record_build(b, any32, emul);
         const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (rc != RCHEM_OK) {
             if (g) cudaGraphDestroy(g);
@@ -1038,6 +1085,7 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
         cudaGraphDestroy(g);
         if (ei != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "instantiating the Fock build: %s", cudaGetErrorString(ei));
         b->graph_version = b->plan_version;
+        b->graph_emul = (int)emul;
     }
     if (capturable) CK(cudaGraphLaunch(b->graph, b->stream));
     const cudaMemcpyKind out = o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -1157,6 +1205,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
     const size_t nn = (size_t)b->packed;
     CK(cudaMemsetAsync(b->d_D, 0, nn * sizeof(double), b->stream));
     CK(cudaMemsetAsync(b->d_D32, 0, nn * sizeof(float), b->stream));
+    CK(cudaMemsetAsync(b->d_Ddf, 0, nn * sizeof(float2), b->stream));
     for (int c = 0; c < ncand; ++c) {
         for (int k = 0; k < RCHEM_NCLASS; ++k) b->ppl[k][0] = b->ppl[k][1] = cand[c];
         b->planned = false;
@@ -1165,6 +1214,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         a.segs = b->d_segs;
         a.D = b->d_D;
         a.D32 = b->d_D32;
+        a.Ddf = b->d_Ddf;
         a.J = b->d_Jh;
         a.K = b->d_Kh;
         for (int k = 0; k < RCHEM_NCLASS; ++k)
@@ -1175,7 +1225,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
                 float ms = 0.f;
                 for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
                     CK(cudaEventRecord(b->ev_t0, b->stream));
-                    rchem_eri_launchers[k](a, p, EPI_JK, b->stream);
+                    rchem_eri_launchers[k](a, p == 1 ? 1 : (o.emulated ? 2 : 0), EPI_JK, b->stream);
                     CK(cudaEventRecord(b->ev_t1, b->stream));
                     CK(cudaEventSynchronize(b->ev_t1));
                     CK(cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1));

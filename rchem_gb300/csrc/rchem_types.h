@@ -13,6 +13,10 @@
 #define RCHEM_HD
 #endif
 
+#ifndef __CUDACC__
+struct float2;  // host-only compiles see the device argument block by pointer only
+#endif
+
 #define RCHEM_LMAX 2          // s, p, d shells (Cartesian)
 #define RCHEM_MAX_NCART 6
 
@@ -39,9 +43,17 @@ struct ShellPair {
     int group, diag; // pair group; 1 if A == B
     double AB[3];    // A - B
     double Q;        // Schwarz bound sqrt(max |(ab|ab)|) over the pair's functions
-    float AB32[3];   // A - B in single precision
+    float AB32[3];   // A - B in single precision (the high words of the double-float form)
     int la_lb;       // 10*l_A + l_B
     int moff, mn;    // the pair's geometry: offset of its n x n block in the packed matrices, n
+    float ABlo[3];   // low words: AB32 + ABlo = A - B to ~48 bits
+    int pad2;
+};
+
+// The same as PairPrim, each value an unevaluated float pair (hi, lo), for the
+// emulated-FP64 (double-float) form; 80 bytes.
+struct PairPrimDF {
+    float p[2], ohp[2], P[3][2], PA[3][2], K[2], pad[2];
 };
 
 // One geometry of a (possibly batched) basis: its block of the packed
@@ -79,6 +91,9 @@ struct EriArgs {
     const float *boys32;
     const double *D;       // density, nbf x nbf row-major
     const float *D32;      // the same in single precision (mixed form)
+    const PairPrimDF *primsdf;  // double-float forms (emulated FP64)
+    const float2 *boysdf;
+    const float2 *Ddf;
     double *J;             // unsymmetrised accumulators (J-hat, K-hat)
     double *K;
     double *eri;           // dense nbf^4 output (ERI-tensor epilogue)

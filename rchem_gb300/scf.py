@@ -10,7 +10,7 @@ nuclear repulsion energy, a density-change criterion and the orbital energies.
 Everything stays FP64 on the GPU: S^-1/2, the Fock diagonalisation (cuSOLVER
 through torch.linalg.eigh) and the DIIS solve; J and K come from
 librchem_gpu.so (rchem_jk_direct) on device pointers, optionally in the mixed
-FP32/FP64 form.
+FP32/FP64 form or with the FP64 quartets in double-float arithmetic.
 """
 from __future__ import annotations
 
@@ -30,7 +30,8 @@ def nuclear_repulsion(atomnos, coords) -> float:
 
 
 def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thresh_d: float = 1e-7,
-        max_iter: int = 128, diis: int = 8, fp32_tau: float = 0.0, schwarz_tau: float = 1e-12, verbose=False):
+        max_iter: int = 128, diis: int = 8, fp32_tau: float = 0.0, schwarz_tau: float = 1e-12, emulated=False,
+        verbose=False):
     """Converge RHF for ``basis``; returns a dict with energies, D, C, eps, W."""
     import torch
 
@@ -58,7 +59,7 @@ def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thres
     converged = False
     it = 0
     for it in range(1, max_iter + 1):
-        _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau)
+        _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau, emulated=emulated)
         F = H + 2.0 * J - K
         e_old, e_new = e_new, float(torch.sum((H + F) * D))
         # DIIS on the orthogonalised commutator FDS - SDF
@@ -97,7 +98,7 @@ def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thres
             converged = True
             break
     # energy at the final density with its own Fock matrix
-    _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau)
+    _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau, emulated=emulated)
     F = H + 2.0 * J - K
     e_elec = float(torch.sum((H + F) * D))
     eps, Cp = torch.linalg.eigh(X.T @ F @ X)

@@ -311,3 +311,76 @@ def test_autotune_keeps_results(gpu):
         rc.JK_direct(J1, K1, b, D)
         np.testing.assert_allclose(J1, J0, atol=1e-12, rtol=0)
         np.testing.assert_allclose(K1, K0, atol=1e-12, rtol=0)
+
+
+# ---- emulated FP64: double-float arithmetic on the FP32 pipe ---------------
+@pytest.mark.parametrize("name", ["6-31gss-fit", "6-31gs-fit"])
+def test_emulated_fp64_vs_oracle_dimer(gpu, oracle_mod, name):
+    """The emulated form keeps the FP64 form's 1e-12 bound against the 8-fold
+    oracle on every class (those above total L 4 run in native FP64)."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    Z, R = rc.geometry.water_cluster(2, 4.5, seed=11)
+    ob = O.expand_basis(Z, R, rc.load_bse(name))
+    D = _sym_density(np.random.default_rng(1), ob.n)
+    Jr, Kr = O.JK_sym(ob, D)
+    with rc.Basis(Z, R, name) as b:
+        n = b.nbf
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, D, schwarz_tau=0.0, emulated=True)
+        assert np.abs(J - Jr).max() < 1e-12
+        assert np.abs(K - Kr).max() < 1e-12
+        assert np.abs(J - J.T).max() == 0.0 and np.abs(K - K.T).max() == 0.0
+
+
+def test_emulated_fp64_full_size_h2o8(gpu):
+    """(H2O)8, 104 functions: emulated vs native FP64 J and K at 1e-12, the
+    energy at fixed density at 1e-11, and the graph rebuilt when the form
+    switches back and forth."""
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o8_631g")
+    D = _sym_density(np.random.default_rng(2), 104)
+    with rc.Basis(Z, R, bname) as b:
+        J, K = np.zeros((104, 104)), np.zeros((104, 104))
+        Je, Ke = np.zeros((104, 104)), np.zeros((104, 104))
+        rc.JK_direct(J, K, b, D)
+        rc.JK_direct(Je, Ke, b, D, emulated=True)
+        assert np.abs(Je - J).max() < 1e-12
+        assert np.abs(Ke - K).max() < 1e-12
+        assert abs(float(np.sum(D * (2 * (Je - J) - (Ke - K))))) < 1e-11
+        J2, K2 = np.zeros((104, 104)), np.zeros((104, 104))
+        rc.JK_direct(J2, K2, b, D)  # FP64 atomics: summation order varies between builds
+        assert np.abs(J2 - J).max() < 1e-13 and np.abs(K2 - K).max() < 1e-13
+        chosen = b.autotune(emulated=True)
+        assert len(chosen) == 42
+        rc.JK_direct(J2, K2, b, D, emulated=True)
+        assert np.abs(J2 - J).max() < 1e-12 and np.abs(K2 - K).max() < 1e-12
+        # emulated under the mixed form: FP32 below 1e-6, double-float above
+        Jm, Km = np.zeros((104, 104)), np.zeros((104, 104))
+        rc.JK_direct(Jm, Km, b, D, fp32_tau=1e-6, emulated=True)
+        assert np.abs(Jm - J).max() < 1e-8 and np.abs(Km - K).max() < 1e-8
+
+
+def test_emulated_fp64_device_and_batch(gpu):
+    """Device pointers and a six-geometry batch in the emulated form."""
+    import torch
+
+    import rchem_gb300 as rc
+
+    geoms = rc.geometry.water_batch(6, seed=3)
+    bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
+    rng = np.random.default_rng(5)
+    Dh = np.zeros(bb.packed)
+    for g in range(bb.ngeom):
+        n = int(bb.geom_nbf[g])
+        bb.block(Dh, g)[:] = _sym_density(rng, n)
+    D = torch.from_numpy(Dh).cuda()
+    J, K = torch.empty_like(D), torch.empty_like(D)
+    Je, Ke = torch.empty_like(D), torch.empty_like(D)
+    rc.batch.jk(bb, D, J, K)
+    rc.batch.jk(bb, D, Je, Ke, emulated=True)
+    assert float((Je - J).abs().max()) < 1e-12
+    assert float((Ke - K).abs().max()) < 1e-12
+    bb.close()

@@ -52,3 +52,17 @@ def test_rhf_energy_variational_and_virial(gpu):
     assert float((D @ S @ D - D).abs().max()) < 1e-7
     comm = F @ D @ S - S @ D @ F
     assert float(comm.abs().max()) < 1e-5
+
+
+def test_rhf_emulated_fp64_energy(gpu):
+    """(H2O)8, 6-31G-shaped basis: the SCF on the emulated-FP64 Fock build
+    lands on the FP64 energy within 1e-9 Eh."""
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o8_631g")
+    with rc.Basis(Z, R, bname) as b:
+        e64 = rc.scf.rhf(b, thresh_e=1e-11)
+        eem = rc.scf.rhf(b, thresh_e=1e-11, emulated=True)
+    assert e64["converged"] and eem["converged"]
+    assert abs(eem["e_total"] - e64["e_total"]) < 1e-9
+    assert float((eem["D"] - e64["D"]).abs().max()) < 1e-7
