@@ -101,14 +101,36 @@ class Emitter:
 
 
 def gen_vrr(la, lb, lc, ld, choose):
-    """Returns (code lines, list of (target e, f) in accumulator order, op counts)."""
+    """Returns (emitter, list of (target e, f) in accumulator order, L).
+
+    The recurrence DAG is built first, then emitted as explicit FMA chains
+    (``rchem_fma``: one DFMA each in FP64, a fused double-float operation in
+    the emulated form).  A target integral that no other term reads is folded
+    straight into its accumulator: acc = fma(X1, a, acc) ... instead of a
+    product, the chain and a separate add, one instruction fewer per target and
+    the same FLOPs."""
     E, F = la + lb, lc + ld
     L = E + F
     em = Emitter()
     memo = {}
+    terms = {}   # node name -> list of terms
+    order = []   # node names, children first
+    uses = {}    # node name -> number of reads by other nodes
+    coefs = set()
 
     def name(e, f, m):
         return "v_%d%d%d_%d%d%d_%d" % (e + f + (m,))
+
+    def use(v):
+        if not v.startswith("F["):
+            uses[v] = uses.get(v, 0) + 1
+        return v
+
+    def coef(kind, n):
+        if n == 1:
+            return kind
+        coefs.add((kind, n))
+        return "%s_%d" % (kind, n)
 
     def node(e, f, m):
         key = (e, f, m)
@@ -117,49 +139,67 @@ def gen_vrr(la, lb, lc, ld, choose):
         if sum(e) == 0 and sum(f) == 0:
             memo[key] = "F[%d]" % m
             return memo[key]
-        terms = []
+        # term kinds: ("mul", X, a) products, ("half", c, rho, a, b) = c*(a - rho*b)
         if sum(f) == 0:
             i = choose(e)
             e1 = sub(e, i)
-            a = node(e1, f, m)
-            b = node(e1, f, m + 1)
-            expr = "PA%s*%s + WP%s*%s" % (XYZ[i], a, XYZ[i], b)
+            t = [("mul", "PA" + XYZ[i], node(e1, f, m)), ("mul", "WP" + XYZ[i], node(e1, f, m + 1))]
             nf, nm = 1, 1
             if e1[i] > 0:
                 e2 = sub(e1, i)
-                c = node(e2, f, m)
-                d = node(e2, f, m + 1)
-                expr = "%s + R(%d)*ohp*(%s - rho_p*%s)" % (expr, e1[i], c, d)
+                t.append(("half", coef("ohp", e1[i]), "rho_p", node(e2, f, m), node(e2, f, m + 1)))
                 nf += 2
-                nm += 0 if e1[i] == 1 else 0
         else:
             i = choose(f)
             f1 = sub(f, i)
-            a = node(e, f1, m)
-            b = node(e, f1, m + 1)
-            expr = "QC%s*%s + WQ%s*%s" % (XYZ[i], a, XYZ[i], b)
+            t = [("mul", "QC" + XYZ[i], node(e, f1, m)), ("mul", "WQ" + XYZ[i], node(e, f1, m + 1))]
             nf, nm = 1, 1
             if f1[i] > 0:
                 f2 = sub(f1, i)
-                c = node(e, f2, m)
-                d = node(e, f2, m + 1)
-                expr = "%s + R(%d)*ohq*(%s - rho_q*%s)" % (expr, f1[i], c, d)
+                t.append(("half", coef("ohq", f1[i]), "rho_q", node(e, f2, m), node(e, f2, m + 1)))
                 nf += 2
             if e[i] > 0:
-                g = node(sub(e, i), f1, m + 1)
-                expr = "%s + R(%d)*ohpq*%s" % (expr, e[i], g)
+                t.append(("mul", coef("ohpq", e[i]), node(sub(e, i), f1, m + 1)))
                 nf += 1
+        for term in t:
+            for v in term[2:]:
+                if term[0] == "mul" or v != term[2]:
+                    use(v)
         nm_ = name(e, f, m)
-        em.emit("const R %s = %s;" % (nm_, expr))
+        terms[nm_] = t
+        order.append(nm_)
         em.nfma += nf
         em.nmul += nm
         memo[key] = nm_
         return nm_
 
+    def chain(t, start):
+        s_ = start
+        for term in t:
+            if term[0] == "mul":
+                _, X, a = term
+                s_ = "%s*%s" % (X, a) if s_ is None else "rchem_fma(%s, %s, %s)" % (X, a, s_)
+            else:
+                _, c, rho, a, b = term
+                s_ = "rchem_fma(%s, rchem_fma(-%s, %s, %s), %s)" % (c, rho, b, a, s_)
+        return s_
+
     targets = [(e, f) for e in comps_range(la, E) for f in comps_range(lc, F)]
-    for k, (e, f) in enumerate(targets):
-        v = node(e, f, 0)
-        em.emit("acc[%d] += %s;" % (k, v))
+    tnames = [node(e, f, 0) for (e, f) in targets]
+    slot = {v: k for k, v in enumerate(tnames)}
+    for kind, n in sorted(coefs):
+        em.emit("const R %s_%d = R(%d)*%s;" % (kind, n, n, kind))
+    folded = set()
+    for v in order:
+        if v in slot and uses.get(v, 0) == 0 and tnames.count(v) == 1:
+            k = slot[v]
+            em.emit("acc[%d] = %s;" % (k, chain(terms[v], "acc[%d]" % k)))
+            folded.add(v)
+        else:
+            em.emit("const R %s = %s;" % (v, chain(terms[v], None)))
+    for k, v in enumerate(tnames):
+        if v not in folded:
+            em.emit("acc[%d] += %s;" % (k, v))
         em.nmul += 1
     return em, targets, L
 
@@ -187,7 +227,7 @@ def gen_hrr(la, lb, lc, ld, targets, choose):
         x = bra(add(a, i), b1, f)
         y = bra(a, b1, f)
         nm = "hb_%d%d%d_%d%d%d_%d%d%d" % (a + b + f)
-        em.emit("const R %s = %s + AB%s*%s;" % (nm, x, XYZ[i], y))
+        em.emit("const R %s = rchem_fma(AB%s, %s, %s);" % (nm, XYZ[i], y, x))
         em.nfma += 1
         bra_memo[key] = nm
         return nm
@@ -207,7 +247,7 @@ def gen_hrr(la, lb, lc, ld, targets, choose):
         x = ket(a, b, add(c, i), d1)
         y = ket(a, b, c, d1)
         nm = "hk_%d%d%d_%d%d%d_%d%d%d_%d%d%d" % (a + b + c + d)
-        em.emit("const R %s = %s + CD%s*%s;" % (nm, x, XYZ[i], y))
+        em.emit("const R %s = rchem_fma(CD%s, %s, %s);" % (nm, XYZ[i], y, x))
         em.nfma += 1
         ket_memo[key] = nm
         return nm

@@ -18,6 +18,7 @@ def main(argv=None):
     ap.add_argument("--workload", default="h2o8_631g")
     ap.add_argument("--builds", type=int, default=3)
     ap.add_argument("--fp32-tau", type=float, default=0.0)
+    ap.add_argument("--emulated", action="store_true", help="double-float arithmetic for the FP64 quartets")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
@@ -34,7 +35,7 @@ def main(argv=None):
     D = torch.from_numpy(X @ X.T / n * 0.1).cuda()
     J, K = torch.empty_like(D), torch.empty_like(D)
     for _ in range(a.builds):
-        JK_direct(J, K, b, D, fp32_tau=a.fp32_tau)
+        JK_direct(J, K, b, D, fp32_tau=a.fp32_tau, emulated=a.emulated)
     torch.cuda.synchronize()
     print(json.dumps(b.class_stats()))
     b.close()
