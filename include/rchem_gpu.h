@@ -164,6 +164,19 @@ int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K
 int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
 
 /*
+ * Batched symmetric eigensolver for the batched SCF (no counterpart in the
+ * reference, whose SCF diagonalises one matrix at a time through
+ * ndarray-linalg's eigh, src/bin/rchem.rs:44,75): A[batch][n][n] (the lower
+ * triangle is read) -> w[batch][n] ascending and V[batch][n][n] with the
+ * eigenvectors as columns (row-major: V[b][i][k] is component i of vector k),
+ * the layout LAPACK dsyevd returns.  One thread block per matrix, cyclic
+ * Jacobi in FP64 in shared memory.  n <= 64 (RCHEM_ERR_UNSUPPORTED above).
+ * Device arrays only; queued on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream) without synchronising.
+ */
+int rchem_eigh_batched(int n, int batch, const double *A, double *w, double *V, void *stream);
+
+/*
  * Autotune the Fock build's tile shapes for this basis and these thresholds
  * (no counterpart in the reference): for every integral class list (21
  * classes x {FP64, FP32}) time the list alone under each candidate number of

@@ -71,6 +71,7 @@ def lib():
     L.rchem_jk_direct_noalloc.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_gradient.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_autotune.argtypes = [vp, p(JKOpts), vp]
+    L.rchem_eigh_batched.argtypes = [i, i, vp, vp, vp, vp]
     L.rchem_jk_class_stats.argtypes = [vp, vp, vp, vp, vp]
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
@@ -107,5 +108,5 @@ def exported_symbols():
         "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
-        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats",
+        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_eigh_batched",
     ]

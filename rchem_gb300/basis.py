@@ -38,6 +38,19 @@ def _ptr(x):
     return x.ctypes.data
 
 
+def _after_torch(basis, *xs):
+    """The library queues its work on the handle's own stream.  When CUDA
+    tensors are passed, work still queued on torch's current stream (producing
+    an input, or reading a buffer the call overwrites) must finish first,
+    unless the handle already runs on that stream (Basis.set_stream)."""
+    if any(_is_cuda(x) for x in xs):
+        import torch
+
+        cur = torch.cuda.current_stream()
+        if getattr(basis, "_stream", None) != cur.cuda_stream:
+            cur.synchronize()
+
+
 class Basis:
     """A basis on the GPU: shells, shell pairs, Schwarz bounds, Boys tables."""
 
@@ -81,6 +94,7 @@ class Basis:
     def set_stream(self, stream_ptr: int):
         """Run this basis' work on a caller-owned CUDA stream (e.g. torch's)."""
         _lib.check(_lib.lib().rchem_basis_set_stream(self.handle, C.c_void_p(stream_ptr)))
+        self._stream = stream_ptr
 
     def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
         """Pick the Fock build's tile shape per integral class for this basis
@@ -128,6 +142,7 @@ def _onee(fn, basis, device=False):
         import torch
 
         out = torch.empty((basis.nbf, basis.nbf), dtype=torch.float64, device="cuda")
+        _after_torch(basis, out)
     _lib.check(fn(basis.handle, C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))
     return out
 
@@ -156,6 +171,7 @@ def moment(basis: Basis, center, order, device=False):
         import torch
 
         out = torch.empty((basis.nbf, basis.nbf), dtype=torch.float64, device="cuda")
+        _after_torch(basis, out)
     _lib.check(_lib.lib().rchem_moment(basis.handle, c.ctypes.data, int(order[0]), int(order[1]), int(order[2]),
                                        C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))
     return out
@@ -181,6 +197,7 @@ def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=F
             raise ValueError("expected %dx%d matrices" % (n, n))
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
                     where=_lib.DEVICE if dev else _lib.HOST, emulated=1 if emulated else 0)
+    _after_torch(basis, D, J, K)
     _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
                                           C.c_void_p(_ptr(K)), C.byref(o)))
 
@@ -191,6 +208,7 @@ def build_I(basis: Basis, device=False):
         import torch
 
         out = torch.empty((n, n, n, n), dtype=torch.float64, device="cuda")
+        _after_torch(basis, out)
     else:
         out = np.empty((n, n, n, n), dtype=np.float64)
     _lib.check(_lib.lib().rchem_build_I(basis.handle, C.c_void_p(_ptr(out)), _lib.DEVICE if device else _lib.HOST))

@@ -5,7 +5,8 @@ each Fock build is one CUDA-graph launch whose class kernels cover the
 quartets of all geometries (quartets never couple two geometries).  Matrices
 are packed: geometry g's n_g x n_g block starts at ``offsets[g]``.  The SCF
 iterations run in FP64 on the GPU, batched over geometries of equal basis size
-(``torch.linalg.eigh`` on stacks), with per-geometry DIIS.
+(the library's batched Jacobi eigensolver on stacks of Fock matrices), with
+per-geometry DIIS.
 
 The reference builds one molecule per process (src/bin/rchem.rs:10-90); this
 is new capability, with the reference's energy conventions.
@@ -17,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .basis import Basis
+from .basis import Basis, _after_torch
 from .bse import expand_shells, load_bse
 
 
@@ -81,14 +82,36 @@ def _packed_matrix(fn, bb: BatchBasis):
     import torch
 
     out = torch.empty(bb.packed, dtype=torch.float64, device="cuda")
+    _after_torch(bb, out)
     _lib.check(fn(bb.handle, C.c_void_p(out.data_ptr()), _lib.DEVICE))
     return out
+
+
+def eigh(A):
+    """Eigenvalues (ascending) and eigenvectors (columns) of a batch of small
+    symmetric FP64 CUDA matrices (..., n, n), n <= 64, through
+    rchem_eigh_batched (one thread block per matrix, cyclic Jacobi), queued on
+    torch's current stream.  Reads the lower triangle, like torch.linalg.eigh."""
+    import torch
+
+    if not (A.is_cuda and A.dtype == torch.float64):
+        raise ValueError("eigh takes CUDA float64 matrices")
+    n = A.shape[-1]
+    lead = A.shape[:-2]
+    A = A.reshape(-1, n, n).contiguous()
+    w = torch.empty(A.shape[:-1], dtype=torch.float64, device=A.device)
+    V = torch.empty_like(A)
+    _lib.check(_lib.lib().rchem_eigh_batched(n, A.shape[0], C.c_void_p(A.data_ptr()), C.c_void_p(w.data_ptr()),
+                                             C.c_void_p(V.data_ptr()),
+                                             C.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)))
+    return w.reshape(*lead, n), V.reshape(*lead, n, n)
 
 
 def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
     """One Fock build over every geometry: packed device vectors D -> J, K."""
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
                     emulated=1 if emulated else 0)
+    _after_torch(bb, D, J, K)
     _lib.check(_lib.lib().rchem_jk_direct(bb.handle, C.c_void_p(D.data_ptr()), C.c_void_p(J.data_ptr()),
                                           C.c_void_p(K.data_ptr()), C.byref(o)))
 
@@ -123,7 +146,7 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
     for grp in groups:
         n, gs, idx, no = grp
         Sg = gather(S, grp)
-        w, U = torch.linalg.eigh(Sg)
+        w, U = eigh(Sg)
         X = (U * w.rsqrt().unsqueeze(-2)) @ U.transpose(-1, -2)
         st.append({"X": X, "S": Sg, "H": gather(H, grp), "focks": [], "errs": []})
 
@@ -133,7 +156,7 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
         for grp, s_, F in zip(groups, st, Fs):
             n, gs, idx, no = grp
             X = s_["X"]
-            eps, Cp = torch.linalg.eigh(X.transpose(-1, -2) @ F @ X)
+            eps, Cp = eigh(X.transpose(-1, -2) @ F @ X)
             Cm = X @ Cp
             Co = Cm[..., :no]
             D[idx] = (Co @ Co.transpose(-1, -2)).reshape(-1)
@@ -199,7 +222,7 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
         Fg = gather(F, grp)
         e_g[gs] = ((s_["H"] + Fg) * gather(D, grp)).sum(dim=(-1, -2)).cpu().numpy()
         X = s_["X"]
-        eps, Cp = torch.linalg.eigh(X.transpose(-1, -2) @ Fg @ X)
+        eps, Cp = eigh(X.transpose(-1, -2) @ Fg @ X)
         Cm = X @ Cp
         Co = Cm[..., :no]
         W[idx] = ((Co * eps[..., :no].unsqueeze(-2)) @ Co.transpose(-1, -2)).reshape(-1)
@@ -220,6 +243,7 @@ def gradient_batch(bb: BatchBasis, res: dict, schwarz_tau=1e-12):
 
     g = torch.empty(3 * len(bb.atomnos), dtype=torch.float64, device="cuda")
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=0.0, where=_lib.DEVICE)
+    _after_torch(bb, res["D"], res["W"], g)
     _lib.check(_lib.lib().rchem_gradient(bb.handle, C.c_void_p(res["D"].data_ptr()), C.c_void_p(res["W"].data_ptr()),
                                          C.c_void_p(g.data_ptr()), C.byref(o)))
     G = g.view(-1, 3).cpu().numpy()

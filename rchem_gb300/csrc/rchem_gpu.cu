@@ -25,6 +25,7 @@
 #include "_gen/eri_classes.h"
 #include "_gen/eri_dispatch.h"
 #include "boys.cuh"
+#include "eigh.cuh"
 #include "eri_kernel.cuh"
 #include "grad.cuh"
 #include "md.cuh"
@@ -1608,5 +1609,30 @@ extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(b->stream));
     b->last_stats = b->plan_stats;
+    return RCHEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched symmetric eigensolver (the batched SCF's diagonalisations)
+// ---------------------------------------------------------------------------
+extern "C" int rchem_eigh_batched(int n, int batch, const double *A, double *w, double *V, void *stream) {
+    if (n < 1 || n > RCHEM_EIGH_MAXN)
+        return set_err(RCHEM_ERR_UNSUPPORTED, "rchem_eigh_batched: n = %d outside 1..%d", n, RCHEM_EIGH_MAXN);
+    if (batch < 0) return set_err(RCHEM_ERR_INVALID, "rchem_eigh_batched: batch = %d", batch);
+    if (batch == 0) return RCHEM_OK;
+    if (!A || !w || !V) return set_err(RCHEM_ERR_INVALID, "rchem_eigh_batched: null array");
+    const void *ptrs[3] = {A, w, V};
+    for (const void *ptr : ptrs) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess ||
+            (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+            cudaGetLastError();
+            return set_err(RCHEM_ERR_INVALID, "rchem_eigh_batched: A, w and V must be device arrays");
+        }
+    }
+    const size_t smem = eigh_smem_bytes(n);
+    CK(cudaFuncSetAttribute(k_eigh_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_eigh_jacobi<<<batch, RCHEM_EIGH_THREADS, smem, (cudaStream_t)stream>>>(n, A, w, V, nullptr);
+    CK(cudaGetLastError());
     return RCHEM_OK;
 }

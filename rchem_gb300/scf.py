@@ -127,6 +127,7 @@ def gradient(basis: _b.Basis, res: dict | None = None, schwarz_tau: float = 1e-1
     W = res["W"].contiguous()
     g = torch.empty(3 * len(basis.atomnos), dtype=torch.float64, device=D.device)
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=0.0, where=_lib.DEVICE)
+    _b._after_torch(basis, D, W, g)
     _lib.check(_lib.lib().rchem_gradient(basis.handle, C.c_void_p(D.data_ptr()), C.c_void_p(W.data_ptr()),
                                          C.c_void_p(g.data_ptr()), C.byref(o)))
     return g.view(-1, 3)

@@ -62,3 +62,39 @@ def test_batched_rhf_and_gradient_match_single(gpu):
         assert abs(res["e_total"][g] - r1["e_total"]) < 1e-9, g
         np.testing.assert_allclose(grads[g], g1, atol=1e-7, rtol=0)
     bb.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 13, 26, 39, 64])
+def test_eigh_batched_vs_lapack(gpu, n):
+    """rchem_eigh_batched against LAPACK (numpy) on random symmetric matrices,
+    one with a degenerate spectrum and the zero matrix: eigenvalues to 1e-13 of
+    the norm, A V = V diag(w), V^T V = I."""
+    import torch
+
+    import rchem_gb300 as rc
+
+    rng = np.random.default_rng(n)
+    X = rng.normal(size=(6, n, n))
+    A = X + X.transpose(0, 2, 1)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+    A[4] = Q @ np.diag(np.repeat(np.arange((n + 2) // 3), 3)[:n].astype(float)) @ Q.T  # triply degenerate
+    A[5] = 0.0
+    At = torch.from_numpy(A).cuda()
+    w, V = rc.batch.eigh(At)
+    torch.cuda.synchronize()
+    w, V = w.cpu().numpy(), V.cpu().numpy()
+    for b in range(A.shape[0]):
+        scale = max(1.0, np.abs(A[b]).max())
+        np.testing.assert_allclose(w[b], np.linalg.eigvalsh(A[b]), atol=1e-13 * scale * n, rtol=0)
+        assert np.all(np.diff(w[b]) >= 0)
+        assert np.abs(A[b] @ V[b] - V[b] * w[b]).max() < 1e-12 * scale * n
+        assert np.abs(V[b].T @ V[b] - np.eye(n)).max() < 1e-13 * n
+
+
+def test_eigh_batched_rejects_large_n(gpu):
+    import torch
+
+    import rchem_gb300 as rc
+
+    with pytest.raises(rc.RchemError):
+        rc.batch.eigh(torch.zeros((2, 65, 65), dtype=torch.float64, device="cuda"))

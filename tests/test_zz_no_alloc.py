@@ -38,6 +38,7 @@ def test_noalloc_matches_jk_direct(gpu, fp32_tau):
             D = torch.from_numpy(_density(n, seed)).cuda()
             J0, K0 = torch.empty_like(D), torch.empty_like(D)
             J1, K1 = torch.full_like(D, np.nan), torch.full_like(D, np.nan)
+            torch.cuda.synchronize()  # the library runs on the handle's own stream
             # the allocating entry point (it also plans the work for these options)
             _lib.check(L.rchem_jk_direct(b.handle, C.c_void_p(D.data_ptr()), C.c_void_p(J0.data_ptr()),
                                          C.c_void_p(K0.data_ptr()), C.byref(opts)))
