@@ -24,9 +24,9 @@
 #define GR_NR 220  // (t,u,v) with t+u+v <= 9
 
 struct GradArgs {
-    const int2 *quartets;  // (bra pair, ket pair) of every surviving quartet
-    int nq;
-    int nbf;
+    const EriTask *tasks;  // warp tasks over the surviving unique quartets
+    const EriSeg *segs;
+    int ntasks;
     const ShellPair *pairs;
     const PairPrim *prims;
     const int *shell_atom;
@@ -149,13 +149,29 @@ __device__ __forceinline__ double gr_dot(const double (*Eb)[GR_NI][GR_NI][GR_NT]
 #define GR_ZD 6                           // bra Hermite box side: la+lb+2 <= 6
 #define GR_ZN (GR_ZD * GR_ZD * GR_ZD)
 
-// One thread per contracted shell quartet (unique, 8-fold): 9 centre derivatives
-// of sum Gamma (ab|cd), weighted by the degeneracy factor, added to the gradient.
+#define GR_MAXC4 1296  // components of a (dd|dd) quartet
+
+// One warp task: up to 32 >> lg unique shell quartets, G = 2^lg lanes each
+// (the segment/task layout of the Fock build).  The G lanes split the
+// quartet's primitive quartets; Gamma (degeneracy and component norms folded
+// in) is formed once per quartet; the 9 centre derivatives are reduced over
+// the G lanes with warp shuffles and added to the gradient by one lane.
 __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= g.nq) return;
-    const int2 q = g.quartets[qi];
-    const ShellPair bp = g.pairs[q.x], kp = g.pairs[q.y];
+    const int lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (w >= g.ntasks) return;  // warp-uniform
+    const EriTask tk = g.tasks[w];
+    const int lgG = (tk.nq_lg >> 8) & 7, nqt = tk.nq_lg & 255;
+    const int G = 1 << lgG, r = lane & (G - 1), qi = lane >> lgG;
+    const bool active = qi < nqt;
+    int sg = tk.seg, off = tk.off + (active ? qi : 0);
+    EriSeg seg = g.segs[sg];
+    while (off >= seg.count) {
+        off -= seg.count;
+        seg = g.segs[++sg];
+    }
+    const ShellPair bp = g.pairs[seg.bra], kp = g.pairs[seg.ket0 + off];
+    const bool same = seg.bra == seg.ket0 + off;
     const int la = g.shell_l[bp.A], lb = g.shell_l[bp.B], lc = g.shell_l[kp.A], ld = g.shell_l[kp.B];
     const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2, nc = (lc + 1) * (lc + 2) / 2,
               nd = (ld + 1) * (ld + 2) / 2;
@@ -164,92 +180,126 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     double deg = 8.0;
     if (bp.diag) deg *= 0.5;
     if (kp.diag) deg *= 0.5;
-    if (q.x == q.y) deg *= 0.5;
+    if (same) deg *= 0.5;
+    // Cartesian components and Gamma, once per quartet
+    int cA[6][3], cB[6][3], cC[6][3], cD[6][3];
+    double nA[6], nB[6], nC[6], nD[6];
+    for (int k = 0; k < na; ++k) {
+        gr_comp(la, k, cA[k]);
+        nA[k] = gr_cnorm(cA[k]);
+    }
+    for (int k = 0; k < nb; ++k) {
+        gr_comp(lb, k, cB[k]);
+        nB[k] = gr_cnorm(cB[k]);
+    }
+    for (int k = 0; k < nc; ++k) {
+        gr_comp(lc, k, cC[k]);
+        nC[k] = gr_cnorm(cC[k]);
+    }
+    for (int k = 0; k < nd; ++k) {
+        gr_comp(ld, k, cD[k]);
+        nD[k] = gr_cnorm(cD[k]);
+    }
+    double Gam[GR_MAXC4];
+    for (int kc = 0; kc < nc; ++kc)
+        for (int kd = 0; kd < nd; ++kd) {
+            const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
+            for (int ka = 0; ka < na; ++ka)
+                for (int kb = 0; kb < nb; ++kb) {
+                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
+                    Gam[((kc * nd + kd) * na + ka) * nb + kb] =
+                        deg * nA[ka] * nB[kb] * nC[kc] * nD[kd] *
+                        (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
+                         0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                }
+        }
     double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
     const int L1 = la + lb + lc + ld + 1;
     const int zd = la + lb + 2;
     double Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], R[GR_NR], F[GR_LMAX + 1];
     double Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
-    for (int ia = 0; ia < bp.npp; ++ia) {
+    const int nk = kp.npp, ntot = active ? bp.npp * nk : 0;  // idle lanes only join the reduction
+    for (int tq = r; tq < ntot; tq += G) {
+        const int ia = tq / nk, ic = tq - ia * nk;
         const PairPrim pa = g.prims[bp.prim0 + ia];
         const double aa = pa.pad, ab = pa.p - pa.pad;  // pad holds the exponent on the first shell
-        for (int ic = 0; ic < kp.npp; ++ic) {
-            const PairPrim pc = g.prims[kp.prim0 + ic];
-            const double ac = pc.pad;
-            const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
-            const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
-            const double T = rho * (X * X + Y * Y + Zc * Zc);
-            boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
-            gr_R(L1, rho, X, Y, Zc, F, R);
-            for (int dd = 0; dd < 3; ++dd) {
-                gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
-                gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
-                for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
-                    for (int j = 0; j <= ld; ++j)
-                        for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
-            }
-            int A[3], B[3], Cc[3], Dd[3], s[3];
-            for (int kc = 0; kc < nc; ++kc) {
-                gr_comp(lc, kc, Cc);
-                const double cnc = gr_cnorm(Cc);
-                const int l_ = kp.aoA + kc;
-                for (int kd = 0; kd < nd; ++kd) {
-                    gr_comp(ld, kd, Dd);
-                    const double cncd = cnc * gr_cnorm(Dd);
-                    const int s_ = kp.aoB + kd;
-                    // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
-                    gr_zvec(Ek, Cc, Dd, R, zd, la + lb + 1, Z0);
-                    for (int x = 0; x < 3; ++x) {
-                        s[0] = Cc[0]; s[1] = Cc[1]; s[2] = Cc[2];
-                        s[x] += 1;
-                        gr_zvec(Ek, s, Dd, R, zd, la + lb, Zp[x]);
-                        if (Cc[x] > 0) {
-                            s[x] -= 2;
-                            gr_zvec(Ek, s, Dd, R, zd, la + lb, Zm[x]);
-                        }
+        const PairPrim pc = g.prims[kp.prim0 + ic];
+        const double ac = pc.pad;
+        const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
+        const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
+        const double T = rho * (X * X + Y * Y + Zc * Zc);
+        boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
+        gr_R(L1, rho, X, Y, Zc, F, R);
+        for (int dd = 0; dd < 3; ++dd) {
+            gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
+            gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
+            for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
+                for (int j = 0; j <= ld; ++j)
+                    for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
+        }
+        int s[3];
+        for (int kc = 0; kc < nc; ++kc) {
+            for (int kd = 0; kd < nd; ++kd) {
+                const double *Gq = Gam + (kc * nd + kd) * na * nb;
+                // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
+                gr_zvec(Ek, cC[kc], cD[kd], R, zd, la + lb + 1, Z0);
+                for (int x = 0; x < 3; ++x) {
+                    s[0] = cC[kc][0];
+                    s[1] = cC[kc][1];
+                    s[2] = cC[kc][2];
+                    s[x] += 1;
+                    gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zp[x]);
+                    if (cC[kc][x] > 0) {
+                        s[x] -= 2;
+                        gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zm[x]);
                     }
-                    for (int ka = 0; ka < na; ++ka) {
-                        gr_comp(la, ka, A);
-                        const double cna = gr_cnorm(A) * cncd;
-                        const int mu = bp.aoA + ka;
-                        for (int kb = 0; kb < nb; ++kb) {
-                            gr_comp(lb, kb, B);
-                            const int nu = bp.aoB + kb;
-                            const double Gam = deg * cna * gr_cnorm(B) *
-                                               (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
-                                                0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] +
-                                                       Dg[mu * n + s_] * Dg[nu * n + l_]));
-                            if (Gam == 0.0) continue;
-                            for (int x = 0; x < 3; ++x) {
-                                // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
-                                s[0] = A[0]; s[1] = A[1]; s[2] = A[2];
-                                s[x] += 1;
-                                double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
-                                if (A[x] > 0) {
-                                    s[x] -= 2;
-                                    v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
-                                }
-                                gA[x] += Gam * v;
-                                // centre B
-                                s[0] = B[0]; s[1] = B[1]; s[2] = B[2];
-                                s[x] += 1;
-                                v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
-                                if (B[x] > 0) {
-                                    s[x] -= 2;
-                                    v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
-                                }
-                                gB[x] += Gam * v;
-                                // centre C
-                                v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
-                                if (Cc[x] > 0) v -= Cc[x] * gr_dot(Eb, A, B, Zm[x], zd);
-                                gC[x] += Gam * v;
+                }
+                for (int ka = 0; ka < na; ++ka) {
+                    const int *A = cA[ka];
+                    for (int kb = 0; kb < nb; ++kb) {
+                        const double Gm = Gq[ka * nb + kb];
+                        if (Gm == 0.0) continue;
+                        const int *B = cB[kb];
+                        for (int x = 0; x < 3; ++x) {
+                            // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
+                            s[0] = A[0];
+                            s[1] = A[1];
+                            s[2] = A[2];
+                            s[x] += 1;
+                            double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
+                            if (A[x] > 0) {
+                                s[x] -= 2;
+                                v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
                             }
+                            gA[x] += Gm * v;
+                            // centre B
+                            s[0] = B[0];
+                            s[1] = B[1];
+                            s[2] = B[2];
+                            s[x] += 1;
+                            v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
+                            if (B[x] > 0) {
+                                s[x] -= 2;
+                                v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
+                            }
+                            gB[x] += Gm * v;
+                            // centre C
+                            v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
+                            if (cC[kc][x] > 0) v -= cC[kc][x] * gr_dot(Eb, A, B, Zm[x], zd);
+                            gC[x] += Gm * v;
                         }
                     }
                 }
             }
         }
     }
+    for (int o = G >> 1; o > 0; o >>= 1)
+        for (int x = 0; x < 3; ++x) {
+            gA[x] += __shfl_xor_sync(0xffffffffu, gA[x], o);
+            gB[x] += __shfl_xor_sync(0xffffffffu, gB[x], o);
+            gC[x] += __shfl_xor_sync(0xffffffffu, gC[x], o);
+        }
+    if (!active || r != 0) return;
     const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A],
               atD = g.shell_atom[kp.B];
     for (int x = 0; x < 3; ++x) {
@@ -284,6 +334,47 @@ __device__ __forceinline__ int geom_of(const GeomDev *geo, int ngeom, long long 
     return lo;
 }
 
+// sum_{tuv} E_x[a_x][b_x][t] E_y[..][u] E_z[..][v] R_{tuv} (R in md_tuv order)
+__device__ __forceinline__ double gr_dot_r(const double (*E)[GR_NI][GR_NI][GR_NT], const int *a, const int *b,
+                                           const double *R) {
+    double s = 0.0;
+    for (int t = 0; t <= a[0] + b[0]; ++t) {
+        const double ex = E[0][a[0]][b[0]][t];
+        for (int u = 0; u <= a[1] + b[1]; ++u) {
+            const double ey = ex * E[1][a[1]][b[1]][u];
+            for (int v = 0; v <= a[2] + b[2]; ++v) s += ey * E[2][a[2]][b[2]][v] * R[md_tuv(t, u, v)];
+        }
+    }
+    return s;
+}
+
+#define GR1_MAXNUC 128  // nuclei of one geometry accumulated in registers/local memory
+
+// 1-D overlap factors S[i][j] = int x_A^i x_B^j exp(-p x_P^2) dx (Obara--Saika),
+// i <= imax, j <= jmax
+__device__ __forceinline__ void gr_s1d(int imax, int jmax, double PA, double PB, double ohp, double p,
+                                       double (*S)[5]) {
+    S[0][0] = sqrt(3.14159265358979323846 / p);
+    for (int i = 0; i <= imax; ++i) {
+        if (i > 0) S[i][0] = PA * S[i - 1][0] + (i > 1 ? ohp * (i - 1) * S[i - 2][0] : 0.0);
+        for (int j = 1; j <= jmax; ++j)
+            S[i][j] = PB * S[i][j - 1] + ohp * ((i > 0 ? i * S[i - 1][j - 1] : 0.0) + (j > 1 ? (j - 1) * S[i][j - 2] : 0.0));
+    }
+}
+
+// 1-D kinetic factor of x_A^i x_B^j: b(2j+1) S_ij - 2b^2 S_i,j+2 - j(j-1)/2 S_i,j-2
+__device__ __forceinline__ double gr_t1d(int i, int j, double b, const double (*S)[5]) {
+    double t = b * (2 * j + 1) * S[i][j] - 2.0 * b * b * S[i][j + 2];
+    if (j >= 2) t -= 0.5 * j * (j - 1) * S[i][j - 2];
+    return t;
+}
+
+// One thread per ordered function pair (mu, nu) of a geometry.  Per primitive
+// pair the Gaussian product, the 1-D overlap table (shared by S and T and by
+// every shifted component) and the Hermite tables are formed once; per
+// nucleus one Boys evaluation and one Hermite Coulomb table serve both shifts
+// in all three directions.  The nuclei's terms are summed over the primitive
+// pairs before any atomic (in a per-thread array for up to GR1_MAXNUC nuclei).
 __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const AOGrad *ao, const ShellGrad *sh,
                          const double *pexp, const double *pcoef, int natoms_total, const double *Z,
                          const double *Ratoms, const double *boys, const double *D, const double *W, double *grad) {
@@ -292,38 +383,86 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
     const GeomDev gm = geo[geom_of(geo, ngeom, idx)];
     const int loc = (int)(idx - gm.moff), mu = gm.ao0 + loc / gm.n, nu = gm.ao0 + loc % gm.n;
     const double Dmn = D[idx], Wmn = W[idx];
+    if (Dmn == 0.0 && Wmn == 0.0) return;
     const AOGrad a = ao[mu], b = ao[nu];
     const ShellGrad sa = sh[a.shell], sb = sh[b.shell];
+    const bool local_nuc = gm.natoms <= GR1_MAXNUC;
     double gH[3] = {0, 0, 0}, gS[3] = {0, 0, 0};
+    double gN[GR1_MAXNUC][3];
+    if (local_nuc)
+        for (int c = 0; c < gm.natoms; ++c) gN[c][0] = gN[c][1] = gN[c][2] = 0.0;
+    const int L1 = a.lmn[0] + a.lmn[1] + a.lmn[2] + b.lmn[0] + b.lmn[1] + b.lmn[2] + 1;
+    double AB[3], rab2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        AB[d] = sa.R[d] - sb.R[d];
+        rab2 += AB[d] * AB[d];
+    }
     for (int j = 0; j < sb.nprim; ++j) {
         const double eb = pexp[sb.prim0 + j], cb = pcoef[sb.prim0 + j];
         for (int i = 0; i < sa.nprim; ++i) {
             const double ea = pexp[sa.prim0 + i], cc = pcoef[sa.prim0 + i] * cb * a.cn * b.cn;
+            const double p = ea + eb, ohp = 0.5 / p;
+            const double Kab = cc * exp(-ea * eb * rab2 / p);
+            double P[3], PA[3];
+            double S1[3][4][5], E[3][GR_NI][GR_NI][GR_NT];
+            for (int d = 0; d < 3; ++d) {
+                P[d] = (ea * sa.R[d] + eb * sb.R[d]) / p;
+                PA[d] = P[d] - sa.R[d];
+                gr_s1d(a.lmn[d] + 1, b.lmn[d] + 2, PA[d], P[d] - sb.R[d], ohp, p, S1[d]);
+                gr_herm(a.lmn[d] + 1, b.lmn[d], PA[d], AB[d], ohp, E[d]);
+            }
+            // overlap and kinetic of the unshifted and shifted components
+            double s0[3], t0[3];
+            for (int d = 0; d < 3; ++d) {
+                s0[d] = S1[d][a.lmn[d]][b.lmn[d]];
+                t0[d] = gr_t1d(a.lmn[d], b.lmn[d], eb, S1[d]);
+            }
             for (int x = 0; x < 3; ++x) {
-                int up[3] = {a.lmn[0], a.lmn[1], a.lmn[2]}, dn[3] = {a.lmn[0], a.lmn[1], a.lmn[2]};
-                up[x] += 1;
-                dn[x] -= 1;
-                const bool has_dn = a.lmn[x] > 0;
-                // overlap and kinetic
-                double s = 2.0 * ea * md_onee_prim(0, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
-                double t = 2.0 * ea * md_onee_prim(1, sa.R, up, ea, sb.R, b.lmn, eb, sa.R, boys);
-                if (has_dn) {
-                    s -= a.lmn[x] * md_onee_prim(0, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
-                    t -= a.lmn[x] * md_onee_prim(1, sa.R, dn, ea, sb.R, b.lmn, eb, sa.R, boys);
+                const int y = (x + 1) % 3, z = (x + 2) % 3, ax = a.lmn[x], bx = b.lmn[x];
+                const double sy = s0[y] * s0[z], ty = t0[y] * s0[z] + s0[y] * t0[z];
+                double ds = 2.0 * ea * S1[x][ax + 1][bx];
+                double dt = 2.0 * ea * (gr_t1d(ax + 1, bx, eb, S1[x]) * sy + S1[x][ax + 1][bx] * ty);
+                if (ax > 0) {
+                    ds -= ax * S1[x][ax - 1][bx];
+                    dt -= ax * (gr_t1d(ax - 1, bx, eb, S1[x]) * sy + S1[x][ax - 1][bx] * ty);
                 }
-                gS[x] += cc * s;
-                gH[x] += cc * t;
-                // nuclear attraction, each nucleus of this geometry
-                for (int c = gm.atom0; c < gm.atom0 + gm.natoms; ++c) {
-                    double v = 2.0 * ea * md_onee_prim(2, sa.R, up, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
-                    if (has_dn) v -= a.lmn[x] * md_onee_prim(2, sa.R, dn, ea, sb.R, b.lmn, eb, Ratoms + 3 * c, boys);
-                    v *= cc * Z[c];
-                    gH[x] += v;
-                    atomicAdd(grad + 3 * c + x, -4.0 * Dmn * v);
+                gS[x] += Kab * ds * sy;
+                gH[x] += Kab * dt;
+            }
+            // nuclear attraction: one Boys evaluation and R table per nucleus
+            const double vpref = -2.0 * 3.14159265358979323846 / p * Kab;
+            for (int c = 0; c < gm.natoms; ++c) {
+                const int cn = gm.atom0 + c;
+                const double X = P[0] - Ratoms[3 * cn], Y = P[1] - Ratoms[3 * cn + 1], Zc = P[2] - Ratoms[3 * cn + 2];
+                double F[GR_LMAX + 1], R[GR_NR];
+                boys_eval_rt<double>(L1, p * (X * X + Y * Y + Zc * Zc), 1.0, boys, F);
+                gr_R(L1, p, X, Y, Zc, F, R);
+                int s[3];
+                double v3[3];
+                for (int x = 0; x < 3; ++x) {
+                    s[0] = a.lmn[0];
+                    s[1] = a.lmn[1];
+                    s[2] = a.lmn[2];
+                    s[x] += 1;
+                    double v = 2.0 * ea * gr_dot_r(E, s, b.lmn, R);
+                    if (a.lmn[x] > 0) {
+                        s[x] -= 2;
+                        v -= a.lmn[x] * gr_dot_r(E, s, b.lmn, R);
+                    }
+                    v3[x] = v * vpref * Z[cn];
+                    gH[x] += v3[x];
+                }
+                if (local_nuc) {
+                    for (int x = 0; x < 3; ++x) gN[c][x] += v3[x];
+                } else {
+                    for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * cn + x, -4.0 * Dmn * v3[x]);
                 }
             }
         }
     }
+    if (local_nuc)
+        for (int c = 0; c < gm.natoms; ++c)
+            for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * (gm.atom0 + c) + x, -4.0 * Dmn * gN[c][x]);
     for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * sa.atom + x, 4.0 * Dmn * gH[x] - 4.0 * Wmn * gS[x]);
     (void)natoms_total;
 }

@@ -28,6 +28,7 @@
 #include "eigh.cuh"
 #include "eri_kernel.cuh"
 #include "grad.cuh"
+#include "grad_cls.cuh"
 #include "md.cuh"
 #include "rchem_types.h"
 
@@ -344,8 +345,11 @@ struct rchem_basis_s {
     float *d_D32 = nullptr;
     // gradient: shell atoms / angular momenta, surviving quartets, W, result
     int *d_shell_atom = nullptr, *d_shell_l = nullptr;
-    int2 *d_gq = nullptr;
+    EriTask *d_gtasks = nullptr;  // the gradient's warp tasks (grouped by class) and segments
+    EriSeg *d_gsegs = nullptr;
     long long gq_n = 0;
+    long long gtask_off[RCHEM_NCLASS + 1] = {}, gtask_cnt[RCHEM_NCLASS + 1] = {};
+    double gtask_cost[RCHEM_NCLASS + 1] = {};
     double gq_tau = -1.0;
     double *d_W = nullptr, *d_grad = nullptr;
 };
@@ -354,7 +358,7 @@ static void free_basis(rchem_basis b) {
     if (!b) return;
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_primsdf, b->d_Ddf, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
                     b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
-                    b->d_shell_atom, b->d_shell_l, b->d_gq, b->d_W, b->d_grad, b->d_geom};
+                    b->d_shell_atom, b->d_shell_l, b->d_gtasks, b->d_gsegs, b->d_W, b->d_grad, b->d_geom};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
@@ -580,6 +584,32 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
 // this many primitive quartets
 static const int kMinPrimPerLane = 16;
 
+// Pack the run of segments sv[s0..] (total quartets) into warp tasks of
+// 32 >> lg quartets each, G = 2^lg lanes per quartet.
+static void pack_tasks(const std::vector<EriSeg> &sv, int s0, long long total, int lg, long long cost,
+                       std::vector<EriTask> &out) {
+    const int perwarp = 32 >> lg;
+    int sg = s0, off = 0;
+    long long left = total;
+    while (left > 0) {
+        const int nl = (int)std::min<long long>(perwarp, left);
+        out.push_back(EriTask{sg, off, nl | (lg << 8), (int)std::min<long long>(cost, 1 << 30)});
+        int adv = nl;
+        while (adv > 0) {
+            const int rem = sv[sg].count - off;
+            if (adv < rem) {
+                off += adv;
+                adv = 0;
+            } else {
+                adv -= rem;
+                ++sg;
+                off = 0;
+            }
+        }
+        left -= nl;
+    }
+}
+
 static int plan_tasks(rchem_basis b, double tau, double tau32) {
     if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32) return RCHEM_OK;
     std::vector<EriSeg> segs[RCHEM_NCLASS][2];
@@ -619,28 +649,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 int lg = 0;
                 const long long ppl = b->ppl[k][prec];
                 while (lg < 5 && nprimq >= ppl << (lg + 1)) ++lg;
-                const int perwarp = 32 >> lg;
-                // pack the run of segments into full warps
-                int sg = s0, off = 0;
-                long long left = total;
-                while (left > 0) {
-                    const int nl = (int)std::min<long long>(perwarp, left);
-                    const long long cost = (nprimq + (1 << lg) - 1) >> lg;
-                    lists[k][prec].push_back(EriTask{sg, off, nl | (lg << 8), (int)std::min<long long>(cost, 1 << 30)});
-                    int adv = nl;
-                    while (adv > 0) {
-                        const int rem = sv[sg].count - off;
-                        if (adv < rem) {
-                            off += adv;
-                            adv = 0;
-                        } else {
-                            adv -= rem;
-                            ++sg;
-                            off = 0;
-                        }
-                    }
-                    left -= nl;
-                }
+                pack_tasks(sv, s0, total, lg, (nprimq + (1 << lg) - 1) >> lg, lists[k][prec]);
                 const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
                 b->list_flops[k][prec] += fl;
                 b->class_quartets[k][prec] += total;
@@ -1102,34 +1111,69 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
 
 // every unique surviving quartet (bra pair >= ket pair in the class order), as
 // for the Fock build, for the one-thread-per-quartet gradient kernel
+// The gradient's work plan: the Schwarz-screened unique quartets of every
+// (bra group, ket group) combination as segments, packed into warp tasks with
+// G lanes per quartet (at least kGradPrimPerLane primitive quartets per lane:
+// a derivative primitive quartet is ~100x a Fock one), heaviest tasks first.
 static int plan_gradient(rchem_basis b, double tau) {
-    if (b->d_gq && b->gq_tau == tau) return RCHEM_OK;
-    std::vector<int2> q;
+    if (b->d_gtasks && b->gq_tau == tau) return RCHEM_OK;
+    constexpr long long kGradPrimPerLane = 2;
+    std::vector<EriSeg> segs;
+    std::vector<EriTask> per_class[RCHEM_NCLASS + 1];
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
         for (int gki = b->geom_group_begin[gb.geom]; gki < b->geom_group_end[gb.geom]; ++gki) {
             const PairGroup &gk = b->groups[gki];
             if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
+            const long long nprimq = (long long)gb.npp * gk.npp;
+            const int L = gb.la + gb.lb + gk.la + gk.lb;
+            const int s0 = (int)segs.size();
+            long long total = 0;
             for (int ib = gb.begin; ib < gb.end; ++ib) {
                 const double Qb = P[ib].Q;
                 if (!(Qb > 0.0)) continue;
                 int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
                 if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
-                for (int j = 0; j < nk; ++j) q.push_back(make_int2(ib, gk.begin + j));
+                if (nk <= 0) continue;
+                segs.push_back(EriSeg{ib, gk.begin, nk, 0});
+                total += nk;
             }
+            if (total == 0) continue;
+            int lg = 0;
+            while (lg < 5 && nprimq >= kGradPrimPerLane << (lg + 1)) ++lg;
+            const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
+            // s/p classes each get their specialised kernel; every class with a d
+            // shell shares one launch of the run-time kernel (list RCHEM_NCLASS)
+            const int k = quartet_kernel(gb.cls, gk.cls);
+            const int *l = rchem_class_l[k];
+            const int list = (l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1) ? k : RCHEM_NCLASS;
+            pack_tasks(segs, s0, total, lg, ((nprimq + (1 << lg) - 1) >> lg) * work, per_class[list]);
         }
     }
-    if (b->d_gq) cudaFree(b->d_gq);
-    b->d_gq = nullptr;
+    // one launch per class (its specialised kernel), heaviest tasks first
+    std::vector<EriTask> tasks;
+    for (int k = 0; k <= RCHEM_NCLASS; ++k) {
+        std::vector<EriTask> &L = per_class[k];
+        std::stable_sort(L.begin(), L.end(), [](const EriTask &x, const EriTask &y) { return x.cost > y.cost; });
+        b->gtask_off[k] = (long long)tasks.size();
+        b->gtask_cnt[k] = (long long)L.size();
+        b->gtask_cost[k] = 0.0;
+        for (const EriTask &t : L) b->gtask_cost[k] += (double)t.cost;
+        tasks.insert(tasks.end(), L.begin(), L.end());
+    }
+    if (b->d_gtasks) cudaFree(b->d_gtasks);
+    if (b->d_gsegs) cudaFree(b->d_gsegs);
+    b->d_gtasks = nullptr;
+    b->d_gsegs = nullptr;
     b->gq_n = 0;
-    CKR(upload(&b->d_gq, q, b->stream));
+    CKR(upload(&b->d_gtasks, tasks, b->stream));
+    CKR(upload(&b->d_gsegs, segs, b->stream));
     CK(cudaStreamSynchronize(b->stream));
-    b->gq_n = (long long)q.size();
+    b->gq_n = (long long)tasks.size();
     b->gq_tau = tau;
     return RCHEM_OK;
 }
-
 extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad,
                               const rchem_jk_opts *opts) {
     if (!b || !D || !W || !grad) return set_err(RCHEM_ERR_INVALID, "null argument");
@@ -1160,9 +1204,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
     CK(cudaMemcpyAsync(b->d_grad, gnuc.data(), 3 * (size_t)na * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     if (b->gq_n > 0) {
         GradArgs g;
-        g.quartets = b->d_gq;
-        g.nq = (int)b->gq_n;
-        g.nbf = 0;
+        g.segs = b->d_gsegs;
         g.pairs = b->d_pairs;
         g.prims = b->d_prims;
         g.shell_atom = b->d_shell_atom;
@@ -1170,8 +1212,45 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         g.boys64 = b->tabs->boys64;
         g.D = b->d_D;
         g.grad = b->d_grad;
-        k_grad2e<<<(unsigned)((b->gq_n + 63) / 64), 64, 0, b->stream>>>(g);
-        CK(cudaGetLastError());
+        // classes run concurrently: longest first, each onto the least-loaded stream
+        std::vector<int> ks;
+        for (int k = 0; k <= RCHEM_NCLASS; ++k)
+            if (b->gtask_cnt[k] > 0) ks.push_back(k);
+        std::stable_sort(ks.begin(), ks.end(), [&](int x, int y) { return b->gtask_cost[x] > b->gtask_cost[y]; });
+        const int nuse = std::min<int>((int)ks.size(), rchem_basis_s::NAUX);
+        CK(cudaEventRecord(b->ev_fork, b->stream));
+        for (int i = 0; i < nuse; ++i) CK(cudaStreamWaitEvent(b->aux[i], b->ev_fork, 0));
+        double load[rchem_basis_s::NAUX] = {0};
+        for (int k : ks) {
+            int best = 0;
+            for (int j = 1; j < nuse; ++j)
+                if (load[j] < load[best]) best = j;
+            load[best] += b->gtask_cost[k];
+            cudaStream_t st = b->aux[best];
+            g.tasks = b->d_gtasks + b->gtask_off[k];
+            g.ntasks = (int)b->gtask_cnt[k];
+            const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
+            const int *l = rchem_class_l[k < RCHEM_NCLASS ? k : RCHEM_NCLASS - 1];
+#define RCHEM_GRAD_CLS(a_, b_, c_, d_)                                                  \
+    if (k < RCHEM_NCLASS && l[0] == a_ && l[1] == b_ && l[2] == c_ && l[3] == d_) {                          \
+        k_grad2e_cls<a_, b_, c_, d_><<<blocks, 64, 0, st>>>(g);                         \
+        CK(cudaGetLastError());                                                          \
+        continue;                                                                        \
+    }
+            RCHEM_GRAD_CLS(0, 0, 0, 0)
+            RCHEM_GRAD_CLS(1, 0, 0, 0)
+            RCHEM_GRAD_CLS(1, 0, 1, 0)
+            RCHEM_GRAD_CLS(1, 1, 0, 0)
+            RCHEM_GRAD_CLS(1, 1, 1, 0)
+            RCHEM_GRAD_CLS(1, 1, 1, 1)
+#undef RCHEM_GRAD_CLS
+            k_grad2e<<<blocks, 64, 0, st>>>(g);  // classes with d shells: run-time angular momenta
+            CK(cudaGetLastError());
+        }
+        for (int i = 0; i < nuse; ++i) {
+            CK(cudaEventRecord(b->ev_join[i], b->aux[i]));
+            CK(cudaStreamWaitEvent(b->stream, b->ev_join[i], 0));
+        }
     }
     const int th = 128;
     k_grad1e<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(
