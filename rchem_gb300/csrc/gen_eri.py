@@ -317,7 +317,7 @@ def best_hrr(la, lb, lc, ld, targets):
 # chain of NTAY-1 FMAs per evaluated function; every F_m for L <= 1, else F_L
 # and e^{-T} followed by the downward recursion (one FMA + one multiply per m);
 # the prefactor multiplies (L+1 or 2); the grid index (one FMA + one add + one FMA).
-NTAY64 = 8
+NTAY64 = 6
 NTAY32 = 4
 
 
