@@ -399,17 +399,50 @@ static EriArgs base_args(rchem_basis b) {
 }
 
 // Schwarz bounds for every pair (class kernels, diagonal epilogue)
+// Pack the run of segments sv[s0..] (total quartets) into warp tasks of
+// 32 >> lg quartets each, G = 2^lg lanes per quartet.
+static void pack_tasks(const std::vector<EriSeg> &sv, int s0, long long total, int lg, long long cost,
+                       std::vector<EriTask> &out) {
+    const int perwarp = 32 >> lg;
+    int sg = s0, off = 0;
+    long long left = total;
+    while (left > 0) {
+        const int nl = (int)std::min<long long>(perwarp, left);
+        out.push_back(EriTask{sg, off, nl | (lg << 8), (int)std::min<long long>(cost, 1 << 30)});
+        int adv = nl;
+        while (adv > 0) {
+            const int rem = sv[sg].count - off;
+            if (adv < rem) {
+                off += adv;
+                adv = 0;
+            } else {
+                adv -= rem;
+                ++sg;
+                off = 0;
+            }
+        }
+        left -= nl;
+    }
+}
+
 static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     const int np = (int)b->pairs.size();
     std::vector<EriSeg> segs(np);
     for (int i = 0; i < np; ++i) segs[i] = EriSeg{i, i, 1, 0};  // (ab|ab), one quartet per segment
+    // per diagonal class, every geometry's pairs in one launch; G lanes per
+    // quartet so that each lane has at least 4 primitive quartets
+    std::vector<EriTask> per_class[RCHEM_NCLASS];
+    for (const PairGroup &g : b->groups) {
+        const long long nprimq = (long long)g.npp * g.npp;
+        int lg = 0;
+        while (lg < 5 && nprimq >= 4LL << (lg + 1)) ++lg;
+        pack_tasks(segs, g.begin, g.end - g.begin, lg, 0, per_class[quartet_kernel(g.cls, g.cls)]);
+    }
     std::vector<EriTask> tasks;
     std::vector<int> tkern;
-    for (const PairGroup &g : b->groups) {
-        for (int i = g.begin; i < g.end; i += 32) {
-            tasks.push_back(EriTask{i, 0, std::min(32, g.end - i), 0});
-            tkern.push_back(quartet_kernel(g.cls, g.cls));
-        }
+    for (int k = 0; k < RCHEM_NCLASS; ++k) {
+        tasks.insert(tasks.end(), per_class[k].begin(), per_class[k].end());
+        tkern.insert(tkern.end(), per_class[k].size(), k);
     }
     EriTask *d_t = nullptr;
     EriSeg *d_s = nullptr;
@@ -583,32 +616,6 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
 // default tile shape: lanes share a quartet only while each keeps at least
 // this many primitive quartets
 static const int kMinPrimPerLane = 16;
-
-// Pack the run of segments sv[s0..] (total quartets) into warp tasks of
-// 32 >> lg quartets each, G = 2^lg lanes per quartet.
-static void pack_tasks(const std::vector<EriSeg> &sv, int s0, long long total, int lg, long long cost,
-                       std::vector<EriTask> &out) {
-    const int perwarp = 32 >> lg;
-    int sg = s0, off = 0;
-    long long left = total;
-    while (left > 0) {
-        const int nl = (int)std::min<long long>(perwarp, left);
-        out.push_back(EriTask{sg, off, nl | (lg << 8), (int)std::min<long long>(cost, 1 << 30)});
-        int adv = nl;
-        while (adv > 0) {
-            const int rem = sv[sg].count - off;
-            if (adv < rem) {
-                off += adv;
-                adv = 0;
-            } else {
-                adv -= rem;
-                ++sg;
-                off = 0;
-            }
-        }
-        left -= nl;
-    }
-}
 
 static int plan_tasks(rchem_basis b, double tau, double tau32) {
     if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32) return RCHEM_OK;

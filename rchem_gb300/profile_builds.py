@@ -1,5 +1,11 @@
-"""Run a few Fock builds of a named workload for a profiler, then print the
-per-class work of the plan (``python -m rchem_gb300.profile_builds``).
+"""Run a few Fock builds (or gradients) of a named workload for a profiler,
+then print the per-class work of the plan (``python -m rchem_gb300.profile_builds``).
+
+Workloads: the single-geometry configurations of ``rchem_gb300.geometry``
+(h2o_sto3g, h2o8_631g, h2o4_631gss, h2o32_631gs) and ``batch512_631g`` (512
+water monomers/dimers/trimers in one batched handle).  The density (and, with
+``--gradient``, the energy-weighted density) is a seeded random symmetric
+matrix: the kernels do the same work for any density.
 
 Example (the launch list of three FP64 builds of (H2O)8 in the 6-31G-shaped
 basis)::
@@ -13,31 +19,59 @@ import argparse
 import json
 
 
+def _sym(rng, n, scale):
+    X = rng.normal(size=(n, n))
+    return X @ X.T / n * scale
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="h2o8_631g")
     ap.add_argument("--builds", type=int, default=3)
     ap.add_argument("--fp32-tau", type=float, default=0.0)
     ap.add_argument("--emulated", action="store_true", help="double-float arithmetic for the FP64 quartets")
+    ap.add_argument("--gradient", action="store_true", help="run the nuclear gradient instead of Fock builds")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
 
-    from . import geometry
+    from . import batch, geometry
     from .basis import Basis, JK_direct
+    from .scf import gradient
 
-    bname, Z, R = geometry.config(a.workload)
-    b = Basis(Z, R, bname)
-    n = b.nbf
-    s = torch.cuda.Stream()
-    b.set_stream(s.cuda_stream)
-    X = np.random.default_rng(0).normal(size=(n, n))
-    D = torch.from_numpy(X @ X.T / n * 0.1).cuda()
-    J, K = torch.empty_like(D), torch.empty_like(D)
-    for _ in range(a.builds):
-        JK_direct(J, K, b, D, fp32_tau=a.fp32_tau, emulated=a.emulated)
+    rng = np.random.default_rng(0)
+    if a.workload == "batch512_631g":
+        b = batch.BatchBasis(geometry.water_batch(512, seed=7), "6-31g-fit")
+        Dh, Wh = np.zeros(b.packed), np.zeros(b.packed)
+        for g in range(b.ngeom):
+            n = int(b.geom_nbf[g])
+            b.block(Dh, g)[:] = _sym(rng, n, 0.1)
+            b.block(Wh, g)[:] = _sym(rng, n, 0.1)
+        D, W = torch.from_numpy(Dh).cuda(), torch.from_numpy(Wh).cuda()
+        for _ in range(a.builds):
+            if a.gradient:
+                batch.gradient_batch(b, {"D": D, "W": W})
+            else:
+                J, K = torch.empty_like(D), torch.empty_like(D)
+                batch.jk(b, D, J, K, fp32_tau=a.fp32_tau, emulated=a.emulated)
+    else:
+        bname, Z, R = geometry.config(a.workload)
+        b = Basis(Z, R, bname)
+        n = b.nbf
+        s = torch.cuda.Stream()
+        b.set_stream(s.cuda_stream)
+        D = torch.from_numpy(_sym(rng, n, 0.1)).cuda()
+        W = torch.from_numpy(_sym(rng, n, 0.1)).cuda()
+        J, K = torch.empty_like(D), torch.empty_like(D)
+        torch.cuda.synchronize()
+        for _ in range(a.builds):
+            if a.gradient:
+                gradient(b, {"D": D, "W": W})
+            else:
+                JK_direct(J, K, b, D, fp32_tau=a.fp32_tau, emulated=a.emulated)
     torch.cuda.synchronize()
-    print(json.dumps(b.class_stats()))
+    if not a.gradient:
+        print(json.dumps(b.class_stats()))
     b.close()
 
 
