@@ -739,6 +739,8 @@ static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32, bool emu
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < (with32 ? 2 : 1); ++p)
             if (b->task_cnt[k][p] > 0) ls.push_back(L{k, p, b->list_flops[k][p] / (p ? 16.0 : 1.0)});
+    // largest lists first, each onto the least-loaded stream (launching the
+    // lists with the longest single warps first measured slower)
     std::stable_sort(ls.begin(), ls.end(), [](const L &x, const L &y) { return x.cost > y.cost; });
     a.segs = b->d_segs;
     const int nuse = std::min<int>((int)ls.size(), rchem_basis_s::NAUX);
