@@ -185,6 +185,7 @@ def north_star(rc, torch):
     bname, Z, R = rc.geometry.config("h2o32_631gs")
     with rc.Basis(Z, R, bname) as b:
         rc.scf.rhf(b, max_iter=2)  # warm-up: work plan, graph, cuSOLVER initialisation
+        b.autotune(1e-12, 0.0)  # tile shapes per class list (and the large classes' kernel) for this form
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r64 = rc.scf.rhf(b, thresh_e=1e-10)
@@ -195,6 +196,7 @@ def north_star(rc, torch):
                "fp64_flops": st64["flops_fp64"], "scf_fp64_s": t_scf64, "scf_iterations": r64["iterations"],
                "e_total_fp64": r64["e_total"], "mixed": {}}
         for tau32 in (1e-6, 1e-4):
+            b.autotune(1e-12, tau32)
             ms, st = _timed_builds(rc, torch, b, D, tau32)
             t0 = time.perf_counter()
             r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32)
@@ -207,6 +209,7 @@ def north_star(rc, torch):
         # emulated FP64 (double-float on the FP32 pipe), alone and under the mixed form
         rec["emulated"] = {}
         for tau32 in (0.0, 1e-6):
+            b.autotune(1e-12, tau32, emulated=True)
             ms, st = _timed_builds(rc, torch, b, D, tau32, emulated=True)
             r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=True)
             rec["emulated"]["fp32_tau=%g" % tau32] = {
@@ -220,10 +223,11 @@ def north_star(rc, torch):
     bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
     rc.batch.rhf_batch(bb, max_iter=2)  # warm-up (plans, graphs)
     rec = {"geometries": bb.ngeom, "packed_elements": bb.packed, "sizes": sorted(set(bb.geom_nbf.tolist()))}
-    for tag, tau32 in (("fp64", 0.0), ("mixed", 1e-6)):
+    for tag, tau32, emul in (("fp64", 0.0, False), ("mixed", 1e-6, False), ("emulated_mixed", 1e-6, True)):
+        bb.autotune(1e-12, tau32, emulated=emul)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32)
+        r = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         g = rc.batch.gradient_batch(bb, r)
@@ -234,22 +238,26 @@ def north_star(rc, torch):
     D = torch.zeros(bb.packed, dtype=torch.float64, device="cuda")
     J, K = torch.empty_like(D), torch.empty_like(D)
     rc.batch.jk(bb, D, J, K)
-    for tag, tau32 in (("fp64", 0.0), ("mixed", 1e-6)):
-        rc.batch.jk(bb, D, J, K, fp32_tau=tau32)
+    for tag, tau32, emul in (("fp64", 0.0, False), ("mixed", 1e-6, False), ("emulated_mixed", 1e-6, True)):
+        bb.autotune(1e-12, tau32, emulated=emul)
+        rc.batch.jk(bb, D, J, K, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(3):
-            rc.batch.jk(bb, D, J, K, fp32_tau=tau32)
+            rc.batch.jk(bb, D, J, K, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         rec[tag]["fock_build_all_geometries_ms"] = (time.perf_counter() - t0) / 3 * 1e3
-    dE = np.abs(np.asarray(rec["mixed"].pop("e_total")) - np.asarray(rec["fp64"].pop("e_total")))
-    rec["mixed_vs_fp64_max_abs_dE_Eh"] = float(dE.max())
+    e64 = np.asarray(rec["fp64"].pop("e_total"))
+    rec["mixed_vs_fp64_max_abs_dE_Eh"] = float(np.abs(np.asarray(rec["mixed"].pop("e_total")) - e64).max())
+    rec["emulated_mixed_vs_fp64_max_abs_dE_Eh"] = float(
+        np.abs(np.asarray(rec["emulated_mixed"].pop("e_total")) - e64).max())
     out["batch512_631g"] = rec
     bb.close()
 
     bname, Z, R = rc.geometry.config("h2o4_631gss")
     with rc.Basis(Z, R, bname) as b:
         rc.scf.gradient(b, rc.scf.rhf(b))  # warm-up (plans, graphs)
+        b.autotune(1e-12, 0.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         res = rc.scf.rhf(b, thresh_e=1e-10)

@@ -72,6 +72,7 @@ def lib():
     L.rchem_gradient.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_autotune.argtypes = [vp, p(JKOpts), vp]
     L.rchem_eigh_batched.argtypes = [i, i, vp, vp, vp, vp]
+    L.rchem_set_tile_shape.argtypes = [vp, i, i, i]
     L.rchem_jk_class_stats.argtypes = [vp, vp, vp, vp, vp]
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
@@ -109,4 +110,5 @@ def exported_symbols():
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
         "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_eigh_batched",
+        "rchem_set_tile_shape",
     ]

@@ -107,6 +107,11 @@ class Basis:
         _lib.check(_lib.lib().rchem_autotune(self.handle, C.byref(o), chosen.ctypes.data))
         return {(k, p): int(chosen[2 * k + p]) for k in range(21) for p in range(2)}
 
+    def set_tile_shape(self, cls: int, prec: int, ppl: int):
+        """Fix one class list's tile shape (rchem_set_tile_shape): ppl = minimum
+        primitive quartets per lane, 0 = the warp-cooperative kernel."""
+        _lib.check(_lib.lib().rchem_set_tile_shape(self.handle, cls, prec, ppl))
+
     def class_stats(self) -> list:
         """Per integral class of the current work plan: (l_a,l_b,l_c,l_d) with the
         FP64 / FP32 shell quartets, primitive quartets and algorithmic FLOPs."""

@@ -117,7 +117,7 @@ def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False)
 
 
 def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=8, fp32_tau=0.0,
-              schwarz_tau=1e-12):
+              schwarz_tau=1e-12, emulated=False):
     """RHF for every geometry of ``bb`` at once; returns per-geometry energies,
     the packed D and W, iteration count and convergence flags."""
     import torch
@@ -171,7 +171,7 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
     conv = np.zeros(bb.ngeom, dtype=bool)
     e_g = np.zeros(bb.ngeom)
     for it in range(1, max_iter + 1):
-        jk(bb, D, J, K, schwarz_tau, fp32_tau)
+        jk(bb, D, J, K, schwarz_tau, fp32_tau, emulated)
         F = H + 2.0 * J - K
         Fx = []
         for grp, s_ in zip(groups, st):
@@ -213,7 +213,7 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
         e_old = e_g.copy()
         del ddg
     # final energies and W at the converged densities
-    jk(bb, D, J, K, schwarz_tau, fp32_tau)
+    jk(bb, D, J, K, schwarz_tau, fp32_tau, emulated)
     F = H + 2.0 * J - K
     W = torch.empty_like(D)
     Dn = torch.empty_like(D)

@@ -63,12 +63,14 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("eri_") and f.endswith(".cu"))
     nvcc = _nvcc()
 
-    headers = [os.path.join(CSRC, f) for f in ("eri_kernel.cuh", "boys.cuh", "rchem_types.h")]
+    headers = [os.path.join(CSRC, f) for f in ("eri_kernel.cuh", "boys.cuh", "df64.cuh", "rchem_types.h")]
 
     def deps(src):
         base = os.path.basename(src)
         if base.startswith("eri_") and src.startswith(GEN):
-            return [src, os.path.join(GEN, base.replace("eri_", "eri_class_").replace(".cu", ".inc"))] + headers
+            prog = os.path.join(GEN, base.replace("eri_", "eri_prog_").replace(".cu", ".inc"))
+            return ([src, os.path.join(GEN, base.replace("eri_", "eri_class_").replace(".cu", ".inc"))] +
+                    ([prog] if os.path.exists(prog) else []) + headers)
         if base == "peak.cu":
             return [src, os.path.join(INCLUDE, "rchem_bench.h")]
         return [src] + hand + [os.path.join(GEN, "eri_dispatch.h"), os.path.join(GEN, "eri_classes.h")]

@@ -331,12 +331,218 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 
 // prec: 0 = FP64, 1 = FP32 (mixed form), 2 = double-float on the FP32 pipe
 // (emulated FP64; instantiated up to l_a+l_b+l_c+l_d = 4, FP64 above)
+// ---------------------------------------------------------------------------
+// Warp-cooperative J/K kernel for the large classes (EriClass::WC): one warp
+// per contracted shell quartet, the recurrence intermediates in shared
+// memory.  The generated program (EriProg) lists the VRR terms and the HRR
+// terms level by level of their DAG; within a level the terms are independent
+// and the 32 lanes take them in turn, one __syncwarp between levels.  Terms
+// are sorted by branch shape inside a level so lanes mostly agree on it.
+template <int LA, int LB, int LC, int LD> struct EriProg;
+
+#define RCHEM_WC_SMEM (96 * 1024)  // shared memory per block the warp count aims at
+
+template <int LA, int LB, int LC, int LD, typename R>
+struct WcShape {
+    using P = EriProg<LA, LB, LC, LD>;
+    static constexpr int PER_WARP = P::SCR + (P::NT > P::NOUT ? P::NT : P::NOUT);  // elements of R
+    static constexpr int FIT = (int)(RCHEM_WC_SMEM / (PER_WARP * sizeof(R)));
+    static constexpr int WARPS = FIT < 1 ? 1 : (FIT > 4 ? 4 : FIT);
+    static constexpr size_t SMEM = (size_t)WARPS * PER_WARP * sizeof(R);
+};
+
+template <typename R>
+__device__ __forceinline__ R wc_sel3(int i, R a, R b, R c) { return i == 0 ? a : (i == 1 ? b : c); }
+template <typename R>
+__device__ __forceinline__ R wc_sel4(int n, const R *v) {  // v[0..3] = 1..4 times a coefficient
+    return n == 1 ? v[0] : (n == 2 ? v[1] : (n == 3 ? v[2] : v[3]));
+}
+
+template <int LA, int LB, int LC, int LD, typename R>
+__global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
+    using C = EriClass<LA, LB, LC, LD>;
+    using P = EriProg<LA, LB, LC, LD>;
+    using W = WcShape<LA, LB, LC, LD, R>;
+    constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, L = C::L;
+    extern __shared__ __align__(16) unsigned char wc_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    R *S = reinterpret_cast<R *>(wc_smem) + wib * W::PER_WARP;  // terms of the recurrences
+    R *A = S + P::SCR;                                           // accumulators, then the integrals
+    const int w = blockIdx.x * W::WARPS + wib;
+    if (w >= a.ntasks) return;  // warp-uniform
+    const EriTask tk = a.tasks[w];
+    int sg = tk.seg, off = tk.off;
+    EriSeg seg = a.segs[sg];
+    while (off >= seg.count) {
+        off -= seg.count;
+        seg = a.segs[++sg];
+    }
+    const int bidx = seg.bra, kidx = seg.ket0 + off;
+    const ShellPair bp = a.pairs[bidx], kp = a.pairs[kidx];
+    for (int k = lane; k < P::NT; k += 32) A[k] = R(0);
+    const R *btab = Tabs<R>::boys(a);
+    const uint4 *vprog = P::vrr();
+    const int *vlev = P::vrrlv();
+    const int nk = kp.npp, ntot = bp.npp * nk;
+    for (int tq = 0; tq < ntot; ++tq) {
+        const int ia = tq / nk, ic = tq - ia * nk;
+        R p, ohp, Pc[3], PA[3], Kab, q, ohq, Qc[3], QC[3], Kcd;
+        PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, Pc, PA, Kab);
+        PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Qc, QC, Kcd);
+        const R pq = p + q;
+        const R rs = rchem_rsqrt(pq);
+        const R ipq = rs * rs;
+        const R PQx = Pc[0] - Qc[0], PQy = Pc[1] - Qc[1], PQz = Pc[2] - Qc[2];
+        const R qi_ = q * ipq, pi_ = p * ipq;
+        const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
+        R F[L + 1];
+        boys_eval<L, R>(T, Kab * Kcd * rs, btab, F);
+        const R WP[3] = {-qi_ * PQx, -qi_ * PQy, -qi_ * PQz}, WQ[3] = {pi_ * PQx, pi_ * PQy, pi_ * PQz};
+        const R ohpq = R(0.5) * ipq;
+        const R cp[4] = {ohp, ohp + ohp, R(3) * ohp, R(4) * ohp};
+        const R cq[4] = {ohq, ohq + ohq, R(3) * ohq, R(4) * ohq};
+        const R cpq[4] = {ohpq, ohpq + ohpq, R(3) * ohpq, R(4) * ohpq};
+        __syncwarp();  // the previous primitive quartet's terms have been read
+#pragma unroll
+        for (int m = 0; m <= L; ++m)
+            if (lane == m) S[m] = F[m];
+        __syncwarp();
+        for (int lv = 0; lv < P::NVL; ++lv) {
+            const int e = __ldg(vlev + lv + 1);
+            for (int t = __ldg(vlev + lv) + lane; t < e; t += 32) {
+                const uint4 op = __ldg(vprog + t);
+                const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
+                const R X = ket ? wc_sel3(dir, QC[0], QC[1], QC[2]) : wc_sel3(dir, PA[0], PA[1], PA[2]);
+                const R Y = ket ? wc_sel3(dir, WQ[0], WQ[1], WQ[2]) : wc_sel3(dir, WP[0], WP[1], WP[2]);
+                R v = rchem_fma(Y, S[op.y & 0xffff], X * S[op.x >> 16]);
+                if (n1) {
+                    const R c1 = ket ? wc_sel4(n1, cq) : wc_sel4(n1, cp);
+                    v = rchem_fma(c1, rchem_fma(-(ket ? pi_ : qi_), S[op.z & 0xffff], S[op.y >> 16]), v);
+                }
+                if (n2) v = rchem_fma(wc_sel4(n2, cpq), S[op.z >> 16], v);
+                S[op.x & 0xffff] = v;
+            }
+            __syncwarp();
+        }
+        for (int k = lane; k < P::NT; k += 32) A[k] += S[__ldg(P::tgt() + k)];
+    }
+    // HRR on the contracted [e0|f0]
+    __syncwarp();
+    for (int k = lane; k < P::NT; k += 32) S[k] = A[k];
+    R AB[3], CD[3];
+    Tabs<R>::ab(bp, AB);
+    Tabs<R>::ab(kp, CD);
+    __syncwarp();
+    const uint2 *hprog = P::hrr();
+    const int *hlev = P::hrrlv();
+    for (int lv = 0; lv < P::NHL; ++lv) {
+        const int e = __ldg(hlev + lv + 1);
+        for (int t = __ldg(hlev + lv) + lane; t < e; t += 32) {
+            const uint2 op = __ldg(hprog + t);
+            const int dir = (op.y >> 16) & 255, side = op.y >> 24;
+            const R X = side ? wc_sel3(dir, CD[0], CD[1], CD[2]) : wc_sel3(dir, AB[0], AB[1], AB[2]);
+            S[op.x & 0xffff] = rchem_fma(X, S[op.y & 0xffff], S[op.x >> 16]);
+        }
+        __syncwarp();
+    }
+    for (int k = lane; k < P::NOUT; k += 32) A[k] = R(__ldg(P::onorm() + k)) * S[__ldg(P::out() + k)];
+    __syncwarp();
+
+    // degeneracy-weighted 8-fold scatter, the lanes splitting each contraction
+    R deg = R(1);
+    if (bp.diag) deg *= R(0.5);
+    if (kp.diag) deg *= R(0.5);
+    if (bidx == kidx) deg *= R(0.5);
+    const R deg2 = deg + deg;
+    const int n = bp.mn, mo = bp.moff;
+    const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
+#define WIDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
+    for (int t = lane; t < NA * NB; t += 32) {  // J-hat bra: 2 (ab|cd) D_cd
+        const int ia = t / NB, ib = t - ia * NB;
+        R sum = R(0);
+        for (int ic = 0; ic < NC; ++ic)
+            for (int id = 0; id < ND; ++id)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id), sum);
+        atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, widen(sum * deg2));
+    }
+    for (int t = lane; t < NC * ND; t += 32) {  // J-hat ket: 2 (ab|cd) D_ab
+        const int ic = t / ND, id = t - ic * ND;
+        R sum = R(0);
+        for (int ia = 0; ia < NA; ++ia)
+            for (int ib = 0; ib < NB; ++ib)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib), sum);
+        atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, widen(sum * deg2));
+    }
+    for (int t = lane; t < NA * NC; t += 32) {  // K-hat[a][c] += (ab|cd) D_bd
+        const int ia = t / NC, ic = t - ia * NC;
+        R sum = R(0);
+        for (int ib = 0; ib < NB; ++ib)
+            for (int id = 0; id < ND; ++id)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id), sum);
+        atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, widen(sum * deg));
+    }
+    for (int t = lane; t < NB * NC; t += 32) {  // K-hat[b][c] += (ab|cd) D_ad
+        const int ib = t / NC, ic = t - ib * NC;
+        R sum = R(0);
+        for (int ia = 0; ia < NA; ++ia)
+            for (int id = 0; id < ND; ++id)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id), sum);
+        atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, widen(sum * deg));
+    }
+    for (int t = lane; t < NA * ND; t += 32) {  // K-hat[a][d] += (ab|cd) D_bc
+        const int ia = t / ND, id = t - ia * ND;
+        R sum = R(0);
+        for (int ib = 0; ib < NB; ++ib)
+            for (int ic = 0; ic < NC; ++ic)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic), sum);
+        atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, widen(sum * deg));
+    }
+    for (int t = lane; t < NB * ND; t += 32) {  // K-hat[b][d] += (ab|cd) D_ac
+        const int ib = t / ND, id = t - ib * ND;
+        R sum = R(0);
+        for (int ia = 0; ia < NA; ++ia)
+            for (int ic = 0; ic < NC; ++ic)
+                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic), sum);
+        atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, widen(sum * deg));
+    }
+#undef WIDX
+}
+
+// Raise the shared-memory limit of the warp-cooperative kernels (once per
+// device, outside any stream capture).
+template <int LA, int LB, int LC, int LD>
+cudaError_t prepare_eri_class() {
+    if constexpr (EriClass<LA, LB, LC, LD>::WC) {
+        cudaError_t e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)WcShape<LA, LB, LC, LD, double>::SMEM);
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)WcShape<LA, LB, LC, LD, float>::SMEM);
+    }
+    return cudaSuccess;
+}
+
 template <int LA, int LB, int LC, int LD>
 void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
     if (a.ntasks <= 0) return;
     const int threads = 128;
     const long long nthreads = (long long)a.ntasks * 32;
     const int blocks = (int)((nthreads + threads - 1) / threads);
+    if constexpr (EriClass<LA, LB, LC, LD>::WC) {
+        if (epi == EPI_JK && a.wc) {  // one warp per task, the plan gives one quartet per task
+            if (prec == 1) {
+                using W = WcShape<LA, LB, LC, LD, float>;
+                eri_wc_kernel<LA, LB, LC, LD, float>
+                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
+            } else {
+                using W = WcShape<LA, LB, LC, LD, double>;
+                eri_wc_kernel<LA, LB, LC, LD, double>
+                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
+            }
+            return;
+        }
+    }
     if (epi == EPI_JK) {
         if (prec == 1) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
         else if constexpr (LA + LB + LC + LD <= 4) {

@@ -328,6 +328,144 @@ def boys_ops(L, ntay=NTAY64):
     return 2 * (ntay - 1) + L + 2, L + 2 + 1
 
 
+# ---------------------------------------------------------------------------
+# Warp-cooperative programs for the large classes.  Their straight-line VRR/HRR
+# working sets (hundreds to thousands of intermediates) do not fit in one
+# thread's registers; instead one warp evaluates one contracted quartet with
+# the intermediates in shared memory, level by level of the recurrence DAG, the
+# 32 lanes taking the independent terms of a level.  The DAG is the same one
+# the straight-line code follows (same direction choices, same terms).
+WC_MINL = 5  # classes with l_a+l_b+l_c+l_d >= WC_MINL get a program
+
+
+def _levels(depth, order, key):
+    """Group node indices by depth; within a level sort by key (branch shape)."""
+    by = {}
+    for n in order:
+        by.setdefault(depth[n], []).append(n)
+    out, bounds = [], [0]
+    for dlev in sorted(by):
+        out.extend(sorted(by[dlev], key=key))
+        bounds.append(len(out))
+    return out, bounds
+
+
+def gen_prog(la, lb, lc, ld, choose_v, choose_h):
+    E, F = la + lb, lc + ld
+    L = E + F
+    idx, depth, recs, order = {}, {}, {}, []
+    for m in range(L + 1):
+        idx[((0, 0, 0), (0, 0, 0), m)] = m
+        depth[m] = 0
+
+    def node(e, f, m):
+        key = (e, f, m)
+        if key in idx:
+            return idx[key]
+        if sum(f) == 0:
+            i = choose_v(e)
+            e1 = sub(e, i)
+            r = {"kind": 0, "dir": i, "a": node(e1, f, m), "b": node(e1, f, m + 1), "c": 0, "d": 0, "g": 0, "n1": 0, "n2": 0}
+            if e1[i] > 0:
+                e2 = sub(e1, i)
+                r.update(c=node(e2, f, m), d=node(e2, f, m + 1), n1=e1[i])
+        else:
+            i = choose_v(f)
+            f1 = sub(f, i)
+            r = {"kind": 1, "dir": i, "a": node(e, f1, m), "b": node(e, f1, m + 1), "c": 0, "d": 0, "g": 0, "n1": 0, "n2": 0}
+            if f1[i] > 0:
+                f2 = sub(f1, i)
+                r.update(c=node(e, f2, m), d=node(e, f2, m + 1), n1=f1[i])
+            if e[i] > 0:
+                r.update(g=node(sub(e, i), f1, m + 1), n2=e[i])
+        k = L + 1 + len(order)
+        kids = [r["a"], r["b"]] + ([r["c"], r["d"]] if r["n1"] else []) + ([r["g"]] if r["n2"] else [])
+        depth[k] = 1 + max(depth[c] for c in kids)
+        recs[k] = r
+        order.append(k)
+        idx[key] = k
+        return k
+
+    targets = [(e, f) for e in comps_range(la, E) for f in comps_range(lc, F)]
+    tgt = [node(e, f, 0) for (e, f) in targets]
+    vorder, vbounds = _levels(depth, order, lambda n: (recs[n]["kind"], recs[n]["n1"] > 0, recs[n]["n2"] > 0))
+    NT = len(targets)
+    eidx = {e: k for k, e in enumerate(comps_range(la, E))}
+    fidx = {f: k for k, f in enumerate(comps_range(lc, F))}
+    nf = len(fidx)
+    hidx, hdepth, hrec, horder = {}, {}, {}, []
+    for k in range(NT):
+        hdepth[k] = 0
+
+    def hnode(key, side, i, x, y):
+        if key in hidx:
+            return hidx[key]
+        k = NT + len(horder)
+        hdepth[k] = 1 + max(hdepth[x], hdepth[y])
+        hrec[k] = {"side": side, "dir": i, "x": x, "y": y}
+        horder.append(k)
+        hidx[key] = k
+        return k
+
+    def bra(a, b, f):
+        if sum(b) == 0:
+            return eidx[a] * nf + fidx[f]
+        key = ("b", a, b, f)
+        if key in hidx:
+            return hidx[key]
+        i = choose_h(b)
+        b1 = sub(b, i)
+        return hnode(key, 0, i, bra(add(a, i), b1, f), bra(a, b1, f))
+
+    def ket(a, b, c, d):
+        if sum(d) == 0:
+            return bra(a, b, c)
+        key = ("k", a, b, c, d)
+        if key in hidx:
+            return hidx[key]
+        i = choose_h(d)
+        d1 = sub(d, i)
+        return hnode(key, 1, i, ket(a, b, add(c, i), d1), ket(a, b, c, d1))
+
+    outs = []
+    for a in ijk_list(la):
+        for b in ijk_list(lb):
+            for c in ijk_list(lc):
+                for d in ijk_list(ld):
+                    outs.append((ket(a, b, c, d), comp_norm(a) * comp_norm(b) * comp_norm(c) * comp_norm(d)))
+    horder2, hbounds = _levels(hdepth, horder, lambda n: hrec[n]["side"])
+    scr = max(L + 1 + len(order), NT + len(horder))
+    assert scr < 65536
+    tag = "%d%d%d%d" % (la, lb, lc, ld)
+    lines = ["// warp-cooperative program of class (%d%d|%d%d): %d VRR terms in %d levels, %d HRR terms in %d levels"
+             % (la, lb, lc, ld, len(order), len(vbounds) - 1, len(horder), len(hbounds) - 1)]
+    lines.append("static __device__ const uint4 rchem_vrr_%s[%d] = {" % (tag, len(vorder)))
+    for n in vorder:
+        r = recs[n]
+        lines.append("  {%du, %du, %du, %du}," % (n | (r["a"] << 16), r["b"] | (r["c"] << 16), r["d"] | (r["g"] << 16),
+                                                  r["dir"] | (r["kind"] << 8) | (r["n1"] << 16) | (r["n2"] << 24)))
+    lines.append("};")
+    lines.append("static __device__ const int rchem_vrrlv_%s[%d] = {%s};" % (tag, len(vbounds), ", ".join(map(str, vbounds))))
+    lines.append("static __device__ const unsigned short rchem_tgt_%s[%d] = {%s};" % (tag, NT, ", ".join(map(str, tgt))))
+    lines.append("static __device__ const uint2 rchem_hrr_%s[%d] = {" % (tag, max(1, len(horder2))))
+    for n in horder2:
+        r = hrec[n]
+        lines.append("  {%du, %du}," % (n | (r["x"] << 16), r["y"] | (r["dir"] << 16) | (r["side"] << 24)))
+    if not horder2:
+        lines.append("  {0u, 0u},")
+    lines.append("};")
+    lines.append("static __device__ const int rchem_hrrlv_%s[%d] = {%s};" % (tag, len(hbounds), ", ".join(map(str, hbounds))))
+    lines.append("static __device__ const unsigned short rchem_out_%s[%d] = {%s};" % (tag, len(outs), ", ".join(str(o[0]) for o in outs)))
+    lines.append("static __device__ const double rchem_onorm_%s[%d] = {%s};" % (tag, len(outs), ", ".join("%.17g" % o[1] for o in outs)))
+    lines.append("template <> struct EriProg<%d,%d,%d,%d> {" % (la, lb, lc, ld))
+    lines.append("  static constexpr int NVL = %d, NHL = %d, NT = %d, NOUT = %d, SCR = %d;" % (len(vbounds) - 1, len(hbounds) - 1, NT, len(outs), scr))
+    for nm in ("vrr", "vrrlv", "tgt", "hrr", "hrrlv", "out", "onorm"):
+        ty = {"vrr": "uint4", "vrrlv": "int", "tgt": "unsigned short", "hrr": "uint2", "hrrlv": "int", "out": "unsigned short", "onorm": "double"}[nm]
+        lines.append("  __device__ static __forceinline__ const %s *%s() { return rchem_%s_%s; }" % (ty, nm, nm, tag))
+    lines.append("};")
+    return lines
+
+
 def main(outdir):
     os.makedirs(outdir, exist_ok=True)
     pairs, cls = classes()
@@ -352,6 +490,8 @@ def main(outdir):
         lines.append("template <> struct EriClass<%d,%d,%d,%d> {" % (la, lb, lc, ld))
         lines.append("  static constexpr int L = %d, NE = %d, NF = %d, NA = %d, NB = %d, NC = %d, ND = %d;" % (L, NE, NF, NA, NB, NC, ND))
         lines.append("  static constexpr double PRIM_FLOPS = %d.0, CONTR_FLOPS = %d.0;" % (prim_flops, contr_flops))
+        lines.append("  static constexpr bool WC = %s;  // a warp-cooperative program evaluates the J/K epilogue class"
+                     % ("true" if L >= WC_MINL else "false"))
         lines.append("  template <typename R> __host__ __device__ static __forceinline__ void vrr(R* __restrict__ acc, const R* __restrict__ F,")
         lines.append("      R PAx, R PAy, R PAz, R WPx, R WPy, R WPz, R QCx, R QCy, R QCz, R WQx, R WQy, R WQz,")
         lines.append("      R ohp, R ohq, R ohpq, R rho_p, R rho_q) {")
@@ -365,6 +505,9 @@ def main(outdir):
         lines.extend(hem.lines)
         lines.append("  }")
         lines.append("};")
+        if L >= WC_MINL:
+            with open(os.path.join(outdir, "eri_prog_%s.inc" % tag), "w") as f:
+                f.write("\n".join(gen_prog(la, lb, lc, ld, CHOICES[chv], CHOICES[chh])) + "\n")
         with open(os.path.join(outdir, "eri_class_%s.inc" % tag), "w") as f:
             f.write("\n".join(lines) + "\n")
         table.append((la, lb, lc, ld, prim_flops, contr_flops, NA * NB * NC * ND))
@@ -374,13 +517,23 @@ def main(outdir):
         with open(os.path.join(outdir, "eri_%s.cu" % tag), "w") as f:
             f.write("// generated by gen_eri.py -- do not edit\n")
             f.write('#include "../eri_kernel.cuh"\n#include "eri_class_%s.inc"\n' % tag)
+            if la + lb + lc + ld >= WC_MINL:
+                f.write('#include "eri_prog_%s.inc"\n' % tag)
             f.write("void rchem_launch_eri_%s(const EriArgs &a, int fp32, int epi, cudaStream_t s) {\n" % tag)
             f.write("    launch_eri_class<%d, %d, %d, %d>(a, fp32, epi, s);\n}\n" % (la, lb, lc, ld))
+            f.write("cudaError_t rchem_prepare_eri_%s() { return prepare_eri_class<%d, %d, %d, %d>(); }\n" % (tag, la, lb, lc, ld))
     with open(os.path.join(outdir, "eri_dispatch.h"), "w") as f:
         f.write("// generated by gen_eri.py -- do not edit\n#pragma once\n#include <cuda_runtime.h>\n")
         f.write('#include "../rchem_types.h"\n')
         for (la, lb, lc, ld) in cls:
             f.write("void rchem_launch_eri_%d%d%d%d(const EriArgs &a, int fp32, int epi, cudaStream_t s);\n" % (la, lb, lc, ld))
+        for (la, lb, lc, ld) in cls:
+            f.write("cudaError_t rchem_prepare_eri_%d%d%d%d();\n" % (la, lb, lc, ld))
+        f.write("typedef cudaError_t (*rchem_eri_preparer)();\n")
+        f.write("static const rchem_eri_preparer rchem_eri_prepare[%d] = {\n" % len(cls))
+        for (la, lb, lc, ld) in cls:
+            f.write("  rchem_prepare_eri_%d%d%d%d,\n" % (la, lb, lc, ld))
+        f.write("};\n")
         f.write("typedef void (*rchem_eri_launcher)(const EriArgs &, int, int, cudaStream_t);\n")
         f.write("static const rchem_eri_launcher rchem_eri_launchers[%d] = {\n" % len(cls))
         for (la, lb, lc, ld) in cls:
@@ -394,6 +547,9 @@ def main(outdir):
         for t in table:
             f.write("  {%d,%d,%d,%d},\n" % t[:4])
         f.write("};\n")
+        f.write("// 1: the J/K epilogue class runs the warp-cooperative program (one quartet per warp)\n")
+        f.write("static const int rchem_class_wc[%d] = {%s};\n" % (
+            len(cls), ", ".join("1" if sum(t[:4]) >= WC_MINL else "0" for t in table)))
         f.write("static const double rchem_class_flops[%d][2] = {\n" % len(cls))
         for t in table:
             f.write("  {%d.0, %d.0},\n" % t[4:6])

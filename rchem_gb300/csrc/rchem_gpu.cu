@@ -88,6 +88,7 @@ static int get_tables(const DevTables **out) {
             const float hi = (float)b64[i];
             bdf[i] = make_float2(hi, (float)(b64[i] - (double)hi));
         }
+        for (int k = 0; k < RCHEM_NCLASS; ++k) CK(rchem_eri_prepare[k]());  // before any stream capture
         DevTables n;
         CK(cudaMalloc(&n.boys64, b64.size() * sizeof(double)));
         CK(cudaMalloc(&n.boys32, b32.size() * sizeof(float)));
@@ -328,6 +329,7 @@ struct rchem_basis_s {
     // tile shape per class list: lanes share a quartet while each keeps at
     // least this many primitive quartets (rchem_autotune chooses them)
     int ppl[RCHEM_NCLASS][2];
+    int wc[RCHEM_NCLASS][2];  // large classes: warp-cooperative J/K kernel (chosen by the autotuner)
     // concurrent class kernels: fork/join over auxiliary streams
     static const int NAUX = 16;
     cudaStream_t aux[NAUX] = {};
@@ -656,6 +658,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 int lg = 0;
                 const long long ppl = b->ppl[k][prec];
                 while (lg < 5 && nprimq >= ppl << (lg + 1)) ++lg;
+                if (b->wc[k][prec]) lg = 5;  // warp-cooperative kernel: one quartet per warp
                 pack_tasks(sv, s0, total, lg, (nprimq + (1 << lg) - 1) >> lg, lists[k][prec]);
                 const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
                 b->list_flops[k][prec] += fl;
@@ -754,6 +757,7 @@ static int launch_lists(rchem_basis b, EriArgs a, int epi, bool with32, bool emu
         load[best] += ls[i].cost;
         a.tasks = b->d_tasks + b->task_off[ls[i].k][ls[i].p];
         a.ntasks = (int)b->task_cnt[ls[i].k][ls[i].p];
+        a.wc = b->wc[ls[i].k][ls[i].p];
         rchem_eri_launchers[ls[i].k](a, ls[i].p == 1 ? 1 : (emul ? 2 : 0), epi, b->aux[best]);
     }
     CK(cudaGetLastError());
@@ -788,7 +792,10 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
     }
     rchem_basis b = new rchem_basis_s();
     CK(cudaGetDevice(&b->dev));
-    for (int k = 0; k < RCHEM_NCLASS; ++k) b->ppl[k][0] = b->ppl[k][1] = kMinPrimPerLane;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) {
+        b->ppl[k][0] = b->ppl[k][1] = kMinPrimPerLane;
+        b->wc[k][0] = b->wc[k][1] = 0;
+    }
     b->natoms = natoms;
     b->Z.assign(atomnos, atomnos + natoms);
     b->R.assign(coords, coords + 3 * natoms);
@@ -1275,6 +1282,19 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
 
 // Autotuner: for every class list of the Fock build, time the list alone under
 // each candidate tile shape and keep the fastest.
+extern "C" int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    if (cls < 0 || cls >= RCHEM_NCLASS || prec < 0 || prec > 1)
+        return set_err(RCHEM_ERR_INVALID, "class %d / precision %d out of range", cls, prec);
+    if (ppl < 0) return set_err(RCHEM_ERR_INVALID, "primitive quartets per lane %d", ppl);
+    if (ppl == 0 && !rchem_class_wc[cls])
+        return set_err(RCHEM_ERR_UNSUPPORTED, "class %d has no warp-cooperative kernel", cls);
+    b->wc[cls][prec] = ppl == 0;
+    b->ppl[cls][prec] = ppl == 0 ? kMinPrimPerLane : ppl;
+    b->planned = false;  // the next build replans with this shape
+    return RCHEM_OK;
+}
+
 extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen) {
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
     rchem_jk_opts o;
@@ -1285,18 +1305,25 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
     static const int cand[] = {4, 8, 16, 32, 64, 1 << 30};
     const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
     float best_ms[RCHEM_NCLASS][2];
-    int best[RCHEM_NCLASS][2];
+    int best[RCHEM_NCLASS][2], best_wc[RCHEM_NCLASS][2];
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
             best_ms[k][p] = 1e30f;
             best[k][p] = kMinPrimPerLane;
+            best_wc[k][p] = 0;
         }
     const size_t nn = (size_t)b->packed;
     CK(cudaMemsetAsync(b->d_D, 0, nn * sizeof(double), b->stream));
     CK(cudaMemsetAsync(b->d_D32, 0, nn * sizeof(float), b->stream));
     CK(cudaMemsetAsync(b->d_Ddf, 0, nn * sizeof(float2), b->stream));
-    for (int c = 0; c < ncand; ++c) {
-        for (int k = 0; k < RCHEM_NCLASS; ++k) b->ppl[k][0] = b->ppl[k][1] = cand[c];
+    // candidates: every lanes-per-quartet shape, then (c == ncand) the
+    // warp-cooperative kernel of the large classes
+    for (int c = 0; c <= ncand; ++c) {
+        const bool wc = c == ncand;
+        for (int k = 0; k < RCHEM_NCLASS; ++k) {
+            b->ppl[k][0] = b->ppl[k][1] = wc ? kMinPrimPerLane : cand[c];
+            b->wc[k][0] = b->wc[k][1] = wc ? rchem_class_wc[k] : 0;
+        }
         b->planned = false;
         CKR(plan_tasks(b, tau, tau32));
         EriArgs a = base_args(b);
@@ -1308,9 +1335,10 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         a.K = b->d_Kh;
         for (int k = 0; k < RCHEM_NCLASS; ++k)
             for (int p = 0; p < 2; ++p) {
-                if (b->task_cnt[k][p] == 0) continue;
+                if (b->task_cnt[k][p] == 0 || (wc && !rchem_class_wc[k])) continue;
                 a.tasks = b->d_tasks + b->task_off[k][p];
                 a.ntasks = (int)b->task_cnt[k][p];
+                a.wc = b->wc[k][p];
                 float ms = 0.f;
                 for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
                     CK(cudaEventRecord(b->ev_t0, b->stream));
@@ -1322,14 +1350,16 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
                 CK(cudaGetLastError());
                 if (ms < best_ms[k][p]) {
                     best_ms[k][p] = ms;
-                    best[k][p] = cand[c];
+                    best[k][p] = wc ? kMinPrimPerLane : cand[c];
+                    best_wc[k][p] = wc ? 1 : 0;
                 }
             }
     }
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
             b->ppl[k][p] = best[k][p];
-            if (chosen) chosen[2 * k + p] = best[k][p];
+            b->wc[k][p] = best_wc[k][p];
+            if (chosen) chosen[2 * k + p] = best_wc[k][p] ? 0 : best[k][p];
         }
     b->planned = false;
     CKR(plan_tasks(b, tau, tau32));

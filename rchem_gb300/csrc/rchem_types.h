@@ -97,6 +97,7 @@ struct EriArgs {
     double *J;             // unsymmetrised accumulators (J-hat, K-hat)
     double *K;
     double *eri;           // dense nbf^4 output (ERI-tensor epilogue)
+    int wc;                // J/K epilogue of a large class: 1 = warp-cooperative kernel, 0 = one lane group per quartet
 };
 
 // Shell as the planner sees it.

@@ -306,7 +306,7 @@ def test_autotune_keeps_results(gpu):
         J0, K0 = np.zeros((104, 104)), np.zeros((104, 104))
         rc.JK_direct(J0, K0, b, D)
         chosen = b.autotune()
-        assert len(chosen) == 42 and all(v >= 4 for v in chosen.values())
+        assert len(chosen) == 42 and all(v == 0 or v >= 4 for v in chosen.values())
         J1, K1 = np.zeros((104, 104)), np.zeros((104, 104))
         rc.JK_direct(J1, K1, b, D)
         np.testing.assert_allclose(J1, J0, atol=1e-12, rtol=0)
@@ -384,3 +384,33 @@ def test_emulated_fp64_device_and_batch(gpu):
     assert float((Je - J).abs().max()) < 1e-12
     assert float((Ke - K).abs().max()) < 1e-12
     bb.close()
+
+
+@pytest.mark.parametrize("name", ["6-31gss-fit", "6-31gs-fit"])
+def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
+    """The warp-cooperative J/K kernel of the large classes (total L >= 5), forced
+    on every such list, FP64 and FP32, against the 8-fold oracle."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    Z, R = rc.geometry.water_cluster(2, 4.5, seed=11)
+    ob = O.expand_basis(Z, R, rc.load_bse(name))
+    D = _sym_density(np.random.default_rng(1), ob.n)
+    Jr, Kr = O.JK_sym(ob, D)
+    with rc.Basis(Z, R, name) as b:
+        n = b.nbf
+        J, K = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(J, K, b, D, schwarz_tau=0.0)  # plans the work: the class table is known from here
+        wc = [k for k, c in enumerate(b.class_stats()) if sum(c["class"]) >= 5]
+        assert len(wc) == 8
+        for k in wc:
+            b.set_tile_shape(k, 0, 0)
+            b.set_tile_shape(k, 1, 0)
+        rc.JK_direct(J, K, b, D, schwarz_tau=0.0)
+        assert np.abs(J - Jr).max() < 1e-12
+        assert np.abs(K - Kr).max() < 1e-12
+        Jm, Km = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(Jm, Km, b, D, schwarz_tau=0.0, fp32_tau=1e30)  # every quartet in FP32
+        assert np.abs(Jm - Jr).max() < 1e-5 and np.abs(Km - Kr).max() < 1e-5
+        with pytest.raises(rc.RchemError):
+            b.set_tile_shape(0, 0, 0)  # (ss|ss) has no warp-cooperative kernel
