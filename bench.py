@@ -185,7 +185,7 @@ def north_star(rc, torch):
     bname, Z, R = rc.geometry.config("h2o32_631gs")
     with rc.Basis(Z, R, bname) as b:
         rc.scf.rhf(b, max_iter=2)  # warm-up: work plan, graph, cuSOLVER initialisation
-        b.autotune(1e-12, 0.0)  # tile shapes per class list (and the large classes' kernel) for this form
+        tuned = b.autotune(1e-12, 0.0)  # tile shapes per class list (and the large classes' kernel) for this form
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r64 = rc.scf.rhf(b, thresh_e=1e-10)
@@ -194,7 +194,8 @@ def north_star(rc, torch):
         ms64, st64 = _timed_builds(rc, torch, b, D, 0.0)
         rec = {"nbf": b.nbf, "fp64_ms": ms64, "fp64_builds_per_s": 1000.0 / ms64, "eris_fp64": st64["eris_fp64"],
                "fp64_flops": st64["flops_fp64"], "scf_fp64_s": t_scf64, "scf_iterations": r64["iterations"],
-               "e_total_fp64": r64["e_total"], "mixed": {}}
+               "e_total_fp64": r64["e_total"], "mixed": {},
+               "warp_cooperative_lists_fp64": sorted(k for (k, p), v in tuned.items() if p == 0 and v == 0)}
         for tau32 in (1e-6, 1e-4):
             b.autotune(1e-12, tau32)
             ms, st = _timed_builds(rc, torch, b, D, tau32)

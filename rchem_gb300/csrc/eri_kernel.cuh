@@ -407,20 +407,29 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         for (int m = 0; m <= L; ++m)
             if (lane == m) S[m] = F[m];
         __syncwarp();
+        // one term: X a + Y b [+ n1 c (c_ - rho d)] [+ n2 ohpq g]
+        auto term = [&](const uint4 op, R ta, R tb, R tc, R td, R tg) {
+            const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
+            const R X = ket ? wc_sel3(dir, QC[0], QC[1], QC[2]) : wc_sel3(dir, PA[0], PA[1], PA[2]);
+            const R Y = ket ? wc_sel3(dir, WQ[0], WQ[1], WQ[2]) : wc_sel3(dir, WP[0], WP[1], WP[2]);
+            R v = rchem_fma(Y, tb, X * ta);
+            if (n1) v = rchem_fma(ket ? wc_sel4(n1, cq) : wc_sel4(n1, cp), rchem_fma(-(ket ? pi_ : qi_), td, tc), v);
+            if (n2) v = rchem_fma(wc_sel4(n2, cpq), tg, v);
+            return v;
+        };
         for (int lv = 0; lv < P::NVL; ++lv) {
             const int e = __ldg(vlev + lv + 1);
-            for (int t = __ldg(vlev + lv) + lane; t < e; t += 32) {
-                const uint4 op = __ldg(vprog + t);
-                const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
-                const R X = ket ? wc_sel3(dir, QC[0], QC[1], QC[2]) : wc_sel3(dir, PA[0], PA[1], PA[2]);
-                const R Y = ket ? wc_sel3(dir, WQ[0], WQ[1], WQ[2]) : wc_sel3(dir, WP[0], WP[1], WP[2]);
-                R v = rchem_fma(Y, S[op.y & 0xffff], X * S[op.x >> 16]);
-                if (n1) {
-                    const R c1 = ket ? wc_sel4(n1, cq) : wc_sel4(n1, cp);
-                    v = rchem_fma(c1, rchem_fma(-(ket ? pi_ : qi_), S[op.z & 0xffff], S[op.y >> 16]), v);
-                }
-                if (n2) v = rchem_fma(wc_sel4(n2, cpq), S[op.z >> 16], v);
-                S[op.x & 0xffff] = v;
+            // two independent terms per lane and pass: all operand loads before either store
+            for (int t = __ldg(vlev + lv) + lane; t < e; t += 64) {
+                const bool two = t + 32 < e;
+                const uint4 o0 = __ldg(vprog + t), o1 = two ? __ldg(vprog + t + 32) : o0;
+                const R a0 = S[o0.x >> 16], b0 = S[o0.y & 0xffff], c0 = S[o0.y >> 16], d0 = S[o0.z & 0xffff],
+                        g0 = S[o0.z >> 16];
+                const R a1 = S[o1.x >> 16], b1 = S[o1.y & 0xffff], c1 = S[o1.y >> 16], d1 = S[o1.z & 0xffff],
+                        g1 = S[o1.z >> 16];
+                const R v0 = term(o0, a0, b0, c0, d0, g0), v1 = term(o1, a1, b1, c1, d1, g1);
+                S[o0.x & 0xffff] = v0;
+                if (two) S[o1.x & 0xffff] = v1;
             }
             __syncwarp();
         }
@@ -435,13 +444,19 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
     __syncwarp();
     const uint2 *hprog = P::hrr();
     const int *hlev = P::hrrlv();
+    auto hcoef = [&](const uint2 op) {
+        const int dir = (op.y >> 16) & 255, side = op.y >> 24;
+        return side ? wc_sel3(dir, CD[0], CD[1], CD[2]) : wc_sel3(dir, AB[0], AB[1], AB[2]);
+    };
     for (int lv = 0; lv < P::NHL; ++lv) {
         const int e = __ldg(hlev + lv + 1);
-        for (int t = __ldg(hlev + lv) + lane; t < e; t += 32) {
-            const uint2 op = __ldg(hprog + t);
-            const int dir = (op.y >> 16) & 255, side = op.y >> 24;
-            const R X = side ? wc_sel3(dir, CD[0], CD[1], CD[2]) : wc_sel3(dir, AB[0], AB[1], AB[2]);
-            S[op.x & 0xffff] = rchem_fma(X, S[op.y & 0xffff], S[op.x >> 16]);
+        for (int t = __ldg(hlev + lv) + lane; t < e; t += 64) {
+            const bool two = t + 32 < e;
+            const uint2 o0 = __ldg(hprog + t), o1 = two ? __ldg(hprog + t + 32) : o0;
+            const R x0 = S[o0.x >> 16], y0 = S[o0.y & 0xffff], x1 = S[o1.x >> 16], y1 = S[o1.y & 0xffff];
+            const R v0 = rchem_fma(hcoef(o0), y0, x0), v1 = rchem_fma(hcoef(o1), y1, x1);
+            S[o0.x & 0xffff] = v0;
+            if (two) S[o1.x & 0xffff] = v1;
         }
         __syncwarp();
     }
