@@ -375,6 +375,11 @@ def main():
     stem = b.stats()
     Je, Ke = J.cpu().numpy(), K.cpu().numpy()
     ms_emul = float(np.mean(msem))
+    # ---- emulated FP64 above fp32_tau = 1e-6, FP32 below ------------------
+    tuned["emulated_mixed"] = b.autotune(1e-12, 1e-6, emulated=True)
+    msem32 = run(1e-6, a.steps, a.warmup, emulated=True)
+    Jem, Kem = J.cpu().numpy(), K.cpu().numpy()
+    ms_emul32 = float(np.mean(msem32))
 
     # ---- end to end through the C ABI with host arrays ---------------------
     b.autotune(1e-12, 0.0)
@@ -445,6 +450,11 @@ def main():
                          "quartets": stem["quartets_fp64"],
                          "dE_fixed_density_Eh": float(np.sum(Dh * (2 * (Je - J64) - (Ke - K64)))),
                          "max_abs_dJ": float(np.abs(Je - J64).max()), "max_abs_dK": float(np.abs(Ke - K64).max())},
+            "emulated_mixed": {"builds_per_s": 1000.0 / ms_emul32, "ms": ms_emul32, "fp32_tau": 1e-6,
+                               "speedup_vs_fp64": ms / ms_emul32,
+                               "dE_fixed_density_Eh": float(np.sum(Dh * (2 * (Jem - J64) - (Kem - K64)))),
+                               "max_abs_dJ": float(np.abs(Jem - J64).max()),
+                               "max_abs_dK": float(np.abs(Kem - K64).max())},
         },
         "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": 2 * n * n * 8},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",

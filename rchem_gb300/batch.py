@@ -119,7 +119,26 @@ def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False)
 def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=8, fp32_tau=0.0,
               schwarz_tau=1e-12, emulated=False):
     """RHF for every geometry of ``bb`` at once; returns per-geometry energies,
-    the packed D and W, iteration count and convergence flags."""
+    the packed D and W, iteration count and convergence flags.
+
+    The iterations run on one side stream shared by torch and the library
+    (the handle is moved to it), so no host synchronisation orders them; the
+    caller's stream waits for the results."""
+    import torch
+
+    caller = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    side.wait_stream(caller)
+    bb.set_stream(side.cuda_stream)
+    with torch.cuda.stream(side):
+        res = _rhf_batch(bb, thresh_e, thresh_d, max_iter, diis, fp32_tau, schwarz_tau, emulated)
+    caller.wait_stream(side)
+    for key in ("D", "W"):  # allocated on the side stream, used on the caller's
+        res[key].record_stream(caller)
+    return res
+
+
+def _rhf_batch(bb, thresh_e, thresh_d, max_iter, diis, fp32_tau, schwarz_tau, emulated):
     import torch
 
     dev = torch.device("cuda")
@@ -173,11 +192,11 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
     for it in range(1, max_iter + 1):
         jk(bb, D, J, K, schwarz_tau, fp32_tau, emulated)
         F = H + 2.0 * J - K
-        Fx = []
+        Fx, egs = [], []
         for grp, s_ in zip(groups, st):
             n, gs, idx, no = grp
             Fg, Dg = gather(F, grp), gather(D, grp)
-            e_g[gs] = ((s_["H"] + Fg) * Dg).sum(dim=(-1, -2)).cpu().numpy()
+            egs.append(((s_["H"] + Fg) * Dg).sum(dim=(-1, -2)))
             X = s_["X"]
             err = X.transpose(-1, -2) @ (Fg @ Dg @ s_["S"] - s_["S"] @ Dg @ Fg) @ X
             s_["focks"].append(Fg)
@@ -194,24 +213,27 @@ def rhf_batch(bb: BatchBasis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=
                 Bm[:, :m, m] = -1.0
                 rhs = torch.zeros((len(gs), m + 1), dtype=torch.float64, device=dev)
                 rhs[:, m] = -1.0
-                c = torch.linalg.solve(Bm, rhs)[:, :m]
-                Fx.append(torch.einsum("gk,gkij->gij", c, torch.stack(s_["focks"], dim=1)))
+                # solve_ex: no host synchronisation; a singular system keeps that geometry's F
+                c, info = torch.linalg.solve_ex(Bm, rhs)
+                ext = torch.einsum("gk,gkij->gij", c[:, :m], torch.stack(s_["focks"], dim=1))
+                Fx.append(torch.where((info != 0)[:, None, None], Fg, ext))
             else:
                 Fx.append(Fg)
         D_old = D
         D, _ = densities(Fx)
-        dD = (D - D_old).abs()
-        ddg = np.array([float(dD[int(bb.offsets[g]):int(bb.offsets[g]) + int(bb.geom_nbf[g]) ** 2].max())
-                        for g in range(bb.ngeom)]) if bb.ngeom <= 64 else None
+        # one device-to-host transfer per iteration: every energy and max |dD|
+        host = torch.cat(egs + [(D - D_old).abs().max().reshape(1)]).cpu().numpy()
+        pos = 0
+        for grp in groups:
+            e_g[grp[1]] = host[pos:pos + len(grp[1])]
+            pos += len(grp[1])
+        dmax = float(host[-1])
         if e_old is not None:
-            de = np.abs(e_g - e_old)
-            dmax = float(dD.max())
-            conv = de < thresh_e
+            conv = np.abs(e_g - e_old) < thresh_e
             if conv.all() and dmax < thresh_d:
                 e_old = e_g.copy()
                 break
         e_old = e_g.copy()
-        del ddg
     # final energies and W at the converged densities
     jk(bb, D, J, K, schwarz_tau, fp32_tau, emulated)
     F = H + 2.0 * J - K
