@@ -180,7 +180,7 @@ int rchem_eigh_batched(int n, int batch, const double *A, double *w, double *V, 
  * Autotune the Fock build's tile shapes for this basis and these thresholds
  * (no counterpart in the reference): for every integral class list (21
  * classes x {FP64, FP32}) time the list alone under each candidate number of
- * lanes per shell quartet, and for the classes with l_a+l_b+l_c+l_d >= 5 also
+ * lanes per shell quartet, and for the classes with l_a+l_b+l_c+l_d >= 4 also
  * the warp-cooperative kernel (one quartet per warp, intermediates in shared
  * memory), and keep the fastest.  chosen (may be NULL) receives 2*21 ints: the
  * minimum primitive quartets per lane picked for each list (2^30 = never split,
@@ -193,7 +193,7 @@ int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen);
  * overrides rchem_autotune for that list): class index cls 0..20 in the order
  * of the generated class table (s,p,d pairs with l_a >= l_b), prec 0 = FP64 /
  * emulated list, 1 = FP32 list; ppl = minimum primitive quartets per lane, or
- * 0 for the warp-cooperative kernel (classes with l_a+l_b+l_c+l_d >= 5 only,
+ * 0 for the warp-cooperative kernel (classes with l_a+l_b+l_c+l_d >= 4 only,
  * else RCHEM_ERR_UNSUPPORTED).  The next Fock build replans.
  */
 int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl);

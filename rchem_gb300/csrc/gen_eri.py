@@ -335,7 +335,7 @@ def boys_ops(L, ntay=NTAY64):
 # the intermediates in shared memory, level by level of the recurrence DAG, the
 # 32 lanes taking the independent terms of a level.  The DAG is the same one
 # the straight-line code follows (same direction choices, same terms).
-WC_MINL = 5  # classes with l_a+l_b+l_c+l_d >= WC_MINL get a program
+WC_MINL = 4  # classes with l_a+l_b+l_c+l_d >= WC_MINL get a program
 
 
 def _levels(depth, order, key):

@@ -388,8 +388,8 @@ def test_emulated_fp64_device_and_batch(gpu):
 
 @pytest.mark.parametrize("name", ["6-31gss-fit", "6-31gs-fit"])
 def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
-    """The warp-cooperative J/K kernel of the large classes (total L >= 5), forced
-    on every such list, FP64 and FP32, against the 8-fold oracle."""
+    """The warp-cooperative J/K kernel of the large classes (total L >= 4), forced
+    on every such list, FP64, emulated FP64 and FP32, against the 8-fold oracle."""
     import rchem_gb300 as rc
 
     O = oracle_mod
@@ -401,12 +401,15 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
         n = b.nbf
         J, K = np.zeros((n, n)), np.zeros((n, n))
         rc.JK_direct(J, K, b, D, schwarz_tau=0.0)  # plans the work: the class table is known from here
-        wc = [k for k, c in enumerate(b.class_stats()) if sum(c["class"]) >= 5]
-        assert len(wc) == 8
+        wc = [k for k, c in enumerate(b.class_stats()) if sum(c["class"]) >= 4]
+        assert len(wc) == 13
         for k in wc:
             b.set_tile_shape(k, 0, 0)
             b.set_tile_shape(k, 1, 0)
         rc.JK_direct(J, K, b, D, schwarz_tau=0.0)
+        assert np.abs(J - Jr).max() < 1e-12
+        assert np.abs(K - Kr).max() < 1e-12
+        rc.JK_direct(J, K, b, D, schwarz_tau=0.0, emulated=True)
         assert np.abs(J - Jr).max() < 1e-12
         assert np.abs(K - Kr).max() < 1e-12
         Jm, Km = np.zeros((n, n)), np.zeros((n, n))
@@ -414,3 +417,41 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
         assert np.abs(Jm - Jr).max() < 1e-5 and np.abs(Km - Kr).max() < 1e-5
         with pytest.raises(rc.RchemError):
             b.set_tile_shape(0, 0, 0)  # (ss|ss) has no warp-cooperative kernel
+
+
+@pytest.mark.parametrize("name", ["6-31gs-fit", "6-31gss-fit"])
+def test_build_I_and_jk_inmem_d_shells_vs_oracle(gpu, oracle_mod, name):
+    """The dense ERI tensor (ERI-store epilogue of all 21 classes, d on O and p
+    on H) and the in-memory J/K against the oracle's build_I/JK_inmem
+    (src/basis.rs:430-484)."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    Z, R = rc.geometry.water_monomer()
+    ob = O.expand_basis(Z, R, rc.load_bse(name))
+    Ir = O.build_I(ob)
+    D = _sym_density(np.random.default_rng(7), ob.n)
+    with rc.Basis(Z, R, name) as b:
+        I = rc.build_I(b)
+        np.testing.assert_allclose(I, Ir, atol=1e-12, rtol=0)
+        J, K = rc.JK_inmem(I, D)
+        Jr, Kr = O.JK_inmem(Ir, D)
+        np.testing.assert_allclose(J, Jr, atol=1e-12, rtol=0)
+        np.testing.assert_allclose(K, Kr, atol=1e-12, rtol=0)
+
+
+@pytest.mark.parametrize("order", [(0, 0, 0), (1, 0, 0), (0, 1, 1), (2, 0, 1), (1, 1, 1), (0, 0, 3)])
+def test_moment_matrices_vs_oracle(gpu, oracle_mod, order):
+    """Multipole-moment matrices (src/integrals/os86.rs:775-828) about an
+    off-origin centre, d functions included."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    Z, R = rc.geometry.water_monomer()
+    center = [0.3, -0.2, 0.5]
+    ob = O.expand_basis(Z, R, rc.load_bse("6-31gss-fit"))
+    Mr = O.M(ob, center, list(order))
+    with rc.Basis(Z, R, "6-31gss-fit") as b:
+        M = rc.moment(b, center, order)
+    scale = max(1.0, float(np.abs(Mr).max()))
+    np.testing.assert_allclose(M, Mr, atol=1e-13 * scale, rtol=0)
