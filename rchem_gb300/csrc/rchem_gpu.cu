@@ -59,6 +59,17 @@ static int set_err(int code, const char *fmt, ...) {
         if (r_ != RCHEM_OK) return r_; \
     } while (0)
 
+// frees a temporary device allocation on every return path
+struct CudaFreeGuard {
+    void *p;
+    explicit CudaFreeGuard(void *q) : p(q) {}
+    ~CudaFreeGuard() {
+        if (p) cudaFree(p);
+    }
+    CudaFreeGuard(const CudaFreeGuard &) = delete;
+    CudaFreeGuard &operator=(const CudaFreeGuard &) = delete;
+};
+
 extern "C" const char *rchem_last_error(void) { return g_err; }
 extern "C" int rchem_abi_version(void) { return 1; }
 
@@ -91,11 +102,15 @@ static int get_tables(const DevTables **out) {
         for (int k = 0; k < RCHEM_NCLASS; ++k) CK(rchem_eri_prepare[k]());  // before any stream capture
         DevTables n;
         CK(cudaMalloc(&n.boys64, b64.size() * sizeof(double)));
+        CudaFreeGuard g64(n.boys64);
         CK(cudaMalloc(&n.boys32, b32.size() * sizeof(float)));
+        CudaFreeGuard g32(n.boys32);
         CK(cudaMalloc(&n.boysdf, bdf.size() * sizeof(float2)));
+        CudaFreeGuard gdf(n.boysdf);
         CK(cudaMemcpy(n.boys64, b64.data(), b64.size() * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boys32, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boysdf, bdf.data(), bdf.size() * sizeof(float2), cudaMemcpyHostToDevice));
+        g64.p = g32.p = gdf.p = nullptr;  // kept for the life of the process
         t = n;
     }
     *out = &t;
@@ -450,8 +465,11 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     EriSeg *d_s = nullptr;
     double *d_Q = nullptr;
     CKR(upload(&d_t, tasks, b->stream));
+    CudaFreeGuard g_t(d_t);
     CKR(upload(&d_s, segs, b->stream));
+    CudaFreeGuard g_s(d_s);
     CK(cudaMalloc(&d_Q, (size_t)np * sizeof(double)));
+    CudaFreeGuard g_Q(d_Q);
     EriArgs a = base_args(b);
     a.J = d_Q;
     a.segs = d_s;
@@ -468,9 +486,6 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     Q.assign(np, 0.0);
     CK(cudaMemcpyAsync(Q.data(), d_Q, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
-    cudaFree(d_t);
-    cudaFree(d_s);
-    cudaFree(d_Q);
     return RCHEM_OK;
 }
 
@@ -1019,19 +1034,16 @@ static int onee(rchem_basis b, int kind, const double *center, int ox, int oy, i
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     double *dst = (where == RCHEM_DEVICE) ? out : b->d_Jo;
     double *d_c = nullptr;
-    if (kind == 3) {
-        CK(cudaMalloc(&d_c, 3 * sizeof(double)));
-        CK(cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-    }
+    if (kind == 3) CK(cudaMalloc(&d_c, 3 * sizeof(double)));
+    CudaFreeGuard g_c(d_c);
+    if (kind == 3) CK(cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, b->stream));
     const long long n2 = b->packed;
     const int th = 128;
     k_onee_matrix<<<(unsigned)((n2 + th - 1) / th), th, 0, b->stream>>>(kind, n2, b->ngeom, b->d_geom, b->d_ao, b->d_sh,
                                                                          b->d_pexp, b->d_pcoef, b->d_Z, b->d_R,
                                                                          b->tabs->boys64, d_c, ox, oy, oz, dst);
     CK(cudaGetLastError());
-    int rc = finish_out(b, dst, out, (size_t)n2, where);
-    if (d_c) cudaFree(d_c);
-    return rc;
+    return finish_out(b, dst, out, (size_t)n2, where);
 }
 
 extern "C" int rchem_S(rchem_basis b, double *out, int where) { return onee(b, 0, nullptr, 0, 0, 0, out, where); }
@@ -1395,35 +1407,38 @@ extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
     const size_t n = b->nbf, n4 = n * n * n * n;
     if (n > 256) return set_err(RCHEM_ERR_UNSUPPORTED, "dense n^4 tensor for n=%zu", n);
     CKR(plan_tasks(b, 0.0, 0.0));  // every quartet, FP64
-    double *d_I = I;
-    if (where == RCHEM_HOST) CK(cudaMalloc(&d_I, n4 * sizeof(double)));
+    double *d_I = I, *d_tmp = nullptr;
+    if (where == RCHEM_HOST) {
+        CK(cudaMalloc(&d_tmp, n4 * sizeof(double)));
+        d_I = d_tmp;
+    }
+    CudaFreeGuard g_I(d_tmp);
     CK(cudaMemsetAsync(d_I, 0, n4 * sizeof(double), b->stream));
     EriArgs a = base_args(b);
     a.eri = d_I;
     CKR(launch_lists(b, a, EPI_STORE, false));
-    int rc = RCHEM_OK;
-    if (where == RCHEM_HOST) {
-        rc = finish_out(b, d_I, I, n4, RCHEM_HOST);
-        cudaFree(d_I);
-    } else {
-        CK(cudaStreamSynchronize(b->stream));
-    }
-    return rc;
+    if (where == RCHEM_HOST) return finish_out(b, d_I, I, n4, RCHEM_HOST);
+    CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
 }
 
 extern "C" int rchem_jk_inmem(int n, const double *I, const double *D, double *J, double *K, int where) {
     if (n <= 0 || !I || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "bad argument");
+    if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     const size_t nn = (size_t)n * n, n4 = nn * nn;
     const double *dI = I, *dD = D;
     double *dJ = J, *dK = K;
-    std::vector<void *> tmp;
+    double *a = nullptr, *b2 = nullptr, *c = nullptr, *d = nullptr;
+    CudaFreeGuard ga(nullptr), gb(nullptr), gc(nullptr), gd(nullptr);
     if (where == RCHEM_HOST) {
-        double *a, *b2, *c, *d;
         CK(cudaMalloc(&a, n4 * sizeof(double)));
+        ga.p = a;
         CK(cudaMalloc(&b2, nn * sizeof(double)));
+        gb.p = b2;
         CK(cudaMalloc(&c, nn * sizeof(double)));
+        gc.p = c;
         CK(cudaMalloc(&d, nn * sizeof(double)));
-        tmp = {a, b2, c, d};
+        gd.p = d;
         CK(cudaMemcpy(a, I, n4 * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(b2, D, nn * sizeof(double), cudaMemcpyHostToDevice));
         dI = a;
@@ -1436,7 +1451,6 @@ extern "C" int rchem_jk_inmem(int n, const double *I, const double *D, double *J
     if (where == RCHEM_HOST) {
         CK(cudaMemcpy(J, dJ, nn * sizeof(double), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(K, dK, nn * sizeof(double), cudaMemcpyDeviceToHost));
-        for (void *p : tmp) cudaFree(p);
     } else {
         CK(cudaDeviceSynchronize());
     }
