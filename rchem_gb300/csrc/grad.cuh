@@ -218,77 +218,84 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     const int zd = la + lb + 2;
     double Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], R[GR_NR], F[GR_LMAX + 1];
     double Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
-    const int nk = kp.npp, ntot = active ? bp.npp * nk : 0;  // idle lanes only join the reduction
-    for (int tq = r; tq < ntot; tq += G) {
-        const int ia = tq / nk, ic = tq - ia * nk;
-        const PairPrim pa = g.prims[bp.prim0 + ia];
-        const double aa = pa.pad, ab = pa.p - pa.pad;  // pad holds the exponent on the first shell
-        const PairPrim pc = g.prims[kp.prim0 + ic];
-        const double ac = pc.pad;
-        const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
-        const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
-        const double T = rho * (X * X + Y * Y + Zc * Zc);
-        boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
-        gr_R(L1, rho, X, Y, Zc, F, R);
-        for (int dd = 0; dd < 3; ++dd) {
-            gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
-            gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
-            for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
-                for (int j = 0; j <= ld; ++j)
-                    for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
+    // work units: (primitive quartet, ket component pair); the G lanes split them
+    // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
+    const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
+    const int nunits = active ? ntot * ncd : 0;  // idle lanes only join the reduction
+    int cur = -1;
+    double aa = 0.0, ab = 0.0, ac = 0.0;
+    for (int u = r; u < nunits; u += G) {
+        const int tq = u / ncd, kcd = u - tq * ncd;
+        if (tq != cur) {  // primitive-quartet tables, kept while the lane stays on it
+            cur = tq;
+            const int ia = tq / nk, ic = tq - ia * nk;
+            const PairPrim pa = g.prims[bp.prim0 + ia];
+            const PairPrim pc = g.prims[kp.prim0 + ic];
+            aa = pa.pad;  // pad holds the exponent on the first shell
+            ab = pa.p - pa.pad;
+            ac = pc.pad;
+            const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
+            const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
+            const double T = rho * (X * X + Y * Y + Zc * Zc);
+            boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
+            gr_R(L1, rho, X, Y, Zc, F, R);
+            for (int dd = 0; dd < 3; ++dd) {
+                gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
+                gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
+                for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
+                    for (int j = 0; j <= ld; ++j)
+                        for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
+            }
         }
         int s[3];
-        for (int kc = 0; kc < nc; ++kc) {
-            for (int kd = 0; kd < nd; ++kd) {
-                const double *Gq = Gam + (kc * nd + kd) * na * nb;
-                // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
-                gr_zvec(Ek, cC[kc], cD[kd], R, zd, la + lb + 1, Z0);
+        const int kc = kcd / nd, kd = kcd - kc * nd;
+        const double *Gq = Gam + (kc * nd + kd) * na * nb;
+        // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
+        gr_zvec(Ek, cC[kc], cD[kd], R, zd, la + lb + 1, Z0);
+        for (int x = 0; x < 3; ++x) {
+            s[0] = cC[kc][0];
+            s[1] = cC[kc][1];
+            s[2] = cC[kc][2];
+            s[x] += 1;
+            gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zp[x]);
+            if (cC[kc][x] > 0) {
+                s[x] -= 2;
+                gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zm[x]);
+            }
+        }
+        for (int ka = 0; ka < na; ++ka) {
+            const int *A = cA[ka];
+            for (int kb = 0; kb < nb; ++kb) {
+                const double Gm = Gq[ka * nb + kb];
+                if (Gm == 0.0) continue;
+                const int *B = cB[kb];
                 for (int x = 0; x < 3; ++x) {
-                    s[0] = cC[kc][0];
-                    s[1] = cC[kc][1];
-                    s[2] = cC[kc][2];
+                    // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
+                    s[0] = A[0];
+                    s[1] = A[1];
+                    s[2] = A[2];
                     s[x] += 1;
-                    gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zp[x]);
-                    if (cC[kc][x] > 0) {
+                    double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
+                    if (A[x] > 0) {
                         s[x] -= 2;
-                        gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zm[x]);
+                        v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
                     }
-                }
-                for (int ka = 0; ka < na; ++ka) {
-                    const int *A = cA[ka];
-                    for (int kb = 0; kb < nb; ++kb) {
-                        const double Gm = Gq[ka * nb + kb];
-                        if (Gm == 0.0) continue;
-                        const int *B = cB[kb];
-                        for (int x = 0; x < 3; ++x) {
-                            // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
-                            s[0] = A[0];
-                            s[1] = A[1];
-                            s[2] = A[2];
-                            s[x] += 1;
-                            double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
-                            if (A[x] > 0) {
-                                s[x] -= 2;
-                                v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
-                            }
-                            gA[x] += Gm * v;
-                            // centre B
-                            s[0] = B[0];
-                            s[1] = B[1];
-                            s[2] = B[2];
-                            s[x] += 1;
-                            v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
-                            if (B[x] > 0) {
-                                s[x] -= 2;
-                                v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
-                            }
-                            gB[x] += Gm * v;
-                            // centre C
-                            v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
-                            if (cC[kc][x] > 0) v -= cC[kc][x] * gr_dot(Eb, A, B, Zm[x], zd);
-                            gC[x] += Gm * v;
-                        }
+                    gA[x] += Gm * v;
+                    // centre B
+                    s[0] = B[0];
+                    s[1] = B[1];
+                    s[2] = B[2];
+                    s[x] += 1;
+                    v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
+                    if (B[x] > 0) {
+                        s[x] -= 2;
+                        v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
                     }
+                    gB[x] += Gm * v;
+                    // centre C
+                    v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
+                    if (cC[kc][x] > 0) v -= cC[kc][x] * gr_dot(Eb, A, B, Zm[x], zd);
+                    gC[x] += Gm * v;
                 }
             }
         }

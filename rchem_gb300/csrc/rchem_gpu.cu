@@ -1168,15 +1168,17 @@ static int plan_gradient(rchem_basis b, double tau) {
                 total += nk;
             }
             if (total == 0) continue;
-            int lg = 0;
-            while (lg < 5 && nprimq >= kGradPrimPerLane << (lg + 1)) ++lg;
-            const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
             // s/p classes each get their specialised kernel; every class with a d
-            // shell shares one launch of the run-time kernel (list RCHEM_NCLASS)
+            // shell shares one launch of the run-time kernel (list RCHEM_NCLASS),
+            // whose lanes split primitive quartets x ket component pairs
             const int k = quartet_kernel(gb.cls, gk.cls);
             const int *l = rchem_class_l[k];
             const int list = (l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1) ? k : RCHEM_NCLASS;
-            pack_tasks(segs, s0, total, lg, ((nprimq + (1 << lg) - 1) >> lg) * work, per_class[list]);
+            const long long units = list == RCHEM_NCLASS ? nprimq * ncart(gk.la) * ncart(gk.lb) : nprimq;
+            int lg = 0;
+            while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
+            const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
+            pack_tasks(segs, s0, total, lg, ((units + (1 << lg) - 1) >> lg) * work, per_class[list]);
         }
     }
     // one launch per class (its specialised kernel), heaviest tasks first
