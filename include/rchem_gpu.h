@@ -97,8 +97,9 @@ typedef struct {
     double fp32_tau;    /* quartets with Q_ab Q_cd < fp32_tau in FP32, FP64 accumulation (0 => FP64 only) */
     int where;          /* RCHEM_HOST or RCHEM_DEVICE for D, J, K */
     int emulated;       /* 1: the FP64 quartets in double-float arithmetic on the FP32 pipe
-                           (~48-bit significand, classes with l_a+l_b+l_c+l_d <= 4; higher
-                           classes stay FP64).  0: native FP64 */
+                           (~48-bit significand): every class with l_a+l_b+l_c+l_d <= 4, and
+                           the larger classes whose list runs the warp-cooperative kernel
+                           (rchem_autotune's choice); the others stay FP64.  0: native FP64 */
 } rchem_jk_opts;
 
 /* Work done by the last Fock build of a handle. */

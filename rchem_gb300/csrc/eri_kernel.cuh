@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 // (emulated FP64; instantiated up to l_a+l_b+l_c+l_d = 4, FP64 above)
 // ---------------------------------------------------------------------------
 // Warp-cooperative J/K kernel for the large classes (EriClass::WC, total
-// angular momentum 4 and up; double, float and, up to L 4, double-float): one warp
+// angular momentum 4 and up; double, float and double-float): one warp
 // per contracted shell quartet, the recurrence intermediates in shared
 // memory.  The generated program (EriProg) lists the VRR terms and the HRR
 // terms level by level of their DAG; within a level the terms are independent
@@ -533,11 +533,9 @@ cudaError_t prepare_eri_class() {
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)WcShape<LA, LB, LC, LD, double>::SMEM);
         if (e != cudaSuccess) return e;
-        if constexpr (LA + LB + LC + LD <= 4) {
-            e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, df64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)WcShape<LA, LB, LC, LD, df64>::SMEM);
-            if (e != cudaSuccess) return e;
-        }
+        e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, df64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)WcShape<LA, LB, LC, LD, df64>::SMEM);
+        if (e != cudaSuccess) return e;
         return cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)WcShape<LA, LB, LC, LD, float>::SMEM);
     }
@@ -556,12 +554,10 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
                 using W = WcShape<LA, LB, LC, LD, float>;
                 eri_wc_kernel<LA, LB, LC, LD, float>
                     <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
-            } else if (LA + LB + LC + LD <= 4 && prec == 2) {
-                if constexpr (LA + LB + LC + LD <= 4) {
-                    using W = WcShape<LA, LB, LC, LD, df64>;
-                    eri_wc_kernel<LA, LB, LC, LD, df64>
-                        <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
-                }
+            } else if (prec == 2) {
+                using W = WcShape<LA, LB, LC, LD, df64>;
+                eri_wc_kernel<LA, LB, LC, LD, df64>
+                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
             } else {
                 using W = WcShape<LA, LB, LC, LD, double>;
                 eri_wc_kernel<LA, LB, LC, LD, double>
