@@ -342,6 +342,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 template <int LA, int LB, int LC, int LD> struct EriProg;
 
 #define RCHEM_WC_SMEM (96 * 1024)  // shared memory per block the warp count aims at
+#define WC_U 4                     // independent recurrence terms per lane and pass
 
 template <int LA, int LB, int LC, int LD, typename R>
 struct WcShape {
@@ -420,17 +421,26 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         };
         for (int lv = 0; lv < P::NVL; ++lv) {
             const int e = __ldg(vlev + lv + 1);
-            // two independent terms per lane and pass: all operand loads before either store
-            for (int t = __ldg(vlev + lv) + lane; t < e; t += 64) {
-                const bool two = t + 32 < e;
-                const uint4 o0 = __ldg(vprog + t), o1 = two ? __ldg(vprog + t + 32) : o0;
-                const R a0 = S[o0.x >> 16], b0 = S[o0.y & 0xffff], c0 = S[o0.y >> 16], d0 = S[o0.z & 0xffff],
-                        g0 = S[o0.z >> 16];
-                const R a1 = S[o1.x >> 16], b1 = S[o1.y & 0xffff], c1 = S[o1.y >> 16], d1 = S[o1.z & 0xffff],
-                        g1 = S[o1.z >> 16];
-                const R v0 = term(o0, a0, b0, c0, d0, g0), v1 = term(o1, a1, b1, c1, d1, g1);
-                S[o0.x & 0xffff] = v0;
-                if (two) S[o1.x & 0xffff] = v1;
+            // WC_U independent terms per lane and pass: every program word, then
+            // every operand, is loaded before any result is stored (latency overlap)
+            for (int t = __ldg(vlev + lv) + lane; t < e; t += 32 * WC_U) {
+                uint4 o[WC_U];
+                R ta[WC_U], tb[WC_U], tc[WC_U], td[WC_U], tg[WC_U];
+#pragma unroll
+                for (int u = 0; u < WC_U; ++u) o[u] = t + 32 * u < e ? __ldg(vprog + t + 32 * u) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+                for (int u = 0; u < WC_U; ++u) {
+                    ta[u] = S[o[u].x >> 16];
+                    tb[u] = S[o[u].y & 0xffff];
+                    tc[u] = S[o[u].y >> 16];
+                    td[u] = S[o[u].z & 0xffff];
+                    tg[u] = S[o[u].z >> 16];
+                }
+#pragma unroll
+                for (int u = 0; u < WC_U; ++u) {
+                    const R v = term(o[u], ta[u], tb[u], tc[u], td[u], tg[u]);
+                    if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
+                }
             }
             __syncwarp();
         }
@@ -451,13 +461,21 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
     };
     for (int lv = 0; lv < P::NHL; ++lv) {
         const int e = __ldg(hlev + lv + 1);
-        for (int t = __ldg(hlev + lv) + lane; t < e; t += 64) {
-            const bool two = t + 32 < e;
-            const uint2 o0 = __ldg(hprog + t), o1 = two ? __ldg(hprog + t + 32) : o0;
-            const R x0 = S[o0.x >> 16], y0 = S[o0.y & 0xffff], x1 = S[o1.x >> 16], y1 = S[o1.y & 0xffff];
-            const R v0 = rchem_fma(hcoef(o0), y0, x0), v1 = rchem_fma(hcoef(o1), y1, x1);
-            S[o0.x & 0xffff] = v0;
-            if (two) S[o1.x & 0xffff] = v1;
+        for (int t = __ldg(hlev + lv) + lane; t < e; t += 32 * WC_U) {
+            uint2 o[WC_U];
+            R tx[WC_U], ty[WC_U];
+#pragma unroll
+            for (int u = 0; u < WC_U; ++u) o[u] = t + 32 * u < e ? __ldg(hprog + t + 32 * u) : make_uint2(0, 0);
+#pragma unroll
+            for (int u = 0; u < WC_U; ++u) {
+                tx[u] = S[o[u].x >> 16];
+                ty[u] = S[o[u].y & 0xffff];
+            }
+#pragma unroll
+            for (int u = 0; u < WC_U; ++u) {
+                const R v = rchem_fma(hcoef(o[u]), ty[u], tx[u]);
+                if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
+            }
         }
         __syncwarp();
     }

@@ -31,6 +31,7 @@ def main(argv=None):
     ap.add_argument("--fp32-tau", type=float, default=0.0)
     ap.add_argument("--emulated", action="store_true", help="double-float arithmetic for the FP64 quartets")
     ap.add_argument("--gradient", action="store_true", help="run the nuclear gradient instead of Fock builds")
+    ap.add_argument("--autotune", action="store_true", help="autotune the tile shapes before the builds")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
@@ -48,6 +49,8 @@ def main(argv=None):
             b.block(Dh, g)[:] = _sym(rng, n, 0.1)
             b.block(Wh, g)[:] = _sym(rng, n, 0.1)
         D, W = torch.from_numpy(Dh).cuda(), torch.from_numpy(Wh).cuda()
+        if a.autotune:
+            b.autotune(1e-12, a.fp32_tau, emulated=a.emulated)
         for _ in range(a.builds):
             if a.gradient:
                 batch.gradient_batch(b, {"D": D, "W": W})
@@ -63,6 +66,8 @@ def main(argv=None):
         D = torch.from_numpy(_sym(rng, n, 0.1)).cuda()
         W = torch.from_numpy(_sym(rng, n, 0.1)).cuda()
         J, K = torch.empty_like(D), torch.empty_like(D)
+        if a.autotune:
+            b.autotune(1e-12, a.fp32_tau, emulated=a.emulated)
         torch.cuda.synchronize()
         for _ in range(a.builds):
             if a.gradient:
