@@ -16,6 +16,16 @@
 template <int LA, int LB, int LC, int LD> struct EriClass;
 #include "eri_all.inc"
 
+// the warp-cooperative programs (csrc/_gen/eri_prog_*.inc), read on the host
+struct uint4 {
+    unsigned x, y, z, w;
+};
+struct uint2 {
+    unsigned x, y;
+};
+template <int LA, int LB, int LC, int LD> struct EriProg;
+#include "eri_prog_all.inc"
+
 static std::vector<double> g_b64;
 static std::vector<float> g_b32;
 
@@ -77,6 +87,65 @@ static void block(const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *re
     for (int i = 0; i < K::NA * K::NB * K::NC * K::ND; ++i) res[i] = (double)out[i];
 }
 
+// The same contracted block, evaluated by running the class's warp-cooperative
+// program one term after another (level order is a valid sequential order).
+template <int LA, int LB, int LC, int LD>
+static void block_prog(const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *res) {
+    using K = EriClass<LA, LB, LC, LD>;
+    using P = EriProg<LA, LB, LC, LD>;
+    std::vector<double> S(P::SCR, 0.0), acc(P::NT, 0.0);
+    const double cp = std::sqrt(2.0) * std::pow(M_PI, 1.25);
+    for (int i = 0; i < A.n; ++i)
+        for (int j = 0; j < B.n; ++j) {
+            double p = A.e[i] + B.e[j], Pc[3], r2 = 0;
+            for (int d = 0; d < 3; ++d) {
+                Pc[d] = (A.e[i] * A.R[d] + B.e[j] * B.R[d]) / p;
+                r2 += (A.R[d] - B.R[d]) * (A.R[d] - B.R[d]);
+            }
+            double Kab = A.c[i] * B.c[j] * std::exp(-A.e[i] * B.e[j] / p * r2) * cp / p;
+            for (int k = 0; k < C.n; ++k)
+                for (int l = 0; l < D.n; ++l) {
+                    double q = C.e[k] + D.e[l], Qc[3], s2 = 0;
+                    for (int d = 0; d < 3; ++d) {
+                        Qc[d] = (C.e[k] * C.R[d] + D.e[l] * D.R[d]) / q;
+                        s2 += (C.R[d] - D.R[d]) * (C.R[d] - D.R[d]);
+                    }
+                    double Kcd = C.c[k] * D.c[l] * std::exp(-C.e[k] * D.e[l] / q * s2) * cp / q;
+                    const double rs = 1.0 / std::sqrt(p + q), ipq = rs * rs;
+                    const double PQ[3] = {Pc[0] - Qc[0], Pc[1] - Qc[1], Pc[2] - Qc[2]};
+                    const double qi = q * ipq, pi = p * ipq;
+                    const double T = p * qi * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
+                    double F[K::L + 1];
+                    boys_eval<K::L, double>(T, Kab * Kcd * rs, g_b64.data(), F);
+                    for (int m = 0; m <= K::L; ++m) S[m] = F[m];
+                    const double PA[3] = {Pc[0] - A.R[0], Pc[1] - A.R[1], Pc[2] - A.R[2]};
+                    const double QC[3] = {Qc[0] - C.R[0], Qc[1] - C.R[1], Qc[2] - C.R[2]};
+                    const double WP[3] = {-qi * PQ[0], -qi * PQ[1], -qi * PQ[2]};
+                    const double WQ[3] = {pi * PQ[0], pi * PQ[1], pi * PQ[2]};
+                    const double ohp = 0.5 / p, ohq = 0.5 / q, ohpq = 0.5 * ipq;
+                    for (int t = 0; t < P::vrrlv()[P::NVL]; ++t) {
+                        const uint4 op = P::vrr()[t];
+                        const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
+                        const double X = ket ? QC[dir] : PA[dir], Y = ket ? WQ[dir] : WP[dir];
+                        double v = Y * S[op.y & 0xffff] + X * S[op.x >> 16];
+                        if (n1) v += n1 * (ket ? ohq : ohp) * (S[op.y >> 16] - (ket ? pi : qi) * S[op.z & 0xffff]);
+                        if (n2) v += n2 * ohpq * S[op.z >> 16];
+                        S[op.x & 0xffff] = v;
+                    }
+                    for (int t = 0; t < P::NT; ++t) acc[t] += S[P::tgt()[t]];
+                }
+        }
+    for (int t = 0; t < P::NT; ++t) S[t] = acc[t];
+    const double AB[3] = {A.R[0] - B.R[0], A.R[1] - B.R[1], A.R[2] - B.R[2]};
+    const double CD[3] = {C.R[0] - D.R[0], C.R[1] - D.R[1], C.R[2] - D.R[2]};
+    for (int t = 0; t < P::hrrlv()[P::NHL]; ++t) {
+        const uint2 op = P::hrr()[t];
+        const int dir = (op.y >> 16) & 255, side = op.y >> 24;
+        S[op.x & 0xffff] = S[op.x >> 16] + (side ? CD[dir] : AB[dir]) * S[op.y & 0xffff];
+    }
+    for (int k = 0; k < P::NOUT; ++k) res[k] = P::onorm()[k] * S[P::out()[k]];
+}
+
 template <int LA, int LB, int LC, int LD>
 static void blk(int f32, const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *res) {
     if (f32) block<LA, LB, LC, LD, float>(A, B, C, D, res);
@@ -105,6 +174,31 @@ extern "C" int host_eri_block(int la, int lb, int lc, int ld, int f32, const dou
         CASE(2, 0, 0, 0) CASE(2, 0, 1, 0) CASE(2, 0, 1, 1) CASE(2, 0, 2, 0) CASE(2, 1, 0, 0) CASE(2, 1, 1, 0)
         CASE(2, 1, 1, 1) CASE(2, 1, 2, 0) CASE(2, 1, 2, 1) CASE(2, 2, 0, 0) CASE(2, 2, 1, 0) CASE(2, 2, 1, 1)
         CASE(2, 2, 2, 0) CASE(2, 2, 2, 1) CASE(2, 2, 2, 2)
+    }
+    return 1;
+}
+
+extern "C" int host_eri_block_prog(int la, int lb, int lc, int ld, const double *R, const int *n, const double *e,
+                                   const double *c, double *res) {
+    init_tables();
+    Sh s[4];
+    int off = 0;
+    for (int k = 0; k < 4; ++k) {
+        for (int d = 0; d < 3; ++d) s[k].R[d] = R[3 * k + d];
+        s[k].n = n[k];
+        s[k].e = e + off;
+        s[k].c = c + off;
+        off += n[k];
+    }
+    const int key = la * 1000 + lb * 100 + lc * 10 + ld;
+#define PCASE(a, b, c_, d)                                                  \
+    case a * 1000 + b * 100 + c_ * 10 + d:                                  \
+        block_prog<a, b, c_, d>(s[0], s[1], s[2], s[3], res);              \
+        return 0;
+    switch (key) {
+        PCASE(1, 1, 1, 1) PCASE(2, 0, 1, 1) PCASE(2, 0, 2, 0) PCASE(2, 1, 1, 0) PCASE(2, 1, 1, 1) PCASE(2, 1, 2, 0)
+        PCASE(2, 1, 2, 1) PCASE(2, 2, 0, 0) PCASE(2, 2, 1, 0) PCASE(2, 2, 1, 1) PCASE(2, 2, 2, 0) PCASE(2, 2, 2, 1)
+        PCASE(2, 2, 2, 2)
     }
     return 1;
 }

@@ -19,6 +19,9 @@ CLASSES = [(0, 0, 0, 0), (1, 0, 0, 0), (1, 0, 1, 0), (1, 1, 0, 0), (1, 1, 1, 0),
            (2, 0, 1, 0), (2, 0, 1, 1), (2, 0, 2, 0), (2, 1, 0, 0), (2, 1, 1, 0), (2, 1, 1, 1), (2, 1, 2, 0),
            (2, 1, 2, 1), (2, 2, 0, 0), (2, 2, 1, 0), (2, 2, 1, 1), (2, 2, 2, 0), (2, 2, 2, 1), (2, 2, 2, 2)]
 
+# classes with a warp-cooperative program (total angular momentum >= 4)
+PROG_CLASSES = [c for c in CLASSES if sum(c) >= 4]
+
 
 @pytest.fixture(scope="module")
 def hostlib(tmp_path_factory):
@@ -33,11 +36,15 @@ def hostlib(tmp_path_factory):
     with open(d / "eri_all.inc", "w") as f:
         for c in CLASSES:
             f.write('#include "%s/eri_class_%d%d%d%d.inc"\n' % ((str(gen),) + c))
+    with open(d / "eri_prog_all.inc", "w") as f:
+        for c in PROG_CLASSES:
+            f.write('#include "%s/eri_prog_%d%d%d%d.inc"\n' % ((str(gen),) + c))
     so = d / "libhost.so"
     subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, "-I", str(d), "-o", str(so),
                     os.path.join(ROOT, "tests", "host_eri_check.cpp")], check=True)
     L = C.CDLL(str(so))
     L.host_eri_block.argtypes = [C.c_int] * 5 + [C.c_void_p] * 5
+    L.host_eri_block_prog.argtypes = [C.c_int] * 4 + [C.c_void_p] * 5
     L.host_boys.restype = C.c_double
     L.host_boys.argtypes = [C.c_int, C.c_double, C.c_int]
     return L
@@ -84,6 +91,28 @@ def test_generated_class_vs_oracle(hostlib, port, cls):
             res = res.reshape(ref.shape)
             scale = 1.0 if f32 == 0 else np.abs(ref).max()
             assert np.abs(res - ref).max() <= tol * scale, (cls, f32, np.abs(res - ref).max())
+
+
+@pytest.mark.parametrize("cls", PROG_CLASSES)
+def test_warp_cooperative_program_vs_oracle(hostlib, port, cls):
+    """The generated level-ordered VRR/HRR program of a large class, run term by
+    term on the host, gives the oracle's contracted integrals."""
+    import oracle
+
+    rng = np.random.default_rng(sum(cls) * 11 + cls[1])
+    R = rng.uniform(-1.5, 1.5, (4, 3))
+    n = np.array([1, 2, 1, 2])
+    e = [rng.uniform(0.2, 3.0, k) for k in n]
+    c = [rng.uniform(0.2, 1.0, k) for k in n]
+    cs = np.concatenate([c[k] * np.array([port.pgto_norm(x, cls[k], 0, 0) for x in e[k]]) for k in range(4)])
+    es = np.concatenate(e)
+    ref = _block_oracle(port, oracle, cls, R, e, c)
+    res = np.zeros(ref.size)
+    rc = hostlib.host_eri_block_prog(*cls, np.ascontiguousarray(R).ctypes.data,
+                                     np.ascontiguousarray(n, dtype=np.int32).ctypes.data, es.ctypes.data,
+                                     cs.ctypes.data, res.ctypes.data)
+    assert rc == 0
+    assert np.abs(res.reshape(ref.shape) - ref).max() <= 1e-14
 
 
 def test_boys_evaluator(hostlib, port):
