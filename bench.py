@@ -231,7 +231,7 @@ def north_star(rc, torch):
         r = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        g = rc.batch.gradient_batch(bb, r)
+        g = rc.batch.gradient_batch(bb, r, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         rec[tag] = {"scf_s": t1 - t0, "gradient_s": t2 - t1, "s_per_geometry": (t2 - t0) / bb.ngeom,
@@ -267,9 +267,25 @@ def north_star(rc, torch):
         g = rc.scf.gradient(b, res)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        out["h2o4_631gss_gradient"] = {"nbf": b.nbf, "scf_s": t1 - t0, "gradient_s": t2 - t1,
-                                       "s_per_geometry": t2 - t0, "max_abs_grad": float(g.abs().max()),
-                                       "check": "central finite differences to 1e-6 Eh/bohr in tests/test_gpu_gradient.py"}
+        rec = {"nbf": b.nbf, "scf_s": t1 - t0, "gradient_s": t2 - t1, "s_per_geometry": t2 - t0,
+               "max_abs_grad": float(g.abs().max()),
+               "check": "central finite differences to 1e-6 Eh/bohr in tests/test_gpu_gradient.py"}
+        # the same energy + gradient in the mixed and emulated+mixed forms
+        for tag, tau32, emul in (("mixed", 1e-6, False), ("emulated_mixed", 1e-6, True)):
+            b.autotune(1e-12, tau32, emulated=emul)
+            rc.scf.gradient(b, rc.scf.rhf(b, fp32_tau=tau32, emulated=emul), fp32_tau=tau32, emulated=emul)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r2 = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            g2 = rc.scf.gradient(b, r2, fp32_tau=tau32, emulated=emul)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            rec[tag] = {"scf_s": t1 - t0, "gradient_s": t2 - t1, "s_per_geometry": t2 - t0,
+                        "dE_vs_fp64_Eh": r2["e_total"] - res["e_total"],
+                        "max_abs_dgrad_vs_fp64": float((g2 - g).abs().max())}
+        out["h2o4_631gss_gradient"] = rec
     return out
 
 

@@ -159,8 +159,10 @@ int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K
  * (both without the factor 2, as in src/bin/rchem.rs:101-104).  Adjoint
  * kernels: derivative ERIs contracted on the fly with the density products,
  * derivative S/T/V contracted with W and D, Hellmann-Feynman term included.
- * No counterpart in the reference, which has no gradients.  opts: schwarz_tau
- * and where (for D, W and grad); fp32_tau is ignored (FP64).
+ * No counterpart in the reference, which has no gradients.  opts: schwarz_tau,
+ * where (for D, W and grad), fp32_tau (s/p quartets with Q_ab Q_cd below it in
+ * FP32, the rest FP64; quartets with a d shell always FP64) and emulated (the
+ * FP64 s/p quartets in double-float arithmetic on the FP32 pipe).
  */
 int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
 

@@ -258,13 +258,14 @@ def _rhf_batch(bb, thresh_e, thresh_d, max_iter, diis, fp32_tau, schwarz_tau, em
             "converged": bool(conv.all())}
 
 
-def gradient_batch(bb: BatchBasis, res: dict, schwarz_tau=1e-12):
-    """Nuclear gradients of every geometry: one set of adjoint-kernel launches;
-    returns a list of (natoms_g x 3) arrays."""
+def gradient_batch(bb: BatchBasis, res: dict, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
+    """Nuclear gradients of every geometry: one set of adjoint-kernel launches
+    (precision options as in scf.gradient); returns a list of (natoms_g x 3) arrays."""
     import torch
 
     g = torch.empty(3 * len(bb.atomnos), dtype=torch.float64, device="cuda")
-    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=0.0, where=_lib.DEVICE)
+    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
+                    emulated=1 if emulated else 0)
     _after_torch(bb, res["D"], res["W"], g)
     _lib.check(_lib.lib().rchem_gradient(bb.handle, C.c_void_p(res["D"].data_ptr()), C.c_void_p(res["W"].data_ptr()),
                                          C.c_void_p(g.data_ptr()), C.byref(o)))

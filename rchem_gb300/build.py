@@ -59,7 +59,8 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == key:
         return LIB
     _generate()
-    srcs = [os.path.join(CSRC, "rchem_gpu.cu"), os.path.join(CSRC, "peak.cu")]
+    srcs = [os.path.join(CSRC, f) for f in ("rchem_gpu.cu", "peak.cu", "grad_sp_f64.cu", "grad_sp_f32.cu",
+                                            "grad_sp_df64.cu")]
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("eri_") and f.endswith(".cu"))
     nvcc = _nvcc()
 

@@ -29,6 +29,10 @@ struct GradArgs {
     int ntasks;
     const ShellPair *pairs;
     const PairPrim *prims;
+    const PairPrim32 *prims32;    // the same in FP32 (mixed form) ...
+    const PairPrimDF *primsdf;    // ... and double-float (emulated form)
+    const float *boys32;
+    const float2 *boysdf;
     const int *shell_atom;
     const int *shell_l;
     const double *boys64;
@@ -151,6 +155,7 @@ __device__ __forceinline__ double gr_dot(const double (*Eb)[GR_NI][GR_NI][GR_NT]
 
 #define GR_MAXC4 1296  // components of a (dd|dd) quartet
 
+#ifndef RCHEM_GRAD_NO_KERNELS  // translation units that only need the shared helpers
 // One warp task: up to 32 >> lg unique shell quartets, G = 2^lg lanes each
 // (the segment/task layout of the Fock build).  The G lanes split the
 // quartet's primitive quartets; Gamma (degeneracy and component norms folded
@@ -316,6 +321,7 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
         atomicAdd(g.grad + 3 * atD + x, -(gA[x] + gB[x] + gC[x]));
     }
 }
+#endif
 
 // One-electron part, one thread per ordered function pair (mu, nu) of a geometry:
 //   4 D_mn d_mu H_mn - 4 W_mn d_mu S_mn on the atom of mu,
@@ -376,6 +382,7 @@ __device__ __forceinline__ double gr_t1d(int i, int j, double b, const double (*
     return t;
 }
 
+#ifndef RCHEM_GRAD_NO_KERNELS
 // One thread per ordered function pair (mu, nu) of a geometry.  Per primitive
 // pair the Gaussian product, the 1-D overlap table (shared by S and T and by
 // every shifted component) and the Hermite tables are formed once; per
@@ -473,3 +480,4 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
     for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * sa.atom + x, 4.0 * Dmn * gH[x] - 4.0 * Wmn * gS[x]);
     (void)natoms_total;
 }
+#endif

@@ -1,5 +1,6 @@
 // grad_cls.cuh -- the two-electron gradient kernel specialised per integral
-// class for s and p shells (l <= 1 on every centre).
+// class for s and p shells (l <= 1 on every centre), in FP64, FP32 (the mixed
+// form's small quartets) or double-float (the emulated form).
 //
 // Same mathematics and work layout as k_grad2e (grad.cuh): McMurchie--Davidson
 // Hermite integrals, the shifted-angular-momentum derivative relation, Gamma
@@ -44,24 +45,24 @@ __device__ __forceinline__ void sfor(F &&f) {
 }
 
 // E[i][j][t] of x_A^i x_B^j (t <= i + j), one Cartesian direction
-template <int IM, int JM>
+template <int IM, int JM, typename R>
 struct Herm {
-    double e[IM + 1][JM + 1][IM + JM + 1];
+    R e[IM + 1][JM + 1][IM + JM + 1];
 };
 
-template <int IM, int JM>
-__device__ __forceinline__ void herm(double PA, double AB, double ohp, Herm<IM, JM> &E) {
-    const double PB = PA + AB;
-    E.e[0][0][0] = 1.0;
+template <int IM, int JM, typename R>
+__device__ __forceinline__ void herm(R PA, R AB, R ohp, Herm<IM, JM, R> &E) {
+    const R PB = PA + AB;
+    E.e[0][0][0] = R(1);
     sfor<IM + 1>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
         if constexpr (i > 0) {
             sfor<i + 1>([&](auto t_) {
                 constexpr int t = decltype(t_)::value;
-                double v = 0.0;
+                R v = R(0);
                 if constexpr (t <= i - 1) v = PA * E.e[i - 1][0][t];
-                if constexpr (t > 0) v = fma(ohp, E.e[i - 1][0][t - 1], v);
-                if constexpr (t + 1 <= i - 1) v = fma(double(t + 1), E.e[i - 1][0][t + 1], v);
+                if constexpr (t > 0) v = rchem_fma(ohp, E.e[i - 1][0][t - 1], v);
+                if constexpr (t + 1 <= i - 1) v = rchem_fma(R(t + 1), E.e[i - 1][0][t + 1], v);
                 E.e[i][0][t] = v;
             });
         }
@@ -69,10 +70,10 @@ __device__ __forceinline__ void herm(double PA, double AB, double ohp, Herm<IM, 
             constexpr int j = decltype(j_)::value + 1;
             sfor<i + j + 1>([&](auto t_) {
                 constexpr int t = decltype(t_)::value;
-                double v = 0.0;
+                R v = R(0);
                 if constexpr (t <= i + j - 1) v = PB * E.e[i][j - 1][t];
-                if constexpr (t > 0) v = fma(ohp, E.e[i][j - 1][t - 1], v);
-                if constexpr (t + 1 <= i + j - 1) v = fma(double(t + 1), E.e[i][j - 1][t + 1], v);
+                if constexpr (t > 0) v = rchem_fma(ohp, E.e[i][j - 1][t - 1], v);
+                if constexpr (t + 1 <= i + j - 1) v = rchem_fma(R(t + 1), E.e[i][j - 1][t + 1], v);
                 E.e[i][j][t] = v;
             });
         });
@@ -81,14 +82,15 @@ __device__ __forceinline__ void herm(double PA, double AB, double ohp, Herm<IM, 
 
 // Hermite Coulomb integrals R_{tuv}, t+u+v <= L, from pref * F_n(T) (F[0..L]):
 // R^n_000 = (-2 rho)^n F_n, R^n_{t+1,u,v} = t R^{n+1}_{t-1,u,v} + X R^{n+1}_{t,u,v} (and for u, v)
-template <int L>
-__device__ __forceinline__ void coulomb(double rho, double X, double Y, double Z, const double *F, double *R) {
-    double Rn[L + 2][nr(L)];
-    double pw[L + 1];
-    pw[0] = 1.0;
+template <int L, typename R>
+__device__ __forceinline__ void coulomb(R rho, R X, R Y, R Z, const R *F, R *Rt) {
+    R Rn[L + 2][nr(L)];
+    R pw[L + 1];
+    pw[0] = R(1);
+    const R m2r = R(-2) * rho;
     sfor<L>([&](auto n_) {
         constexpr int n = decltype(n_)::value + 1;
-        pw[n] = pw[n - 1] * (-2.0 * rho);
+        pw[n] = pw[n - 1] * m2r;
     });
     sfor<L + 1>([&](auto m_) {
         constexpr int n = L - decltype(m_)::value;
@@ -98,18 +100,18 @@ __device__ __forceinline__ void coulomb(double rho, double X, double Y, double Z
                 sfor<top + 1>([&](auto v_) {
                     constexpr int t = decltype(t_)::value, u = decltype(u_)::value, v = decltype(v_)::value;
                     if constexpr (t + u + v <= top) {
-                        double r;
+                        R r;
                         if constexpr (t + u + v == 0) {
                             r = pw[n] * F[n];
                         } else if constexpr (t > 0) {
                             r = X * Rn[n + 1][tuv(t - 1, u, v)];
-                            if constexpr (t > 1) r = fma(double(t - 1), Rn[n + 1][tuv(t - 2, u, v)], r);
+                            if constexpr (t > 1) r = rchem_fma(R(t - 1), Rn[n + 1][tuv(t - 2, u, v)], r);
                         } else if constexpr (u > 0) {
                             r = Y * Rn[n + 1][tuv(0, u - 1, v)];
-                            if constexpr (u > 1) r = fma(double(u - 1), Rn[n + 1][tuv(0, u - 2, v)], r);
+                            if constexpr (u > 1) r = rchem_fma(R(u - 1), Rn[n + 1][tuv(0, u - 2, v)], r);
                         } else {
                             r = Z * Rn[n + 1][tuv(0, 0, v - 1)];
-                            if constexpr (v > 1) r = fma(double(v - 1), Rn[n + 1][tuv(0, 0, v - 2)], r);
+                            if constexpr (v > 1) r = rchem_fma(R(v - 1), Rn[n + 1][tuv(0, 0, v - 2)], r);
                         }
                         Rn[n][tuv(t, u, v)] = r;
                     }
@@ -117,27 +119,27 @@ __device__ __forceinline__ void coulomb(double rho, double X, double Y, double Z
             });
         });
     });
-    sfor<nr(L)>([&](auto i_) { R[decltype(i_)::value] = Rn[0][decltype(i_)::value]; });
+    sfor<nr(L)>([&](auto i_) { Rt[decltype(i_)::value] = Rn[0][decltype(i_)::value]; });
 }
 
 // Z_{tuv} = sum_{t'u'v'} Ek_x[c][d][t'] Ek_y[..][u'] Ek_z[..][v'] R_{t+t',u+u',v+v'}, t+u+v <= BM
 // (the ket of components (cx,cy,cz),(dx,dy,dz) contracted with R; the sign (-1)^t' is in Ek)
-template <int BM, int CX, int CY, int CZ, int DX, int DY, int DZ, int IM, int JM>
-__device__ __forceinline__ void zvec(const Herm<IM, JM> *Ek, const double *R, double *Zo) {
+template <int BM, int CX, int CY, int CZ, int DX, int DY, int DZ, int IM, int JM, typename R>
+__device__ __forceinline__ void zvec(const Herm<IM, JM, R> *Ek, const R *Rt, R *Zo) {
     sfor<BM + 1>([&](auto t_) {
         sfor<BM + 1>([&](auto u_) {
             sfor<BM + 1>([&](auto v_) {
                 constexpr int t = decltype(t_)::value, u = decltype(u_)::value, v = decltype(v_)::value;
                 if constexpr (t + u + v <= BM) {
-                    double z = 0.0;
+                    R z = R(0);
                     sfor<CX + DX + 1>([&](auto a_) {
                         constexpr int a = decltype(a_)::value;
                         sfor<CY + DY + 1>([&](auto b_) {
                             constexpr int b = decltype(b_)::value;
-                            const double fxy = Ek[0].e[CX][DX][a] * Ek[1].e[CY][DY][b];
+                            const R fxy = Ek[0].e[CX][DX][a] * Ek[1].e[CY][DY][b];
                             sfor<CZ + DZ + 1>([&](auto c_) {
                                 constexpr int c = decltype(c_)::value;
-                                z = fma(fxy * Ek[2].e[CZ][DZ][c], R[tuv(t + a, u + b, v + c)], z);
+                                z = rchem_fma(fxy * Ek[2].e[CZ][DZ][c], Rt[tuv(t + a, u + b, v + c)], z);
                             });
                         });
                     });
@@ -149,17 +151,17 @@ __device__ __forceinline__ void zvec(const Herm<IM, JM> *Ek, const double *R, do
 }
 
 // sum_{tuv} Eb_x[ax][bx][t] Eb_y[ay][by][u] Eb_z[az][bz][v] Z_{tuv}
-template <int AX, int AY, int AZ, int BX, int BY, int BZ, int IM, int JM>
-__device__ __forceinline__ double dot(const Herm<IM, JM> *Eb, const double *Zv) {
-    double s = 0.0;
+template <int AX, int AY, int AZ, int BX, int BY, int BZ, int IM, int JM, typename R>
+__device__ __forceinline__ R dot(const Herm<IM, JM, R> *Eb, const R *Zv) {
+    R s = R(0);
     sfor<AX + BX + 1>([&](auto t_) {
         constexpr int t = decltype(t_)::value;
         sfor<AY + BY + 1>([&](auto u_) {
             constexpr int u = decltype(u_)::value;
-            const double exy = Eb[0].e[AX][BX][t] * Eb[1].e[AY][BY][u];
+            const R exy = Eb[0].e[AX][BX][t] * Eb[1].e[AY][BY][u];
             sfor<AZ + BZ + 1>([&](auto v_) {
                 constexpr int v = decltype(v_)::value;
-                s = fma(exy * Eb[2].e[AZ][BZ][v], Zv[tuv(t, u, v)], s);
+                s = rchem_fma(exy * Eb[2].e[AZ][BZ][v], Zv[tuv(t, u, v)], s);
             });
         });
     });
@@ -168,7 +170,48 @@ __device__ __forceinline__ double dot(const Herm<IM, JM> *Eb, const double *Zv) 
 
 }  // namespace gt
 
-template <int LA, int LB, int LC, int LD>
+// primitive pair in the kernel's arithmetic: p, 1/(2p), P, P-A, K and the
+// exponent on the pair's first shell (the derivative weight 2 alpha)
+template <typename R> struct GradPrim;
+template <> struct GradPrim<double> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, double &p, double &ohp, double *P, double *PA,
+                                               double &K, double &ea) {
+        const PairPrim q = g.prims[i];
+        p = q.p; ohp = q.ohp; K = q.K; ea = q.pad;
+        for (int d = 0; d < 3; ++d) { P[d] = q.P[d]; PA[d] = q.PA[d]; }
+    }
+    static __device__ __forceinline__ const double *boys(const GradArgs &g) { return g.boys64; }
+};
+template <> struct GradPrim<float> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, float &p, float &ohp, float *P, float *PA,
+                                               float &K, float &ea) {
+        const float4 *q = reinterpret_cast<const float4 *>(g.prims32 + i);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2);
+        p = v0.x; ohp = v0.y; P[0] = v0.z; P[1] = v0.w; P[2] = v1.x; PA[0] = v1.y; PA[1] = v1.z; PA[2] = v1.w;
+        K = v2.x; ea = v2.y;
+    }
+    static __device__ __forceinline__ const float *boys(const GradArgs &g) { return g.boys32; }
+};
+template <> struct GradPrim<df64> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, df64 &p, df64 &ohp, df64 *P, df64 *PA,
+                                               df64 &K, df64 &ea) {
+        const float4 *q = reinterpret_cast<const float4 *>(g.primsdf + i);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2), v3 = __ldg(q + 3), v4 = __ldg(q + 4);
+        p = df64(v0.x, v0.y); ohp = df64(v0.z, v0.w);
+        P[0] = df64(v1.x, v1.y); P[1] = df64(v1.z, v1.w); P[2] = df64(v2.x, v2.y);
+        PA[0] = df64(v2.z, v2.w); PA[1] = df64(v3.x, v3.y); PA[2] = df64(v3.z, v3.w);
+        K = df64(v4.x, v4.y); ea = df64(v4.z, v4.w);
+    }
+    static __device__ __forceinline__ const df64 *boys(const GradArgs &g) {
+        return reinterpret_cast<const df64 *>(g.boysdf);
+    }
+};
+
+__device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x; }
+__device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
+__device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
+
+template <int LA, int LB, int LC, int LD, typename R>
 __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
     using namespace gt;
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
@@ -194,8 +237,9 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
     if (bp.diag) deg *= 0.5;
     if (kp.diag) deg *= 0.5;
     if (seg.bra == seg.ket0 + off) deg *= 0.5;
-    // Gamma with the degeneracy and the component norms (l <= 1: all norms are 1)
-    double Gam[NC * ND * NA * NB];
+    // Gamma with the degeneracy and the component norms (l <= 1: all norms are 1),
+    // formed in FP64 and then rounded to the kernel's arithmetic
+    R Gam[NC * ND * NA * NB];
     sfor<NC>([&](auto kc_) {
         sfor<ND>([&](auto kd_) {
             constexpr int kc = decltype(kc_)::value, kd = decltype(kd_)::value;
@@ -205,32 +249,38 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
                 sfor<NB>([&](auto kb_) {
                     constexpr int ka = decltype(ka_)::value, kb = decltype(kb_)::value;
                     const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    Gam[((kc * ND + kd) * NA + ka) * NB + kb] =
+                    Gam[((kc * ND + kd) * NA + ka) * NB + kb] = gt_narrow(
                         deg * (2.0 * Dg[mu * n + nu] * Dls -
-                               0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                               0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
+                        (R *)nullptr);
                 });
             });
         });
     });
-    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+    R AB[3], CD[3];
+    Tabs<R>::ab(bp, AB);
+    Tabs<R>::ab(kp, CD);
+    const R *btab = GradPrim<R>::boys(g);
+    R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int nk = kp.npp, ntot = active ? bp.npp * nk : 0;  // idle lanes only join the reduction
     for (int tq = r; tq < ntot; tq += G) {
         const int ia = tq / nk, ic = tq - ia * nk;
-        const PairPrim pa = g.prims[bp.prim0 + ia];
-        const PairPrim pc = g.prims[kp.prim0 + ic];
-        const double aa = pa.pad, ab = pa.p - pa.pad, ac = pc.pad;  // pad: exponent on the first shell
-        const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
-        const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
-        const double T = rho * (X * X + Y * Y + Zc * Zc);
-        double F[L1 + 1], R[nr(L1)];
-        boys_eval<L1, double>(T, pa.K * pc.K * rs, g.boys64, F);
-        coulomb<L1>(rho, X, Y, Zc, F, R);
-        Herm<LA + 1, LB + 1> Eb[3];
-        Herm<LC + 1, LD> Ek[3];
+        R p, ohp, Pc[3], PA[3], Kab, aa, q, ohq, Qc[3], QC[3], Kcd, ac;
+        GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
+        GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
+        const R ab = p - aa;
+        const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+        const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
+        const R T = rho * (X * X + Y * Y + Zc * Zc);
+        R F[L1 + 1], Rt[nr(L1)];
+        boys_eval<L1, R>(T, Kab * Kcd * rs, btab, F);
+        coulomb<L1, R>(rho, X, Y, Zc, F, Rt);
+        Herm<LA + 1, LB + 1, R> Eb[3];
+        Herm<LC + 1, LD, R> Ek[3];
         sfor<3>([&](auto d_) {
             constexpr int d = decltype(d_)::value;
-            herm<LA + 1, LB + 1>(pa.PA[d], bp.AB[d], pa.ohp, Eb[d]);
-            herm<LC + 1, LD>(pc.PA[d], kp.AB[d], pc.ohp, Ek[d]);
+            herm<LA + 1, LB + 1, R>(PA[d], AB[d], ohp, Eb[d]);
+            herm<LC + 1, LD, R>(QC[d], CD[d], ohq, Ek[d]);
             sfor<LC + 2>([&](auto i_) {  // ket sign (-1)^t folded in
                 sfor<LD + 1>([&](auto j_) {
                     constexpr int i = decltype(i_)::value, j = decltype(j_)::value;
@@ -241,56 +291,57 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
                 });
             });
         });
+        const R a2 = aa + aa, b2 = ab + ab, c2 = ac + ac;
         sfor<NC>([&](auto kc_) {
             sfor<ND>([&](auto kd_) {
                 constexpr int kc = decltype(kc_)::value, kd = decltype(kd_)::value;
                 constexpr int cx = comp(LC, kc, 0), cy = comp(LC, kc, 1), cz = comp(LC, kc, 2);
                 constexpr int dx = comp(LD, kd, 0), dy = comp(LD, kd, 1), dz = comp(LD, kd, 2);
                 // ket contracted with R: unshifted (the bra may be shifted by one), C shifted by +-1
-                double Z0[nr(BM)], Zp[3][nr(BM - 1)], Zm[3][nr(BM - 1)];
-                zvec<BM, cx, cy, cz, dx, dy, dz>(Ek, R, Z0);
-                zvec<BM - 1, cx + 1, cy, cz, dx, dy, dz>(Ek, R, Zp[0]);
-                zvec<BM - 1, cx, cy + 1, cz, dx, dy, dz>(Ek, R, Zp[1]);
-                zvec<BM - 1, cx, cy, cz + 1, dx, dy, dz>(Ek, R, Zp[2]);
-                if constexpr (cx > 0) zvec<BM - 1, cx - 1, cy, cz, dx, dy, dz>(Ek, R, Zm[0]);
-                if constexpr (cy > 0) zvec<BM - 1, cx, cy - 1, cz, dx, dy, dz>(Ek, R, Zm[1]);
-                if constexpr (cz > 0) zvec<BM - 1, cx, cy, cz - 1, dx, dy, dz>(Ek, R, Zm[2]);
+                R Z0[nr(BM)], Zp[3][nr(BM - 1)], Zm[3][nr(BM - 1)];
+                zvec<BM, cx, cy, cz, dx, dy, dz>(Ek, Rt, Z0);
+                zvec<BM - 1, cx + 1, cy, cz, dx, dy, dz>(Ek, Rt, Zp[0]);
+                zvec<BM - 1, cx, cy + 1, cz, dx, dy, dz>(Ek, Rt, Zp[1]);
+                zvec<BM - 1, cx, cy, cz + 1, dx, dy, dz>(Ek, Rt, Zp[2]);
+                if constexpr (cx > 0) zvec<BM - 1, cx - 1, cy, cz, dx, dy, dz>(Ek, Rt, Zm[0]);
+                if constexpr (cy > 0) zvec<BM - 1, cx, cy - 1, cz, dx, dy, dz>(Ek, Rt, Zm[1]);
+                if constexpr (cz > 0) zvec<BM - 1, cx, cy, cz - 1, dx, dy, dz>(Ek, Rt, Zm[2]);
                 sfor<NA>([&](auto ka_) {
                     sfor<NB>([&](auto kb_) {
                         constexpr int ka = decltype(ka_)::value, kb = decltype(kb_)::value;
                         constexpr int ax = comp(LA, ka, 0), ay = comp(LA, ka, 1), az = comp(LA, ka, 2);
                         constexpr int bx = comp(LB, kb, 0), by = comp(LB, kb, 1), bz = comp(LB, kb, 2);
-                        const double Gm = Gam[((kc * ND + kd) * NA + ka) * NB + kb];
+                        const R Gm = Gam[((kc * ND + kd) * NA + ka) * NB + kb];
                         // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
-                        double vx = 2.0 * aa * dot<ax + 1, ay, az, bx, by, bz>(Eb, Z0);
-                        double vy = 2.0 * aa * dot<ax, ay + 1, az, bx, by, bz>(Eb, Z0);
-                        double vz = 2.0 * aa * dot<ax, ay, az + 1, bx, by, bz>(Eb, Z0);
-                        if constexpr (ax > 0) vx -= ax * dot<ax - 1, ay, az, bx, by, bz>(Eb, Z0);
-                        if constexpr (ay > 0) vy -= ay * dot<ax, ay - 1, az, bx, by, bz>(Eb, Z0);
-                        if constexpr (az > 0) vz -= az * dot<ax, ay, az - 1, bx, by, bz>(Eb, Z0);
-                        gA[0] = fma(Gm, vx, gA[0]);
-                        gA[1] = fma(Gm, vy, gA[1]);
-                        gA[2] = fma(Gm, vz, gA[2]);
+                        R vx = a2 * dot<ax + 1, ay, az, bx, by, bz>(Eb, Z0);
+                        R vy = a2 * dot<ax, ay + 1, az, bx, by, bz>(Eb, Z0);
+                        R vz = a2 * dot<ax, ay, az + 1, bx, by, bz>(Eb, Z0);
+                        if constexpr (ax > 0) vx = vx - R(ax) * dot<ax - 1, ay, az, bx, by, bz>(Eb, Z0);
+                        if constexpr (ay > 0) vy = vy - R(ay) * dot<ax, ay - 1, az, bx, by, bz>(Eb, Z0);
+                        if constexpr (az > 0) vz = vz - R(az) * dot<ax, ay, az - 1, bx, by, bz>(Eb, Z0);
+                        gA[0] = rchem_fma(Gm, vx, gA[0]);
+                        gA[1] = rchem_fma(Gm, vy, gA[1]);
+                        gA[2] = rchem_fma(Gm, vz, gA[2]);
                         // centre B
-                        vx = 2.0 * ab * dot<ax, ay, az, bx + 1, by, bz>(Eb, Z0);
-                        vy = 2.0 * ab * dot<ax, ay, az, bx, by + 1, bz>(Eb, Z0);
-                        vz = 2.0 * ab * dot<ax, ay, az, bx, by, bz + 1>(Eb, Z0);
-                        if constexpr (bx > 0) vx -= bx * dot<ax, ay, az, bx - 1, by, bz>(Eb, Z0);
-                        if constexpr (by > 0) vy -= by * dot<ax, ay, az, bx, by - 1, bz>(Eb, Z0);
-                        if constexpr (bz > 0) vz -= bz * dot<ax, ay, az, bx, by, bz - 1>(Eb, Z0);
-                        gB[0] = fma(Gm, vx, gB[0]);
-                        gB[1] = fma(Gm, vy, gB[1]);
-                        gB[2] = fma(Gm, vz, gB[2]);
+                        vx = b2 * dot<ax, ay, az, bx + 1, by, bz>(Eb, Z0);
+                        vy = b2 * dot<ax, ay, az, bx, by + 1, bz>(Eb, Z0);
+                        vz = b2 * dot<ax, ay, az, bx, by, bz + 1>(Eb, Z0);
+                        if constexpr (bx > 0) vx = vx - R(bx) * dot<ax, ay, az, bx - 1, by, bz>(Eb, Z0);
+                        if constexpr (by > 0) vy = vy - R(by) * dot<ax, ay, az, bx, by - 1, bz>(Eb, Z0);
+                        if constexpr (bz > 0) vz = vz - R(bz) * dot<ax, ay, az, bx, by, bz - 1>(Eb, Z0);
+                        gB[0] = rchem_fma(Gm, vx, gB[0]);
+                        gB[1] = rchem_fma(Gm, vy, gB[1]);
+                        gB[2] = rchem_fma(Gm, vz, gB[2]);
                         // centre C
-                        vx = 2.0 * ac * dot<ax, ay, az, bx, by, bz>(Eb, Zp[0]);
-                        vy = 2.0 * ac * dot<ax, ay, az, bx, by, bz>(Eb, Zp[1]);
-                        vz = 2.0 * ac * dot<ax, ay, az, bx, by, bz>(Eb, Zp[2]);
-                        if constexpr (cx > 0) vx -= cx * dot<ax, ay, az, bx, by, bz>(Eb, Zm[0]);
-                        if constexpr (cy > 0) vy -= cy * dot<ax, ay, az, bx, by, bz>(Eb, Zm[1]);
-                        if constexpr (cz > 0) vz -= cz * dot<ax, ay, az, bx, by, bz>(Eb, Zm[2]);
-                        gC[0] = fma(Gm, vx, gC[0]);
-                        gC[1] = fma(Gm, vy, gC[1]);
-                        gC[2] = fma(Gm, vz, gC[2]);
+                        vx = c2 * dot<ax, ay, az, bx, by, bz>(Eb, Zp[0]);
+                        vy = c2 * dot<ax, ay, az, bx, by, bz>(Eb, Zp[1]);
+                        vz = c2 * dot<ax, ay, az, bx, by, bz>(Eb, Zp[2]);
+                        if constexpr (cx > 0) vx = vx - R(cx) * dot<ax, ay, az, bx, by, bz>(Eb, Zm[0]);
+                        if constexpr (cy > 0) vy = vy - R(cy) * dot<ax, ay, az, bx, by, bz>(Eb, Zm[1]);
+                        if constexpr (cz > 0) vz = vz - R(cz) * dot<ax, ay, az, bx, by, bz>(Eb, Zm[2]);
+                        gC[0] = rchem_fma(Gm, vx, gC[0]);
+                        gC[1] = rchem_fma(Gm, vy, gC[1]);
+                        gC[2] = rchem_fma(Gm, vz, gC[2]);
                     });
                 });
             });
@@ -306,9 +357,10 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
     const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A],
               atD = g.shell_atom[kp.B];
     for (int x = 0; x < 3; ++x) {
-        atomicAdd(g.grad + 3 * atA + x, gA[x]);
-        atomicAdd(g.grad + 3 * atB + x, gB[x]);
-        atomicAdd(g.grad + 3 * atC + x, gC[x]);
-        atomicAdd(g.grad + 3 * atD + x, -(gA[x] + gB[x] + gC[x]));
+        const double a = widen(gA[x]), b = widen(gB[x]), c = widen(gC[x]);
+        atomicAdd(g.grad + 3 * atA + x, a);
+        atomicAdd(g.grad + 3 * atB + x, b);
+        atomicAdd(g.grad + 3 * atC + x, c);
+        atomicAdd(g.grad + 3 * atD + x, -(a + b + c));
     }
 }

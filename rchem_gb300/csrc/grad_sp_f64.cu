@@ -1,0 +1,6 @@
+// grad_sp_f64.cu -- the s/p gradient kernels in double arithmetic.
+#include "grad_sp_launch.cuh"
+
+bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st) {
+    return grad_sp_launch<double>(k, g, blocks, st);
+}

@@ -28,7 +28,6 @@
 #include "eigh.cuh"
 #include "eri_kernel.cuh"
 #include "grad.cuh"
-#include "grad_cls.cuh"
 #include "md.cuh"
 #include "rchem_types.h"
 
@@ -155,6 +154,12 @@ static int pair_cls(int la, int lb) {
     return t[la][lb];
 }
 static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
+// gradient work lists: (class, precision) pairs, then one list for every class with a d shell
+#define GRAD_NLIST (2 * RCHEM_NCLASS + 1)
+// the specialised s/p gradient kernels, one translation unit per arithmetic (grad_sp_*.cu)
+bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
@@ -365,8 +370,9 @@ struct rchem_basis_s {
     EriTask *d_gtasks = nullptr;  // the gradient's warp tasks (grouped by class) and segments
     EriSeg *d_gsegs = nullptr;
     long long gq_n = 0;
-    long long gtask_off[RCHEM_NCLASS + 1] = {}, gtask_cnt[RCHEM_NCLASS + 1] = {};
-    double gtask_cost[RCHEM_NCLASS + 1] = {};
+    long long gtask_off[GRAD_NLIST] = {}, gtask_cnt[GRAD_NLIST] = {};
+    double gtask_cost[GRAD_NLIST] = {};
+    double gq_tau32 = -1.0;
     double gq_tau = -1.0;
     double *d_W = nullptr, *d_grad = nullptr;
 };
@@ -587,7 +593,8 @@ static int build_pairs(rchem_basis b) {
             r.PA[d] = (float)q.PA[d];
         }
         r.K = (float)q.K;
-        r.pad[0] = r.pad[1] = r.pad[2] = 0.f;
+        r.pad[0] = (float)q.pad;  // exponent on the first shell (the gradient's weight)
+        r.pad[1] = r.pad[2] = 0.f;
     }
     std::vector<PairPrimDF> pdf(prims.size());
     auto split = [](double v, float *hl) {
@@ -604,7 +611,7 @@ static int build_pairs(rchem_basis b) {
             split(q.PA[d], r.PA[d]);
         }
         split(q.K, r.K);
-        r.pad[0] = r.pad[1] = 0.f;
+        split(q.pad, r.pad);  // exponent on the first shell
     }
     CKR(upload(&b->d_prims, prims, b->stream));
     CKR(upload(&b->d_prims32, p32, b->stream));
@@ -1143,11 +1150,12 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
 // (bra group, ket group) combination as segments, packed into warp tasks with
 // G lanes per quartet (at least kGradPrimPerLane primitive quartets per lane:
 // a derivative primitive quartet is ~100x a Fock one), heaviest tasks first.
-static int plan_gradient(rchem_basis b, double tau) {
-    if (b->d_gtasks && b->gq_tau == tau) return RCHEM_OK;
+static int plan_gradient(rchem_basis b, double tau, double tau32) {
+    if (b->d_gtasks && b->gq_tau == tau && b->gq_tau32 == tau32) return RCHEM_OK;
     constexpr long long kGradPrimPerLane = 2;
     std::vector<EriSeg> segs;
-    std::vector<EriTask> per_class[RCHEM_NCLASS + 1];
+    // lists: 2 k (+1 for FP32) for the s/p class k, GRAD_NLIST - 1 for every class with a d shell
+    std::vector<EriTask> per_class[GRAD_NLIST];
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
@@ -1156,34 +1164,39 @@ static int plan_gradient(rchem_basis b, double tau) {
             if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
             const long long nprimq = (long long)gb.npp * gk.npp;
             const int L = gb.la + gb.lb + gk.la + gk.lb;
-            const int s0 = (int)segs.size();
-            long long total = 0;
-            for (int ib = gb.begin; ib < gb.end; ++ib) {
-                const double Qb = P[ib].Q;
-                if (!(Qb > 0.0)) continue;
-                int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
-                if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
-                if (nk <= 0) continue;
-                segs.push_back(EriSeg{ib, gk.begin, nk, 0});
-                total += nk;
-            }
-            if (total == 0) continue;
-            // s/p classes each get their specialised kernel; every class with a d
-            // shell shares one launch of the run-time kernel (list RCHEM_NCLASS),
-            // whose lanes split primitive quartets x ket component pairs
+            // s/p classes get their specialised kernel in FP64 (or double-float) and, below
+            // tau32, FP32; every class with a d shell shares one FP64 launch of the
+            // run-time kernel, whose lanes split primitive quartets x ket component pairs
             const int k = quartet_kernel(gb.cls, gk.cls);
             const int *l = rchem_class_l[k];
-            const int list = (l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1) ? k : RCHEM_NCLASS;
-            const long long units = list == RCHEM_NCLASS ? nprimq * ncart(gk.la) * ncart(gk.lb) : nprimq;
+            const bool sp = l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1;
+            const long long units = sp ? nprimq : nprimq * ncart(gk.la) * ncart(gk.lb);
             int lg = 0;
             while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
             const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
-            pack_tasks(segs, s0, total, lg, ((units + (1 << lg) - 1) >> lg) * work, per_class[list]);
+            for (int prec = 0; prec < (sp ? 2 : 1); ++prec) {
+                const int s0 = (int)segs.size();
+                long long total = 0;
+                for (int ib = gb.begin; ib < gb.end; ++ib) {
+                    const double Qb = P[ib].Q;
+                    if (!(Qb > 0.0)) continue;
+                    int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
+                    if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
+                    const int m = (sp && tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
+                    const int lo = prec ? m : 0, hi = prec ? nk : m;
+                    if (hi <= lo) continue;
+                    segs.push_back(EriSeg{ib, gk.begin + lo, hi - lo, 0});
+                    total += hi - lo;
+                }
+                if (total == 0) continue;
+                pack_tasks(segs, s0, total, lg, ((units + (1 << lg) - 1) >> lg) * work,
+                           per_class[sp ? 2 * k + prec : GRAD_NLIST - 1]);
+            }
         }
     }
     // one launch per class (its specialised kernel), heaviest tasks first
     std::vector<EriTask> tasks;
-    for (int k = 0; k <= RCHEM_NCLASS; ++k) {
+    for (int k = 0; k < GRAD_NLIST; ++k) {
         std::vector<EriTask> &L = per_class[k];
         std::stable_sort(L.begin(), L.end(), [](const EriTask &x, const EriTask &y) { return x.cost > y.cost; });
         b->gtask_off[k] = (long long)tasks.size();
@@ -1202,6 +1215,7 @@ static int plan_gradient(rchem_basis b, double tau) {
     CK(cudaStreamSynchronize(b->stream));
     b->gq_n = (long long)tasks.size();
     b->gq_tau = tau;
+    b->gq_tau32 = tau32;
     return RCHEM_OK;
 }
 extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad,
@@ -1212,7 +1226,8 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
     if (opts) o = *opts;
     if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
-    CKR(plan_gradient(b, tau));
+    const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
+    CKR(plan_gradient(b, tau, tau32));
     const int na = b->natoms;
     const size_t nn = (size_t)b->packed;
     const cudaMemcpyKind in = o.where == RCHEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
@@ -1237,14 +1252,18 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         g.segs = b->d_gsegs;
         g.pairs = b->d_pairs;
         g.prims = b->d_prims;
+        g.prims32 = b->d_prims32;
+        g.primsdf = b->d_primsdf;
         g.shell_atom = b->d_shell_atom;
         g.shell_l = b->d_shell_l;
         g.boys64 = b->tabs->boys64;
+        g.boys32 = b->tabs->boys32;
+        g.boysdf = b->tabs->boysdf;
         g.D = b->d_D;
         g.grad = b->d_grad;
         // classes run concurrently: longest first, each onto the least-loaded stream
         std::vector<int> ks;
-        for (int k = 0; k <= RCHEM_NCLASS; ++k)
+        for (int k = 0; k < GRAD_NLIST; ++k)
             if (b->gtask_cnt[k] > 0) ks.push_back(k);
         std::stable_sort(ks.begin(), ks.end(), [&](int x, int y) { return b->gtask_cost[x] > b->gtask_cost[y]; });
         const int nuse = std::min<int>((int)ks.size(), rchem_basis_s::NAUX);
@@ -1260,20 +1279,15 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             g.tasks = b->d_gtasks + b->gtask_off[k];
             g.ntasks = (int)b->gtask_cnt[k];
             const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
-            const int *l = rchem_class_l[k < RCHEM_NCLASS ? k : RCHEM_NCLASS - 1];
-#define RCHEM_GRAD_CLS(a_, b_, c_, d_)                                                  \
-    if (k < RCHEM_NCLASS && l[0] == a_ && l[1] == b_ && l[2] == c_ && l[3] == d_) {                          \
-        k_grad2e_cls<a_, b_, c_, d_><<<blocks, 64, 0, st>>>(g);                         \
-        CK(cudaGetLastError());                                                          \
-        continue;                                                                        \
-    }
-            RCHEM_GRAD_CLS(0, 0, 0, 0)
-            RCHEM_GRAD_CLS(1, 0, 0, 0)
-            RCHEM_GRAD_CLS(1, 0, 1, 0)
-            RCHEM_GRAD_CLS(1, 1, 0, 0)
-            RCHEM_GRAD_CLS(1, 1, 1, 0)
-            RCHEM_GRAD_CLS(1, 1, 1, 1)
-#undef RCHEM_GRAD_CLS
+            if (k < GRAD_NLIST - 1) {  // an s/p class: its specialised kernel
+                const int cls = k / 2;
+                const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
+                                        : (o.emulated ? rchem_grad_sp_df64(cls, g, blocks, st)
+                                                      : rchem_grad_sp_f64(cls, g, blocks, st));
+                if (!ok) return set_err(RCHEM_ERR_UNSUPPORTED, "gradient list %d has no specialised kernel", k);
+                CK(cudaGetLastError());
+                continue;
+            }
             k_grad2e<<<blocks, 64, 0, st>>>(g);  // classes with d shells: run-time angular momenta
             CK(cudaGetLastError());
         }

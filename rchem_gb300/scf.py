@@ -110,11 +110,14 @@ def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thres
             "F": F, "H": H, "S": S, "iterations": it, "converged": converged, "history": hist}
 
 
-def gradient(basis: _b.Basis, res: dict | None = None, schwarz_tau: float = 1e-12, **scf_kw):
+def gradient(basis: _b.Basis, res: dict | None = None, schwarz_tau: float = 1e-12, fp32_tau: float = 0.0,
+             emulated: bool = False, **scf_kw):
     """Nuclear gradient dE/dR (natoms x 3, hartree/bohr) of the converged RHF
     energy, from the adjoint kernels of librchem_gpu.so (rchem_gradient): the
     derivative integrals are contracted on the GPU with D and W = sum_i eps_i
-    C_i C_i^T and never stored.  Runs the SCF first when ``res`` is None."""
+    C_i C_i^T and never stored.  ``fp32_tau`` > 0 computes the s/p quartets
+    whose Schwarz product is below it in FP32; ``emulated`` the other s/p
+    quartets in double-float arithmetic.  Runs the SCF first when ``res`` is None."""
     import ctypes as C
 
     import torch
@@ -126,7 +129,8 @@ def gradient(basis: _b.Basis, res: dict | None = None, schwarz_tau: float = 1e-1
     D = res["D"].contiguous()
     W = res["W"].contiguous()
     g = torch.empty(3 * len(basis.atomnos), dtype=torch.float64, device=D.device)
-    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=0.0, where=_lib.DEVICE)
+    o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
+                    emulated=1 if emulated else 0)
     _b._after_torch(basis, D, W, g)
     _lib.check(_lib.lib().rchem_gradient(basis.handle, C.c_void_p(D.data_ptr()), C.c_void_p(W.data_ptr()),
                                          C.c_void_p(g.data_ptr()), C.byref(o)))

@@ -98,3 +98,17 @@ def test_eigh_batched_rejects_large_n(gpu):
 
     with pytest.raises(rc.RchemError):
         rc.batch.eigh(torch.zeros((2, 65, 65), dtype=torch.float64, device="cuda"))
+
+
+def test_batched_gradient_precision_forms(gpu):
+    """Batched gradients in the emulated and mixed forms against FP64."""
+    import rchem_gb300 as rc
+
+    bb = rc.batch.BatchBasis(_geoms(6, seed=8), "6-31g-fit")
+    res = rc.batch.rhf_batch(bb, thresh_e=1e-11, thresh_d=1e-8)
+    g64 = np.concatenate(rc.batch.gradient_batch(bb, res))
+    gem = np.concatenate(rc.batch.gradient_batch(bb, res, emulated=True))
+    gmx = np.concatenate(rc.batch.gradient_batch(bb, res, fp32_tau=1e-6, emulated=True))
+    assert np.abs(gem - g64).max() < 1e-10
+    assert np.abs(gmx - g64).max() < 1e-7
+    bb.close()

@@ -93,3 +93,23 @@ def test_gradient_h2o4_631gss_fd(gpu):
     bname, Z, R = rc.geometry.config("h2o4_631gss")
     g, worst = _fd_check(Z, R, bname)
     assert np.abs(g.reshape(-1, 3).sum(axis=0)).max() < 1e-8
+
+
+def test_gradient_precision_forms_h2o4(gpu):
+    """The same converged density through the FP32 (fp32_tau = 1e-6) and
+    double-float forms of the gradient kernels: the emulated form within 1e-10
+    of FP64, the mixed forms well inside the 1e-6 Eh/bohr finite-difference
+    tolerance; every form keeps translational invariance."""
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o4_631gss")
+    with rc.Basis(Z, R, bname) as b:
+        res = rc.scf.rhf(b, thresh_e=1e-12, thresh_d=1e-9)
+        g64 = rc.scf.gradient(b, res)
+        forms = {"emulated": rc.scf.gradient(b, res, emulated=True),
+                 "mixed": rc.scf.gradient(b, res, fp32_tau=1e-6),
+                 "emulated_mixed": rc.scf.gradient(b, res, fp32_tau=1e-6, emulated=True)}
+    tol = {"emulated": 1e-10, "mixed": 1e-7, "emulated_mixed": 1e-7}
+    for k, g in forms.items():
+        assert float((g - g64).abs().max()) < tol[k], (k, float((g - g64).abs().max()))
+        assert float(g.sum(dim=0).abs().max()) < 1e-8, k
