@@ -160,9 +160,9 @@ int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K
  * kernels: derivative ERIs contracted on the fly with the density products,
  * derivative S/T/V contracted with W and D, Hellmann-Feynman term included.
  * No counterpart in the reference, which has no gradients.  opts: schwarz_tau,
- * where (for D, W and grad), fp32_tau (s/p quartets with Q_ab Q_cd below it in
- * FP32, the rest FP64; quartets with a d shell always FP64) and emulated (the
- * FP64 s/p quartets in double-float arithmetic on the FP32 pipe).
+ * where (for D, W and grad), fp32_tau (quartets with Q_ab Q_cd below it in
+ * FP32, the rest FP64) and emulated (the FP64 quartets in double-float
+ * arithmetic on the FP32 pipe).
  */
 int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
 

@@ -149,7 +149,7 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
 // Runtime-L variant for the generic (non-class) kernels; L <= BOYS_MMAX.
 template <typename R>
 RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab, R *F) {
-    if (T < R(BOYS_TMAX)) {
+    if (rchem_lt(T, R(BOYS_TMAX))) {
         int i;
         R x;
         boys_grid(T, i, x);
@@ -157,7 +157,7 @@ RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab,
     } else {
         const R rs = rchem_rsqrt(T);
         const R inv2T = R(0.5) * rs * rs;
-        const R ex = R(rchem_expf(-(float)T)) * pref;
+        const R ex = R(rchem_expf(-rchem_tofloat(T))) * pref;
         F[0] = R(0.88622692545275801365) * rs * pref;
         for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;
     }

@@ -15,6 +15,7 @@
 // invariance gives the fourth centre).
 #pragma once
 #include "boys.cuh"
+#include "df64.cuh"
 #include "md.cuh"
 #include "rchem_types.h"
 
@@ -41,53 +42,54 @@ struct GradArgs {
 };
 
 // E[i][j][t] of x_A^i x_B^j for i <= imax, j <= jmax (no exponential factor)
-__device__ __forceinline__ void gr_herm(int imax, int jmax, double PA, double AB, double ohp,
-                                        double (*E)[GR_NI][GR_NT]) {
-    const double PB = PA + AB;  // P - B = (P - A) + (A - B)
+template <typename R>
+__device__ __forceinline__ void gr_herm(int imax, int jmax, R PA, R AB, R ohp, R (*E)[GR_NI][GR_NT]) {
+    const R PB = PA + AB;  // P - B = (P - A) + (A - B)
     for (int i = 0; i <= imax; ++i)
         for (int j = 0; j <= jmax; ++j)
-            for (int t = 0; t < GR_NT; ++t) E[i][j][t] = 0.0;
-    E[0][0][0] = 1.0;
+            for (int t = 0; t < GR_NT; ++t) E[i][j][t] = R(0);
+    E[0][0][0] = R(1);
     for (int i = 0; i <= imax; ++i) {
         if (i > 0)
             for (int t = 0; t <= i; ++t) {
-                double v = PA * E[i - 1][0][t];
-                if (t > 0) v += ohp * E[i - 1][0][t - 1];
-                if (t + 1 <= i - 1) v += (t + 1) * E[i - 1][0][t + 1];
+                R v = PA * E[i - 1][0][t];
+                if (t > 0) v = rchem_fma(ohp, E[i - 1][0][t - 1], v);
+                if (t + 1 <= i - 1) v = rchem_fma(R(t + 1), E[i - 1][0][t + 1], v);
                 E[i][0][t] = v;
             }
         for (int j = 1; j <= jmax; ++j)
             for (int t = 0; t <= i + j; ++t) {
-                double v = PB * E[i][j - 1][t];
-                if (t > 0) v += ohp * E[i][j - 1][t - 1];
-                if (t + 1 <= i + j - 1) v += (t + 1) * E[i][j - 1][t + 1];
+                R v = PB * E[i][j - 1][t];
+                if (t > 0) v = rchem_fma(ohp, E[i][j - 1][t - 1], v);
+                if (t + 1 <= i + j - 1) v = rchem_fma(R(t + 1), E[i][j - 1][t + 1], v);
                 E[i][j][t] = v;
             }
     }
 }
 
-__device__ __forceinline__ void gr_R(int L, double a, double X, double Y, double Z, const double *F, double *out) {
-    double buf[2][GR_NR];
-    double *cur = buf[0], *nxt = buf[1];
-    const double m2a = -2.0 * a;
-    double pw = 1.0;
-    for (int n = 0; n < L; ++n) pw *= m2a;
-    cur[0] = pw * F[L];
+template <typename R>
+__device__ __forceinline__ void gr_R(int L, R a, R X, R Y, R Z, const R *F, R *out) {
+    R buf[2][GR_NR];
+    R *cur = buf[0], *nxt = buf[1];
+    const R m2a = R(-2) * a;
+    R pw[GR_LMAX + 1];
+    pw[0] = R(1);
+    for (int n = 1; n <= L; ++n) pw[n] = pw[n - 1] * m2a;
+    cur[0] = pw[L] * F[L];
     for (int n = L - 1; n >= 0; --n) {
-        pw /= m2a;
         const int top = L - n;
         for (int N = 0; N <= top; ++N)
             for (int t = N; t >= 0; --t)
                 for (int u = N - t; u >= 0; --u) {
                     const int v = N - t - u;
-                    double r;
-                    if (N == 0) r = pw * F[n];
-                    else if (t > 0) r = X * cur[md_tuv(t - 1, u, v)] + (t > 1 ? (t - 1) * cur[md_tuv(t - 2, u, v)] : 0.0);
-                    else if (u > 0) r = Y * cur[md_tuv(0, u - 1, v)] + (u > 1 ? (u - 1) * cur[md_tuv(0, u - 2, v)] : 0.0);
-                    else r = Z * cur[md_tuv(0, 0, v - 1)] + (v > 1 ? (v - 1) * cur[md_tuv(0, 0, v - 2)] : 0.0);
+                    R r;
+                    if (N == 0) r = pw[n] * F[n];
+                    else if (t > 0) r = X * cur[md_tuv(t - 1, u, v)] + (t > 1 ? R(t - 1) * cur[md_tuv(t - 2, u, v)] : R(0));
+                    else if (u > 0) r = Y * cur[md_tuv(0, u - 1, v)] + (u > 1 ? R(u - 1) * cur[md_tuv(0, u - 2, v)] : R(0));
+                    else r = Z * cur[md_tuv(0, 0, v - 1)] + (v > 1 ? R(v - 1) * cur[md_tuv(0, 0, v - 2)] : R(0));
                     nxt[md_tuv(t, u, v)] = r;
                 }
-        double *tmp = cur;
+        R *tmp = cur;
         cur = nxt;
         nxt = tmp;
     }
@@ -116,19 +118,20 @@ __device__ __forceinline__ double gr_cnorm(const int *p) {
 // Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
 // Hermite index with t+u+v <= bmax (box of side zd): the ket of one component
 // contracted with the Coulomb integrals once, reused by every bra component.
-__device__ __forceinline__ void gr_zvec(const double (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d,
-                                        const double *R, int zd, int bmax, double *Z) {
+template <typename T>
+__device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
+                                        int zd, int bmax, T *Z) {
     for (int t = 0; t < zd; ++t)
         for (int u = 0; u < zd; ++u)
             for (int v = 0; v < zd; ++v) {
-                double z = 0.0;
+                T z = T(0);
                 if (t + u + v <= bmax)
                     for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
-                        const double fx = Ek[0][c[0]][d[0]][tt];
+                        const T fx = Ek[0][c[0]][d[0]][tt];
                         for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
-                            const double fy = fx * Ek[1][c[1]][d[1]][uu];
+                            const T fy = fx * Ek[1][c[1]][d[1]][uu];
                             for (int vv = 0; vv <= c[2] + d[2]; ++vv)
-                                z += fy * Ek[2][c[2]][d[2]][vv] * R[md_tuv(t + tt, u + uu, v + vv)];
+                                z = rchem_fma(fy * Ek[2][c[2]][d[2]][vv], R[md_tuv(t + tt, u + uu, v + vv)], z);
                         }
                     }
                 Z[(t * zd + u) * zd + v] = z;
@@ -136,32 +139,75 @@ __device__ __forceinline__ void gr_zvec(const double (*Ek)[GR_NI][GR_NI][GR_NT],
 }
 
 // sum_{tuv} E^{ab}_{tuv} Z_{tuv}
-__device__ __forceinline__ double gr_dot(const double (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b,
-                                         const double *Z, int zd) {
-    double s = 0.0;
+template <typename R>
+__device__ __forceinline__ R gr_dot(const R (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b, const R *Z,
+                                    int zd) {
+    R s = R(0);
     for (int t = 0; t <= a[0] + b[0]; ++t) {
-        const double ex = Eb[0][a[0]][b[0]][t];
+        const R ex = Eb[0][a[0]][b[0]][t];
         for (int u = 0; u <= a[1] + b[1]; ++u) {
-            const double ey = ex * Eb[1][a[1]][b[1]][u];
-            const double *Zr = Z + (t * zd + u) * zd;
-            for (int v = 0; v <= a[2] + b[2]; ++v) s += ey * Eb[2][a[2]][b[2]][v] * Zr[v];
+            const R ey = ex * Eb[1][a[1]][b[1]][u];
+            const R *Zr = Z + (t * zd + u) * zd;
+            for (int v = 0; v <= a[2] + b[2]; ++v) s = rchem_fma(ey * Eb[2][a[2]][b[2]][v], Zr[v], s);
         }
     }
     return s;
 }
+
+// primitive pair in the kernel's arithmetic: p, 1/(2p), P, P-A, K and the
+// exponent on the pair's first shell (the derivative weight 2 alpha)
+template <typename R> struct GradPrim;
+template <> struct GradPrim<double> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, double &p, double &ohp, double *P, double *PA,
+                                               double &K, double &ea) {
+        const PairPrim q = g.prims[i];
+        p = q.p; ohp = q.ohp; K = q.K; ea = q.pad;
+        for (int d = 0; d < 3; ++d) { P[d] = q.P[d]; PA[d] = q.PA[d]; }
+    }
+    static __device__ __forceinline__ const double *boys(const GradArgs &g) { return g.boys64; }
+};
+template <> struct GradPrim<float> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, float &p, float &ohp, float *P, float *PA,
+                                               float &K, float &ea) {
+        const float4 *q = reinterpret_cast<const float4 *>(g.prims32 + i);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2);
+        p = v0.x; ohp = v0.y; P[0] = v0.z; P[1] = v0.w; P[2] = v1.x; PA[0] = v1.y; PA[1] = v1.z; PA[2] = v1.w;
+        K = v2.x; ea = v2.y;
+    }
+    static __device__ __forceinline__ const float *boys(const GradArgs &g) { return g.boys32; }
+};
+template <> struct GradPrim<df64> {
+    static __device__ __forceinline__ void get(const GradArgs &g, int i, df64 &p, df64 &ohp, df64 *P, df64 *PA,
+                                               df64 &K, df64 &ea) {
+        const float4 *q = reinterpret_cast<const float4 *>(g.primsdf + i);
+        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2), v3 = __ldg(q + 3), v4 = __ldg(q + 4);
+        p = df64(v0.x, v0.y); ohp = df64(v0.z, v0.w);
+        P[0] = df64(v1.x, v1.y); P[1] = df64(v1.z, v1.w); P[2] = df64(v2.x, v2.y);
+        PA[0] = df64(v2.z, v2.w); PA[1] = df64(v3.x, v3.y); PA[2] = df64(v3.z, v3.w);
+        K = df64(v4.x, v4.y); ea = df64(v4.z, v4.w);
+    }
+    static __device__ __forceinline__ const df64 *boys(const GradArgs &g) {
+        return reinterpret_cast<const df64 *>(g.boysdf);
+    }
+};
+
+__device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x; }
+__device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
+__device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
 
 #define GR_ZD 6                           // bra Hermite box side: la+lb+2 <= 6
 #define GR_ZN (GR_ZD * GR_ZD * GR_ZD)
 
 #define GR_MAXC4 1296  // components of a (dd|dd) quartet
 
-#ifndef RCHEM_GRAD_NO_KERNELS  // translation units that only need the shared helpers
 // One warp task: up to 32 >> lg unique shell quartets, G = 2^lg lanes each
-// (the segment/task layout of the Fock build).  The G lanes split the
-// quartet's primitive quartets; Gamma (degeneracy and component norms folded
-// in) is formed once per quartet; the 9 centre derivatives are reduced over
-// the G lanes with warp shuffles and added to the gradient by one lane.
-__global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
+// (the segment/task layout of the Fock build).  Run-time angular momenta (the
+// classes with a d shell).  The G lanes split (primitive quartet, ket component
+// pair) units; Gamma (degeneracy and component norms folded in) is formed once
+// per quartet in FP64 and rounded to R; the 9 centre derivatives are reduced
+// over the G lanes with warp shuffles and added to the gradient by one lane.
+template <typename R>
+__global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     const int lane = threadIdx.x & 31;
     const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
     if (w >= g.ntasks) return;  // warp-uniform
@@ -205,48 +251,54 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
         gr_comp(ld, k, cD[k]);
         nD[k] = gr_cnorm(cD[k]);
     }
-    double Gam[GR_MAXC4];
+    R Gam[GR_MAXC4];
     for (int kc = 0; kc < nc; ++kc)
         for (int kd = 0; kd < nd; ++kd) {
             const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
             for (int ka = 0; ka < na; ++ka)
                 for (int kb = 0; kb < nb; ++kb) {
                     const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    Gam[((kc * nd + kd) * na + ka) * nb + kb] =
+                    Gam[((kc * nd + kd) * na + ka) * nb + kb] = gt_narrow(
                         deg * nA[ka] * nB[kb] * nC[kc] * nD[kd] *
-                        (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
-                         0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                            (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
+                             0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
+                        (R *)nullptr);
                 }
         }
-    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+    R AB[3], CD[3];
+    Tabs<R>::ab(bp, AB);
+    Tabs<R>::ab(kp, CD);
+    const R *btab = GradPrim<R>::boys(g);
+    R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int L1 = la + lb + lc + ld + 1;
     const int zd = la + lb + 2;
-    double Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], R[GR_NR], F[GR_LMAX + 1];
-    double Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
+    R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
+    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
     // work units: (primitive quartet, ket component pair); the G lanes split them
     // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
     const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
     const int nunits = active ? ntot * ncd : 0;  // idle lanes only join the reduction
     int cur = -1;
-    double aa = 0.0, ab = 0.0, ac = 0.0;
+    R a2 = R(0), b2 = R(0), c2 = R(0);
     for (int u = r; u < nunits; u += G) {
         const int tq = u / ncd, kcd = u - tq * ncd;
         if (tq != cur) {  // primitive-quartet tables, kept while the lane stays on it
             cur = tq;
             const int ia = tq / nk, ic = tq - ia * nk;
-            const PairPrim pa = g.prims[bp.prim0 + ia];
-            const PairPrim pc = g.prims[kp.prim0 + ic];
-            aa = pa.pad;  // pad holds the exponent on the first shell
-            ab = pa.p - pa.pad;
-            ac = pc.pad;
-            const double pq = pa.p + pc.p, rs = rsqrt(pq), ipq = rs * rs, rho = pa.p * pc.p * ipq;
-            const double X = pa.P[0] - pc.P[0], Y = pa.P[1] - pc.P[1], Zc = pa.P[2] - pc.P[2];
-            const double T = rho * (X * X + Y * Y + Zc * Zc);
-            boys_eval_rt<double>(L1, T, pa.K * pc.K * rs, g.boys64, F);
-            gr_R(L1, rho, X, Y, Zc, F, R);
+            R p, ohp, Pc[3], PA[3], Kab, aa, q, ohq, Qc[3], QC[3], Kcd, ac;
+            GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
+            GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
+            a2 = aa + aa;
+            b2 = (p - aa) + (p - aa);
+            c2 = ac + ac;
+            const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+            const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
+            const R T = rho * (X * X + Y * Y + Zc * Zc);
+            boys_eval_rt<R>(L1, T, Kab * Kcd * rs, btab, F);
+            gr_R<R>(L1, rho, X, Y, Zc, F, Rt);
             for (int dd = 0; dd < 3; ++dd) {
-                gr_herm(la + 1, lb + 1, pa.PA[dd], bp.AB[dd], pa.ohp, Eb[dd]);
-                gr_herm(lc + 1, ld, pc.PA[dd], kp.AB[dd], pc.ohp, Ek[dd]);
+                gr_herm<R>(la + 1, lb + 1, PA[dd], AB[dd], ohp, Eb[dd]);
+                gr_herm<R>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
                 for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
                     for (int j = 0; j <= ld; ++j)
                         for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
@@ -254,25 +306,24 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
         }
         int s[3];
         const int kc = kcd / nd, kd = kcd - kc * nd;
-        const double *Gq = Gam + (kc * nd + kd) * na * nb;
+        const R *Gq = Gam + (kc * nd + kd) * na * nb;
         // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
-        gr_zvec(Ek, cC[kc], cD[kd], R, zd, la + lb + 1, Z0);
+        gr_zvec<R>(Ek, cC[kc], cD[kd], Rt, zd, la + lb + 1, Z0);
         for (int x = 0; x < 3; ++x) {
             s[0] = cC[kc][0];
             s[1] = cC[kc][1];
             s[2] = cC[kc][2];
             s[x] += 1;
-            gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zp[x]);
+            gr_zvec<R>(Ek, s, cD[kd], Rt, zd, la + lb, Zp[x]);
             if (cC[kc][x] > 0) {
                 s[x] -= 2;
-                gr_zvec(Ek, s, cD[kd], R, zd, la + lb, Zm[x]);
+                gr_zvec<R>(Ek, s, cD[kd], Rt, zd, la + lb, Zm[x]);
             }
         }
         for (int ka = 0; ka < na; ++ka) {
             const int *A = cA[ka];
             for (int kb = 0; kb < nb; ++kb) {
-                const double Gm = Gq[ka * nb + kb];
-                if (Gm == 0.0) continue;
+                const R Gm = Gq[ka * nb + kb];
                 const int *B = cB[kb];
                 for (int x = 0; x < 3; ++x) {
                     // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
@@ -280,27 +331,27 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
                     s[1] = A[1];
                     s[2] = A[2];
                     s[x] += 1;
-                    double v = 2.0 * aa * gr_dot(Eb, s, B, Z0, zd);
+                    R v = a2 * gr_dot<R>(Eb, s, B, Z0, zd);
                     if (A[x] > 0) {
                         s[x] -= 2;
-                        v -= A[x] * gr_dot(Eb, s, B, Z0, zd);
+                        v = v - R(A[x]) * gr_dot<R>(Eb, s, B, Z0, zd);
                     }
-                    gA[x] += Gm * v;
+                    gA[x] = rchem_fma(Gm, v, gA[x]);
                     // centre B
                     s[0] = B[0];
                     s[1] = B[1];
                     s[2] = B[2];
                     s[x] += 1;
-                    v = 2.0 * ab * gr_dot(Eb, A, s, Z0, zd);
+                    v = b2 * gr_dot<R>(Eb, A, s, Z0, zd);
                     if (B[x] > 0) {
                         s[x] -= 2;
-                        v -= B[x] * gr_dot(Eb, A, s, Z0, zd);
+                        v = v - R(B[x]) * gr_dot<R>(Eb, A, s, Z0, zd);
                     }
-                    gB[x] += Gm * v;
+                    gB[x] = rchem_fma(Gm, v, gB[x]);
                     // centre C
-                    v = 2.0 * ac * gr_dot(Eb, A, B, Zp[x], zd);
-                    if (cC[kc][x] > 0) v -= cC[kc][x] * gr_dot(Eb, A, B, Zm[x], zd);
-                    gC[x] += Gm * v;
+                    v = c2 * gr_dot<R>(Eb, A, B, Zp[x], zd);
+                    if (cC[kc][x] > 0) v = v - R(cC[kc][x]) * gr_dot<R>(Eb, A, B, Zm[x], zd);
+                    gC[x] = rchem_fma(Gm, v, gC[x]);
                 }
             }
         }
@@ -315,13 +366,13 @@ __global__ void __launch_bounds__(64) k_grad2e(GradArgs g) {
     const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A],
               atD = g.shell_atom[kp.B];
     for (int x = 0; x < 3; ++x) {
-        atomicAdd(g.grad + 3 * atA + x, gA[x]);
-        atomicAdd(g.grad + 3 * atB + x, gB[x]);
-        atomicAdd(g.grad + 3 * atC + x, gC[x]);
-        atomicAdd(g.grad + 3 * atD + x, -(gA[x] + gB[x] + gC[x]));
+        const double a = widen(gA[x]), b = widen(gB[x]), c = widen(gC[x]);
+        atomicAdd(g.grad + 3 * atA + x, a);
+        atomicAdd(g.grad + 3 * atB + x, b);
+        atomicAdd(g.grad + 3 * atC + x, c);
+        atomicAdd(g.grad + 3 * atD + x, -(a + b + c));
     }
 }
-#endif
 
 // One-electron part, one thread per ordered function pair (mu, nu) of a geometry:
 //   4 D_mn d_mu H_mn - 4 W_mn d_mu S_mn on the atom of mu,
@@ -423,7 +474,7 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
                 P[d] = (ea * sa.R[d] + eb * sb.R[d]) / p;
                 PA[d] = P[d] - sa.R[d];
                 gr_s1d(a.lmn[d] + 1, b.lmn[d] + 2, PA[d], P[d] - sb.R[d], ohp, p, S1[d]);
-                gr_herm(a.lmn[d] + 1, b.lmn[d], PA[d], AB[d], ohp, E[d]);
+                gr_herm<double>(a.lmn[d] + 1, b.lmn[d], PA[d], AB[d], ohp, E[d]);
             }
             // overlap and kinetic of the unshifted and shifted components
             double s0[3], t0[3];
@@ -450,7 +501,7 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
                 const double X = P[0] - Ratoms[3 * cn], Y = P[1] - Ratoms[3 * cn + 1], Zc = P[2] - Ratoms[3 * cn + 2];
                 double F[GR_LMAX + 1], R[GR_NR];
                 boys_eval_rt<double>(L1, p * (X * X + Y * Y + Zc * Zc), 1.0, boys, F);
-                gr_R(L1, p, X, Y, Zc, F, R);
+                gr_R<double>(L1, p, X, Y, Zc, F, R);
                 int s[3];
                 double v3[3];
                 for (int x = 0; x < 3; ++x) {

@@ -170,47 +170,6 @@ __device__ __forceinline__ R dot(const Herm<IM, JM, R> *Eb, const R *Zv) {
 
 }  // namespace gt
 
-// primitive pair in the kernel's arithmetic: p, 1/(2p), P, P-A, K and the
-// exponent on the pair's first shell (the derivative weight 2 alpha)
-template <typename R> struct GradPrim;
-template <> struct GradPrim<double> {
-    static __device__ __forceinline__ void get(const GradArgs &g, int i, double &p, double &ohp, double *P, double *PA,
-                                               double &K, double &ea) {
-        const PairPrim q = g.prims[i];
-        p = q.p; ohp = q.ohp; K = q.K; ea = q.pad;
-        for (int d = 0; d < 3; ++d) { P[d] = q.P[d]; PA[d] = q.PA[d]; }
-    }
-    static __device__ __forceinline__ const double *boys(const GradArgs &g) { return g.boys64; }
-};
-template <> struct GradPrim<float> {
-    static __device__ __forceinline__ void get(const GradArgs &g, int i, float &p, float &ohp, float *P, float *PA,
-                                               float &K, float &ea) {
-        const float4 *q = reinterpret_cast<const float4 *>(g.prims32 + i);
-        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2);
-        p = v0.x; ohp = v0.y; P[0] = v0.z; P[1] = v0.w; P[2] = v1.x; PA[0] = v1.y; PA[1] = v1.z; PA[2] = v1.w;
-        K = v2.x; ea = v2.y;
-    }
-    static __device__ __forceinline__ const float *boys(const GradArgs &g) { return g.boys32; }
-};
-template <> struct GradPrim<df64> {
-    static __device__ __forceinline__ void get(const GradArgs &g, int i, df64 &p, df64 &ohp, df64 *P, df64 *PA,
-                                               df64 &K, df64 &ea) {
-        const float4 *q = reinterpret_cast<const float4 *>(g.primsdf + i);
-        const float4 v0 = __ldg(q), v1 = __ldg(q + 1), v2 = __ldg(q + 2), v3 = __ldg(q + 3), v4 = __ldg(q + 4);
-        p = df64(v0.x, v0.y); ohp = df64(v0.z, v0.w);
-        P[0] = df64(v1.x, v1.y); P[1] = df64(v1.z, v1.w); P[2] = df64(v2.x, v2.y);
-        PA[0] = df64(v2.z, v2.w); PA[1] = df64(v3.x, v3.y); PA[2] = df64(v3.z, v3.w);
-        K = df64(v4.x, v4.y); ea = df64(v4.z, v4.w);
-    }
-    static __device__ __forceinline__ const df64 *boys(const GradArgs &g) {
-        return reinterpret_cast<const df64 *>(g.boysdf);
-    }
-};
-
-__device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x; }
-__device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
-__device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
-
 template <int LA, int LB, int LC, int LD, typename R>
 __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
     using namespace gt;

@@ -154,12 +154,14 @@ static int pair_cls(int la, int lb) {
     return t[la][lb];
 }
 static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
-// gradient work lists: (class, precision) pairs, then one list for every class with a d shell
-#define GRAD_NLIST (2 * RCHEM_NCLASS + 1)
+// gradient work lists: (s/p class, precision) pairs, then (every class with a d shell, precision)
+#define GRAD_NLIST (2 * RCHEM_NCLASS + 2)
 // the specialised s/p gradient kernels, one translation unit per arithmetic (grad_sp_*.cu)
 bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
+void rchem_grad_rt_df64(const GradArgs &g, unsigned blocks, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
@@ -1154,7 +1156,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
     if (b->d_gtasks && b->gq_tau == tau && b->gq_tau32 == tau32) return RCHEM_OK;
     constexpr long long kGradPrimPerLane = 2;
     std::vector<EriSeg> segs;
-    // lists: 2 k (+1 for FP32) for the s/p class k, GRAD_NLIST - 1 for every class with a d shell
+    // lists: 2 k (+1 for FP32) for the s/p class k, 2 NCLASS (+1) for every class with a d shell
     std::vector<EriTask> per_class[GRAD_NLIST];
     const std::vector<ShellPair> &P = b->pairs;
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
@@ -1164,9 +1166,9 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
             const long long nprimq = (long long)gb.npp * gk.npp;
             const int L = gb.la + gb.lb + gk.la + gk.lb;
-            // s/p classes get their specialised kernel in FP64 (or double-float) and, below
-            // tau32, FP32; every class with a d shell shares one FP64 launch of the
-            // run-time kernel, whose lanes split primitive quartets x ket component pairs
+            // s/p classes get their specialised kernel, every class with a d shell the
+            // run-time kernel (its lanes split primitive quartets x ket component pairs);
+            // FP64 (or double-float) above tau32, FP32 below
             const int k = quartet_kernel(gb.cls, gk.cls);
             const int *l = rchem_class_l[k];
             const bool sp = l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1;
@@ -1174,7 +1176,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             int lg = 0;
             while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
             const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
-            for (int prec = 0; prec < (sp ? 2 : 1); ++prec) {
+            for (int prec = 0; prec < 2; ++prec) {
                 const int s0 = (int)segs.size();
                 long long total = 0;
                 for (int ib = gb.begin; ib < gb.end; ++ib) {
@@ -1182,7 +1184,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
                     if (!(Qb > 0.0)) continue;
                     int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
                     if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
-                    const int m = (sp && tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
+                    const int m = (tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
                     const int lo = prec ? m : 0, hi = prec ? nk : m;
                     if (hi <= lo) continue;
                     segs.push_back(EriSeg{ib, gk.begin + lo, hi - lo, 0});
@@ -1190,7 +1192,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
                 }
                 if (total == 0) continue;
                 pack_tasks(segs, s0, total, lg, ((units + (1 << lg) - 1) >> lg) * work,
-                           per_class[sp ? 2 * k + prec : GRAD_NLIST - 1]);
+                           per_class[sp ? 2 * k + prec : 2 * RCHEM_NCLASS + prec]);
             }
         }
     }
@@ -1279,7 +1281,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             g.tasks = b->d_gtasks + b->gtask_off[k];
             g.ntasks = (int)b->gtask_cnt[k];
             const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
-            if (k < GRAD_NLIST - 1) {  // an s/p class: its specialised kernel
+            if (k < 2 * RCHEM_NCLASS) {  // an s/p class: its specialised kernel
                 const int cls = k / 2;
                 const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
                                         : (o.emulated ? rchem_grad_sp_df64(cls, g, blocks, st)
@@ -1288,7 +1290,10 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
                 CK(cudaGetLastError());
                 continue;
             }
-            k_grad2e<<<blocks, 64, 0, st>>>(g);  // classes with d shells: run-time angular momenta
+            // classes with d shells: run-time angular momenta
+            if (k & 1) rchem_grad_rt_f32(g, blocks, st);
+            else if (o.emulated) rchem_grad_rt_df64(g, blocks, st);
+            else k_grad2e_rt<double><<<blocks, 64, 0, st>>>(g);
             CK(cudaGetLastError());
         }
         for (int i = 0; i < nuse; ++i) {
