@@ -116,39 +116,36 @@ __device__ __forceinline__ double gr_cnorm(const int *p) {
 }
 
 // Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
-// Hermite index with t+u+v <= bmax (box of side zd): the ket of one component
+// Hermite index with t+u+v <= bmax (stored compactly in md_tuv order): the ket of one component
 // contracted with the Coulomb integrals once, reused by every bra component.
 template <typename T>
 __device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
-                                        int zd, int bmax, T *Z) {
-    for (int t = 0; t < zd; ++t)
-        for (int u = 0; u < zd; ++u)
-            for (int v = 0; v < zd; ++v) {
+                                        int bmax, T *Z) {
+    for (int t = 0; t <= bmax; ++t)
+        for (int u = 0; u <= bmax - t; ++u)
+            for (int v = 0; v <= bmax - t - u; ++v) {
                 T z = T(0);
-                if (t + u + v <= bmax)
-                    for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
-                        const T fx = Ek[0][c[0]][d[0]][tt];
-                        for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
-                            const T fy = fx * Ek[1][c[1]][d[1]][uu];
-                            for (int vv = 0; vv <= c[2] + d[2]; ++vv)
-                                z = rchem_fma(fy * Ek[2][c[2]][d[2]][vv], R[md_tuv(t + tt, u + uu, v + vv)], z);
-                        }
+                for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
+                    const T fx = Ek[0][c[0]][d[0]][tt];
+                    for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
+                        const T fy = fx * Ek[1][c[1]][d[1]][uu];
+                        for (int vv = 0; vv <= c[2] + d[2]; ++vv)
+                            z = rchem_fma(fy * Ek[2][c[2]][d[2]][vv], R[md_tuv(t + tt, u + uu, v + vv)], z);
                     }
-                Z[(t * zd + u) * zd + v] = z;
+                }
+                Z[md_tuv(t, u, v)] = z;  // compact (t,u,v) order: only t+u+v <= bmax is stored
             }
 }
 
 // sum_{tuv} E^{ab}_{tuv} Z_{tuv}
 template <typename R>
-__device__ __forceinline__ R gr_dot(const R (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b, const R *Z,
-                                    int zd) {
+__device__ __forceinline__ R gr_dot(const R (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b, const R *Z) {
     R s = R(0);
     for (int t = 0; t <= a[0] + b[0]; ++t) {
         const R ex = Eb[0][a[0]][b[0]][t];
         for (int u = 0; u <= a[1] + b[1]; ++u) {
             const R ey = ex * Eb[1][a[1]][b[1]][u];
-            const R *Zr = Z + (t * zd + u) * zd;
-            for (int v = 0; v <= a[2] + b[2]; ++v) s = rchem_fma(ey * Eb[2][a[2]][b[2]][v], Zr[v], s);
+            for (int v = 0; v <= a[2] + b[2]; ++v) s = rchem_fma(ey * Eb[2][a[2]][b[2]][v], Z[md_tuv(t, u, v)], s);
         }
     }
     return s;
@@ -195,8 +192,7 @@ __device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x;
 __device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
 __device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
 
-#define GR_ZD 6                           // bra Hermite box side: la+lb+2 <= 6
-#define GR_ZN (GR_ZD * GR_ZD * GR_ZD)
+#define GR_ZN 56  // (t,u,v) with t+u+v <= la+lb+1 <= 5
 
 #define GR_MAXC4 1296  // components of a (dd|dd) quartet
 
@@ -271,7 +267,6 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     const R *btab = GradPrim<R>::boys(g);
     R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int L1 = la + lb + lc + ld + 1;
-    const int zd = la + lb + 2;
     R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
     R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
     // work units: (primitive quartet, ket component pair); the G lanes split them
@@ -308,16 +303,16 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
         const int kc = kcd / nd, kd = kcd - kc * nd;
         const R *Gq = Gam + (kc * nd + kd) * na * nb;
         // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
-        gr_zvec<R>(Ek, cC[kc], cD[kd], Rt, zd, la + lb + 1, Z0);
+        gr_zvec<R>(Ek, cC[kc], cD[kd], Rt, la + lb + 1, Z0);
         for (int x = 0; x < 3; ++x) {
             s[0] = cC[kc][0];
             s[1] = cC[kc][1];
             s[2] = cC[kc][2];
             s[x] += 1;
-            gr_zvec<R>(Ek, s, cD[kd], Rt, zd, la + lb, Zp[x]);
+            gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
             if (cC[kc][x] > 0) {
                 s[x] -= 2;
-                gr_zvec<R>(Ek, s, cD[kd], Rt, zd, la + lb, Zm[x]);
+                gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
             }
         }
         for (int ka = 0; ka < na; ++ka) {
@@ -331,10 +326,10 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
                     s[1] = A[1];
                     s[2] = A[2];
                     s[x] += 1;
-                    R v = a2 * gr_dot<R>(Eb, s, B, Z0, zd);
+                    R v = a2 * gr_dot<R>(Eb, s, B, Z0);
                     if (A[x] > 0) {
                         s[x] -= 2;
-                        v = v - R(A[x]) * gr_dot<R>(Eb, s, B, Z0, zd);
+                        v = v - R(A[x]) * gr_dot<R>(Eb, s, B, Z0);
                     }
                     gA[x] = rchem_fma(Gm, v, gA[x]);
                     // centre B
@@ -342,15 +337,15 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
                     s[1] = B[1];
                     s[2] = B[2];
                     s[x] += 1;
-                    v = b2 * gr_dot<R>(Eb, A, s, Z0, zd);
+                    v = b2 * gr_dot<R>(Eb, A, s, Z0);
                     if (B[x] > 0) {
                         s[x] -= 2;
-                        v = v - R(B[x]) * gr_dot<R>(Eb, A, s, Z0, zd);
+                        v = v - R(B[x]) * gr_dot<R>(Eb, A, s, Z0);
                     }
                     gB[x] = rchem_fma(Gm, v, gB[x]);
                     // centre C
-                    v = c2 * gr_dot<R>(Eb, A, B, Zp[x], zd);
-                    if (cC[kc][x] > 0) v = v - R(cC[kc][x]) * gr_dot<R>(Eb, A, B, Zm[x], zd);
+                    v = c2 * gr_dot<R>(Eb, A, B, Zp[x]);
+                    if (cC[kc][x] > 0) v = v - R(cC[kc][x]) * gr_dot<R>(Eb, A, B, Zm[x]);
                     gC[x] = rchem_fma(Gm, v, gC[x]);
                 }
             }

@@ -161,7 +161,6 @@ bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t s
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
-void rchem_grad_rt_df64(const GradArgs &g, unsigned blocks, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
@@ -1290,9 +1289,10 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
                 CK(cudaGetLastError());
                 continue;
             }
-            // classes with d shells: run-time angular momenta
+            // classes with d shells: run-time angular momenta, FP32 below tau32 and FP64
+            // above, also in the emulated form (this kernel is bound by its local-memory
+            // tables, not the FP64 pipe: double-float measured slower)
             if (k & 1) rchem_grad_rt_f32(g, blocks, st);
-            else if (o.emulated) rchem_grad_rt_df64(g, blocks, st);
             else k_grad2e_rt<double><<<blocks, 64, 0, st>>>(g);
             CK(cudaGetLastError());
         }
