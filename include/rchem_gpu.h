@@ -161,8 +161,9 @@ int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K
  * derivative S/T/V contracted with W and D, Hellmann-Feynman term included.
  * No counterpart in the reference, which has no gradients.  opts: schwarz_tau,
  * where (for D, W and grad), fp32_tau (quartets with Q_ab Q_cd below it in
- * FP32, the rest FP64) and emulated (the FP64 quartets of the s/p classes in
- * double-float arithmetic on the FP32 pipe; classes with a d shell stay FP64).
+ * FP32, the rest FP64) and emulated (the FP64 quartets of the s/p classes up to
+ * (pp|ps) in double-float arithmetic on the FP32 pipe; (pp|pp) and the classes
+ * with a d shell stay FP64).
  */
 int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad, const rchem_jk_opts *opts);
 

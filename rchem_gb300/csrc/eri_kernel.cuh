@@ -360,7 +360,7 @@ __device__ __forceinline__ R wc_sel4(int n, const R *v) {  // v[0..3] = 1..4 tim
     return n == 1 ? v[0] : (n == 2 ? v[1] : (n == 3 ? v[2] : v[3]));
 }
 
-template <int LA, int LB, int LC, int LD, typename R>
+template <int LA, int LB, int LC, int LD, typename R, int EPI = EPI_JK>
 __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
     using C = EriClass<LA, LB, LC, LD>;
     using P = EriProg<LA, LB, LC, LD>;
@@ -481,6 +481,36 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
     }
     for (int k = lane; k < P::NOUT; k += 32) A[k] = R(__ldg(P::onorm() + k)) * S[__ldg(P::out() + k)];
     __syncwarp();
+    if constexpr (EPI == EPI_DIAG) {  // Schwarz bound sqrt(max |(ab|ab)|) of a diagonal quartet
+        if constexpr (LA == LC && LB == LD) {
+            double m = 0.0;
+            for (int t = lane; t < NA * NB; t += 32) {
+                const int ia = t / NB, ib = t - ia * NB;
+                m = fmax(m, fabs((double)A[((ia * NB + ib) * NC + ia) * ND + ib]));
+            }
+            for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) a.J[kidx] = sqrt(m);
+        }
+        return;
+    }
+    if constexpr (EPI == EPI_STORE) {  // the dense tensor, 8 symmetric positions per integral
+        const size_t N1 = (size_t)bp.mn, N2 = N1 * N1, N3 = N2 * N1;
+        const int i0 = bp.aoA, j0 = bp.aoB, k0 = kp.aoA, l0s = kp.aoB;
+        for (int t = lane; t < NA * NB * NC * ND; t += 32) {
+            const int id = t % ND, ic = (t / ND) % NC, ib = (t / (ND * NC)) % NB, ia = t / (ND * NC * NB);
+            const double v = (double)A[t];
+            const size_t i = i0 + ia, j = j0 + ib, k = k0 + ic, l = l0s + id;
+            a.eri[i * N3 + j * N2 + k * N1 + l] = v;
+            a.eri[j * N3 + i * N2 + k * N1 + l] = v;
+            a.eri[i * N3 + j * N2 + l * N1 + k] = v;
+            a.eri[j * N3 + i * N2 + l * N1 + k] = v;
+            a.eri[k * N3 + l * N2 + i * N1 + j] = v;
+            a.eri[l * N3 + k * N2 + i * N1 + j] = v;
+            a.eri[k * N3 + l * N2 + j * N1 + i] = v;
+            a.eri[l * N3 + k * N2 + j * N1 + i] = v;
+        }
+        return;
+    }
 
     // degeneracy-weighted 8-fold scatter, the lanes splitting each contraction
     R deg = R(1);
@@ -554,6 +584,18 @@ cudaError_t prepare_eri_class() {
         e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, df64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)WcShape<LA, LB, LC, LD, df64>::SMEM);
         if (e != cudaSuccess) return e;
+        if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
+            e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double, EPI_STORE>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)WcShape<LA, LB, LC, LD, double>::SMEM);
+            if (e != cudaSuccess) return e;
+            if constexpr (LA == LC && LB == LD) {
+                e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double, EPI_DIAG>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)WcShape<LA, LB, LC, LD, double>::SMEM);
+                if (e != cudaSuccess) return e;
+            }
+        }
         return cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)WcShape<LA, LB, LC, LD, float>::SMEM);
     }
@@ -566,8 +608,23 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
     const int threads = 128;
     const long long nthreads = (long long)a.ntasks * 32;
     const int blocks = (int)((nthreads + threads - 1) / threads);
+    if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
+        // the largest classes exist only as warp-cooperative kernels (one quartet per
+        // task in every plan); their straight-line code would take minutes to compile
+        using W = WcShape<LA, LB, LC, LD, double>;
+        const int wb = (a.ntasks + W::WARPS - 1) / W::WARPS;
+        if (epi == EPI_STORE) {
+            eri_wc_kernel<LA, LB, LC, LD, double, EPI_STORE><<<wb, 32 * W::WARPS, W::SMEM, s>>>(a);
+            return;
+        }
+        if (epi == EPI_DIAG) {
+            if constexpr (LA == LC && LB == LD)
+                eri_wc_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<wb, 32 * W::WARPS, W::SMEM, s>>>(a);
+            return;
+        }
+    }
     if constexpr (EriClass<LA, LB, LC, LD>::WC) {
-        if (epi == EPI_JK && a.wc) {  // one warp per task, the plan gives one quartet per task
+        if (epi == EPI_JK && (a.wc || EriClass<LA, LB, LC, LD>::WC_ONLY)) {  // one quartet per task
             if (prec == 1) {
                 using W = WcShape<LA, LB, LC, LD, float>;
                 eri_wc_kernel<LA, LB, LC, LD, float>
@@ -584,6 +641,7 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
             return;
         }
     }
+    if constexpr (!EriClass<LA, LB, LC, LD>::WC_ONLY) {
     if (epi == EPI_JK) {
         if (prec == 1) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
         else if constexpr (LA + LB + LC + LD <= 4) {
@@ -596,5 +654,6 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
         eri_class_kernel<LA, LB, LC, LD, double, EPI_STORE><<<blocks, threads, 0, s>>>(a);
     } else if constexpr (LA == LC && LB == LD) {
         eri_class_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<blocks, threads, 0, s>>>(a);
+    }
     }
 }

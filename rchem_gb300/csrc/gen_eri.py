@@ -336,6 +336,7 @@ def boys_ops(L, ntay=NTAY64):
 # 32 lanes taking the independent terms of a level.  The DAG is the same one
 # the straight-line code follows (same direction choices, same terms).
 WC_MINL = 4  # classes with l_a+l_b+l_c+l_d >= WC_MINL get a program
+WC_ONLY_MINL = 7  # ... and from here on have no one-lane-group-per-quartet kernel at all
 
 
 def _levels(depth, order, key):
@@ -492,6 +493,8 @@ def main(outdir):
         lines.append("  static constexpr double PRIM_FLOPS = %d.0, CONTR_FLOPS = %d.0;" % (prim_flops, contr_flops))
         lines.append("  static constexpr bool WC = %s;  // a warp-cooperative program evaluates the J/K epilogue class"
                      % ("true" if L >= WC_MINL else "false"))
+        lines.append("  static constexpr bool WC_ONLY = %s;  // every epilogue runs the warp-cooperative kernel"
+                     % ("true" if L >= WC_ONLY_MINL else "false"))
         lines.append("  template <typename R> __host__ __device__ static __forceinline__ void vrr(R* __restrict__ acc, const R* __restrict__ F,")
         lines.append("      R PAx, R PAy, R PAz, R WPx, R WPy, R WPz, R QCx, R QCy, R QCz, R WQx, R WQy, R WQz,")
         lines.append("      R ohp, R ohq, R ohpq, R rho_p, R rho_q) {")
@@ -550,6 +553,9 @@ def main(outdir):
         f.write("// 1: the J/K epilogue class runs the warp-cooperative program (one quartet per warp)\n")
         f.write("static const int rchem_class_wc[%d] = {%s};\n" % (
             len(cls), ", ".join("1" if sum(t[:4]) >= WC_MINL else "0" for t in table)))
+        f.write("// 1: the class has only the warp-cooperative kernel (one quartet per warp in every plan)\n")
+        f.write("static const int rchem_class_wc_only[%d] = {%s};\n" % (
+            len(cls), ", ".join("1" if sum(t[:4]) >= WC_ONLY_MINL else "0" for t in table)))
         f.write("static const double rchem_class_flops[%d][2] = {\n" % len(cls))
         for t in table:
             f.write("  {%d.0, %d.0},\n" % t[4:6])

@@ -460,6 +460,7 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
         const long long nprimq = (long long)g.npp * g.npp;
         int lg = 0;
         while (lg < 5 && nprimq >= 4LL << (lg + 1)) ++lg;
+        if (rchem_class_wc_only[quartet_kernel(g.cls, g.cls)]) lg = 5;  // warp-cooperative: one quartet per warp
         pack_tasks(segs, g.begin, g.end - g.begin, lg, 0, per_class[quartet_kernel(g.cls, g.cls)]);
     }
     std::vector<EriTask> tasks;
@@ -681,7 +682,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 int lg = 0;
                 const long long ppl = b->ppl[k][prec];
                 while (lg < 5 && nprimq >= ppl << (lg + 1)) ++lg;
-                if (b->wc[k][prec]) lg = 5;  // warp-cooperative kernel: one quartet per warp
+                if (b->wc[k][prec] || rchem_class_wc_only[k]) lg = 5;  // warp-cooperative: one quartet per warp
                 pack_tasks(sv, s0, total, lg, (nprimq + (1 << lg) - 1) >> lg, lists[k][prec]);
                 const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
                 b->list_flops[k][prec] += fl;
@@ -1283,8 +1284,8 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             if (k < 2 * RCHEM_NCLASS) {  // an s/p class: its specialised kernel
                 const int cls = k / 2;
                 const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
-                                        : (o.emulated ? rchem_grad_sp_df64(cls, g, blocks, st)
-                                                      : rchem_grad_sp_f64(cls, g, blocks, st));
+                                        : ((o.emulated && rchem_grad_sp_df64(cls, g, blocks, st)) ||
+                                           rchem_grad_sp_f64(cls, g, blocks, st));
                 if (!ok) return set_err(RCHEM_ERR_UNSUPPORTED, "gradient list %d has no specialised kernel", k);
                 CK(cudaGetLastError());
                 continue;
