@@ -406,6 +406,10 @@ static int upload(T **dst, const std::vector<T> &src, cudaStream_t s) {
 }
 
 static const double kPrimCut = 1e-22;  // drop primitive pairs with exp(-ab/p |AB|^2) below this
+// ... and those whose prefactor bounds every primitive integral they enter below
+// 1e-16: |K_ab| max|K_cd| < kPrimRel (an integral of such a pair with any ket is
+// below about kPrimRel times its angular factors, far under the 1e-12 targets)
+static const double kPrimRel = 1e-16;
 
 static EriArgs base_args(rchem_basis b) {
     EriArgs a;
@@ -553,6 +557,24 @@ static int build_pairs(rchem_basis b) {
             c.cls = pair_cls(sa.l, sb.l);
             cands.push_back(std::move(c));
         }
+    // relative primitive cut against the largest pair prefactor
+    double kmax = 0.0;
+    for (const Cand &c : cands)
+        for (const PairPrim &q : c.pp) kmax = std::max(kmax, std::fabs(q.K));
+    {
+        std::vector<Cand> kept;
+        kept.reserve(cands.size());
+        for (Cand &c : cands) {
+            std::vector<PairPrim> pp;
+            for (const PairPrim &q : c.pp)
+                if (std::fabs(q.K) * kmax >= kPrimRel) pp.push_back(q);
+            if (pp.empty()) continue;
+            c.pp = std::move(pp);
+            c.sp.npp = (int)c.pp.size();
+            kept.push_back(std::move(c));
+        }
+        cands = std::move(kept);
+    }
     // groups keyed by (geometry, class, npp), geometries in order
     std::map<std::tuple<int, int, int>, std::vector<int>> gm;
     for (int i = 0; i < (int)cands.size(); ++i)
