@@ -236,20 +236,27 @@ def target_workloads(rc, torch):
     # in one handle: every Fock build is one graph launch over all of them
     geoms = rc.geometry.water_batch(512, seed=7)
     bb = rc.batch.BatchBasis(geoms, "6-31g-fit")
-    rc.batch.rhf_batch(bb, max_iter=2)  # warm-up (plans, graphs)
-    rec = {"geometries": bb.ngeom, "packed_elements": bb.packed, "sizes": sorted(set(bb.geom_nbf.tolist()))}
+    rc.batch.rhf_native(bb, max_iter=2)  # warm-up (plans, graphs)
+    rc.batch.rhf_batch(bb, max_iter=2)
+    rec = {"geometries": bb.ngeom, "packed_elements": bb.packed, "sizes": sorted(set(bb.geom_nbf.tolist())),
+           "scf_driver": "rchem_rhf (the whole SCF loop in the library)"}
     for tag, tau32, emul in (("fp64", 0.0, False), ("mixed", 1e-6, False), ("emulated_mixed", 1e-6, True)):
         bb.autotune(1e-12, tau32, emulated=emul)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
+        r = rc.batch.rhf_native(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         g = rc.batch.gradient_batch(bb, r, fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
+        rp = rc.batch.rhf_batch(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
         rec[tag] = {"scf_s": t1 - t0, "gradient_s": t2 - t1, "s_per_geometry": (t2 - t0) / bb.ngeom,
-                    "iterations": r["iterations"], "converged": r["converged"], "e_total": r["e_total"]}
+                    "iterations": r["iterations"], "converged": r["converged"], "e_total": r["e_total"],
+                    "python_driver_scf_s": t3 - t2,
+                    "python_driver_max_abs_dE_Eh": float(np.abs(rp["e_total"] - r["e_total"]).max())}
     D = torch.zeros(bb.packed, dtype=torch.float64, device="cuda")
     J, K = torch.empty_like(D), torch.empty_like(D)
     rc.batch.jk(bb, D, J, K)

@@ -181,6 +181,37 @@ int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad
 int rchem_eigh_batched(int n, int batch, const double *A, double *w, double *V, void *stream);
 
 /*
+ * Restricted Hartree-Fock for every geometry of a handle at once, entirely on
+ * the GPU (no counterpart in the reference's C layer: it is the SCF loop of
+ * src/bin/rchem.rs:40-127 -- symmetric orthogonalisation, core-Hamiltonian
+ * guess, D = C_occ C_occ^T without the factor 2, F = H + 2J - K,
+ * E = sum (H + F) o D -- with Pulay DIIS on X^T (FDS - SDF) X added).  All
+ * geometries iterate together until every energy changes by less than
+ * thresh_e and the density by less than thresh_d.  Diagonalisations use the
+ * batched Jacobi solver: every geometry must have n <= 64 basis functions
+ * (RCHEM_ERR_UNSUPPORTED otherwise; the Python driver rchem_gb300.scf covers
+ * larger single geometries).
+ *   opts      thresholds, iteration cap, DIIS length (0..8) and the Fock-build
+ *             options (jk.schwarz_tau, jk.fp32_tau, jk.emulated; jk.where
+ *             says where D_out / W_out live); NULL = defaults
+ *             (1e-10, 1e-7, 128, 8, FP64, host)
+ *   nocc      doubly occupied orbitals per geometry (NULL: half the electrons)
+ *   e_elec, e_nuc   host arrays[ngeom] (may be NULL): E_elec as the reference
+ *             prints it and the nuclear repulsion
+ *   D_out, W_out    packed density and energy-weighted density (may be NULL),
+ *             the inputs of rchem_gradient
+ */
+typedef struct {
+    double thresh_e;   /* |Delta E| per geometry between iterations */
+    double thresh_d;   /* max |Delta D| */
+    int max_iter;
+    int diis;          /* DIIS history length, 0 = plain Roothaan iterations */
+    rchem_jk_opts jk;
+} rchem_scf_opts;
+int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *nocc, double *e_elec, double *e_nuc,
+              double *D_out, double *W_out, int *iterations, int *converged);
+
+/*
  * Autotune the Fock build's tile shapes for this basis and these thresholds
  * (no counterpart in the reference): for every integral class list (21
  * classes x {FP64, FP32}) time the list alone under each candidate number of

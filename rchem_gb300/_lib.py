@@ -38,6 +38,11 @@ class JKStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class SCFOpts(C.Structure):
+    _fields_ = [("thresh_e", C.c_double), ("thresh_d", C.c_double), ("max_iter", C.c_int), ("diis", C.c_int),
+                ("jk", JKOpts)]
+
+
 class Prim(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("norm", C.c_double), ("alpha", C.c_double),
                 ("l", C.c_int), ("m", C.c_int), ("n", C.c_int), ("pad", C.c_int)]
@@ -73,6 +78,7 @@ def lib():
     L.rchem_autotune.argtypes = [vp, p(JKOpts), vp]
     L.rchem_eigh_batched.argtypes = [i, i, vp, vp, vp, vp]
     L.rchem_set_tile_shape.argtypes = [vp, i, i, i]
+    L.rchem_rhf.argtypes = [vp, p(SCFOpts), vp, vp, vp, vp, vp, vp, vp]
     L.rchem_jk_class_stats.argtypes = [vp, vp, vp, vp, vp]
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
@@ -110,5 +116,5 @@ def exported_symbols():
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
         "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_eigh_batched",
-        "rchem_set_tile_shape",
+        "rchem_set_tile_shape", "rchem_rhf",
     ]

@@ -258,6 +258,30 @@ def _rhf_batch(bb, thresh_e, thresh_d, max_iter, diis, fp32_tau, schwarz_tau, em
             "converged": bool(conv.all())}
 
 
+def rhf_native(bb: Basis, thresh_e=1e-10, thresh_d=1e-7, max_iter=128, diis=8, fp32_tau=0.0, schwarz_tau=1e-12,
+               emulated=False):
+    """The same RHF as rhf_batch, run entirely inside librchem_gpu.so
+    (rchem_rhf): one C call, every geometry's matrices on the GPU, Jacobi
+    diagonalisation (each geometry n <= 64).  Works on a single-geometry Basis
+    too.  Returns per-geometry energies and the packed D and W."""
+    import torch
+
+    ng = getattr(bb, "ngeom", 1)
+    packed = getattr(bb, "packed", bb.nbf * bb.nbf)
+    o = _lib.SCFOpts(thresh_e=thresh_e, thresh_d=thresh_d, max_iter=max_iter, diis=diis,
+                     jk=_lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
+                                    where=_lib.DEVICE, emulated=1 if emulated else 0))
+    e_elec, e_nuc = np.zeros(ng), np.zeros(ng)
+    D = torch.empty(packed, dtype=torch.float64, device="cuda")
+    W = torch.empty_like(D)
+    it, conv = C.c_int(0), C.c_int(0)
+    _after_torch(bb, D, W)
+    _lib.check(_lib.lib().rchem_rhf(bb.handle, C.byref(o), None, e_elec.ctypes.data, e_nuc.ctypes.data,
+                                    C.c_void_p(D.data_ptr()), C.c_void_p(W.data_ptr()), C.byref(it), C.byref(conv)))
+    return {"e_elec": e_elec, "e_nuc": e_nuc, "e_total": e_elec + e_nuc, "D": D, "W": W, "iterations": it.value,
+            "converged": bool(conv.value)}
+
+
 def gradient_batch(bb: BatchBasis, res: dict, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
     """Nuclear gradients of every geometry: one set of adjoint-kernel launches
     (precision options as in scf.gradient); returns a list of (natoms_g x 3) arrays."""

@@ -19,12 +19,13 @@
 #define RCHEM_EIGH_MAXSWEEP 40
 #define RCHEM_EIGH_THREADS 256
 
-// shared layout: A[n][ld], V[n][ld] (ld = n | 1, odd, so column walks do not
-// repeat banks), then the m/2 rotations (c, s, p, q) and the reduction slots
-__global__ void __launch_bounds__(RCHEM_EIGH_THREADS) k_eigh_jacobi(int n, const double *__restrict__ Ain,
-                                                                     double *__restrict__ w_out,
-                                                                     double *__restrict__ V_out, int *sweeps_out) {
-    extern __shared__ double sm[];
+// One matrix per thread block: A (n x n, row-major, lower triangle read) ->
+// w[n] ascending, V[n x n] eigenvectors as columns.  Shared layout: A[n][ld],
+// V[n][ld] (ld = n | 1, odd, so column walks do not repeat banks), then the
+// m/2 rotations (c, s, p, q) and the reduction slots.
+__device__ __forceinline__ void eigh_jacobi_block(int n, const double *__restrict__ Ain, double *__restrict__ w_out,
+                                                  double *__restrict__ V_out, double *sm, int *s_done_ptr,
+                                                  int *sweeps_out) {
     const int ld = n | 1;
     const int m = n + (n & 1);  // players of the round-robin (one dummy when n is odd)
     const int np = m / 2;
@@ -35,14 +36,13 @@ __global__ void __launch_bounds__(RCHEM_EIGH_THREADS) k_eigh_jacobi(int n, const
     double *red = rs + np;        // reduction scratch [RCHEM_EIGH_THREADS / 32 * 2]
     int *rp = (int *)(red + 2 * (RCHEM_EIGH_THREADS / 32));  // p[np], q[np]
     int *rq = rp + np;
-    __shared__ int s_done;
+    int &s_done = *s_done_ptr;
     const int tid = threadIdx.x, nth = blockDim.x;
-    const size_t base = (size_t)blockIdx.x * n * n;
 
     // load the lower triangle, mirror it; V = I
     for (int e = tid; e < n * n; e += nth) {
         const int i = e / n, j = e - i * n;
-        const double v = i >= j ? Ain[base + (size_t)i * n + j] : Ain[base + (size_t)j * n + i];
+        const double v = i >= j ? Ain[(size_t)i * n + j] : Ain[(size_t)j * n + i];
         A[i * ld + j] = v;
         V[i * ld + j] = i == j ? 1.0 : 0.0;
     }
@@ -139,10 +139,20 @@ __global__ void __launch_bounds__(RCHEM_EIGH_THREADS) k_eigh_jacobi(int n, const
             const double wj = A[j * ld + j];
             rank += (wj < wi) || (wj == wi && j < i);
         }
-        w_out[(size_t)blockIdx.x * n + rank] = wi;
-        for (int row = 0; row < n; ++row) V_out[base + (size_t)row * n + rank] = V[row * ld + i];
+        w_out[rank] = wi;
+        for (int row = 0; row < n; ++row) V_out[(size_t)row * n + rank] = V[row * ld + i];
     }
-    if (sweeps_out && tid == 0) sweeps_out[blockIdx.x] = sweep;
+    if (sweeps_out && tid == 0) *sweeps_out = sweep;
+}
+
+__global__ void __launch_bounds__(RCHEM_EIGH_THREADS) k_eigh_jacobi(int n, const double *__restrict__ Ain,
+                                                                     double *__restrict__ w_out,
+                                                                     double *__restrict__ V_out, int *sweeps_out) {
+    extern __shared__ double sm[];
+    __shared__ int s_done;
+    const size_t base = (size_t)blockIdx.x * n * n;
+    eigh_jacobi_block(n, Ain + base, w_out + (size_t)blockIdx.x * n, V_out + base, sm, &s_done,
+                      sweeps_out ? sweeps_out + blockIdx.x : nullptr);
 }
 
 inline size_t eigh_smem_bytes(int n) {

@@ -28,6 +28,7 @@
 #include "eigh.cuh"
 #include "eri_kernel.cuh"
 #include "grad.cuh"
+#include "scf_batch.cuh"
 #include "md.cuh"
 #include "rchem_types.h"
 
@@ -67,6 +68,14 @@ struct CudaFreeGuard {
     }
     CudaFreeGuard(const CudaFreeGuard &) = delete;
     CudaFreeGuard &operator=(const CudaFreeGuard &) = delete;
+};
+// ... and a list of them
+struct CudaFreeList {
+    std::vector<void *> p;
+    ~CudaFreeList() {
+        for (void *q : p)
+            if (q) cudaFree(q);
+    }
 };
 
 extern "C" const char *rchem_last_error(void) { return g_err; }
@@ -1810,5 +1819,181 @@ extern "C" int rchem_eigh_batched(int n, int batch, const double *A, double *w, 
     CK(cudaFuncSetAttribute(k_eigh_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_eigh_jacobi<<<batch, RCHEM_EIGH_THREADS, smem, (cudaStream_t)stream>>>(n, A, w, V, nullptr);
     CK(cudaGetLastError());
+    return RCHEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// native RHF driver: every geometry of the handle at once (scf_batch.cuh)
+// ---------------------------------------------------------------------------
+__global__ void k_scf_add(long long packed, const double *x, double *y) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < packed) y[i] += x[i];
+}
+
+extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *nocc_in, double *e_elec,
+                         double *e_nuc, double *D_out, double *W_out, int *iterations, int *converged) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    rchem_scf_opts o;
+    memset(&o, 0, sizeof(o));
+    o.thresh_e = 1e-10;
+    o.thresh_d = 1e-7;
+    o.max_iter = 128;
+    o.diis = RCHEM_DIIS_MAX;
+    if (opts) o = *opts;
+    if (o.diis < 0 || o.diis > RCHEM_DIIS_MAX) return set_err(RCHEM_ERR_INVALID, "diis = %d (0..%d)", o.diis, RCHEM_DIIS_MAX);
+    if (o.max_iter < 1) return set_err(RCHEM_ERR_INVALID, "max_iter = %d", o.max_iter);
+    if (o.jk.where != RCHEM_HOST && o.jk.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.jk.where);
+    const int ng = b->ngeom;
+    const long long packed = b->packed;
+    int nmax = 0;
+    std::vector<int> nocc(ng);
+    for (int g = 0; g < ng; ++g) {
+        const GeomDev &gm = b->geoms[g];
+        nmax = std::max(nmax, gm.n);
+        if (nocc_in) {
+            nocc[g] = nocc_in[g];
+        } else {
+            int ne = 0;
+            for (int a = gm.atom0; a < gm.atom0 + gm.natoms; ++a) ne += b->Z[a];
+            if (ne % 2) return set_err(RCHEM_ERR_INVALID, "geometry %d has an odd electron count (%d)", g, ne);
+            nocc[g] = ne / 2;
+        }
+        if (nocc[g] < 0 || nocc[g] > gm.n) return set_err(RCHEM_ERR_INVALID, "geometry %d: nocc %d", g, nocc[g]);
+    }
+    if (nmax > RCHEM_EIGH_MAXN)
+        return set_err(RCHEM_ERR_UNSUPPORTED, "rchem_rhf diagonalises n <= %d per geometry (largest: %d)",
+                       RCHEM_EIGH_MAXN, nmax);
+    cudaStream_t st = b->stream;
+    const size_t bytes = (size_t)packed * sizeof(double);
+    // device buffers, freed on every return path
+    enum { S_, H_, X_, T1_, T2_, F_, FX_, D_, DO_, J_, K_, W_, CV_, EPS_, NB_ };
+    double *buf[NB_] = {};
+    CudaFreeList guards;
+    for (int k = 0; k < NB_; ++k) {
+        CK(cudaMalloc(&buf[k], bytes));
+        guards.p.push_back(buf[k]);
+    }
+    const int nh = std::max(o.diis, 1);
+    double *Fh = nullptr, *Eh = nullptr, *d_e = nullptr, *d_dm = nullptr, *d_coef = nullptr;
+    int *d_nocc = nullptr;
+    CK(cudaMalloc(&Fh, bytes * nh));
+    guards.p.push_back(Fh);
+    CK(cudaMalloc(&Eh, bytes * nh));
+    guards.p.push_back(Eh);
+    CK(cudaMalloc(&d_e, ng * sizeof(double)));
+    guards.p.push_back(d_e);
+    CK(cudaMalloc(&d_dm, ng * sizeof(double)));
+    guards.p.push_back(d_dm);
+    CK(cudaMalloc(&d_coef, (size_t)ng * RCHEM_DIIS_MAX * sizeof(double)));
+    guards.p.push_back(d_coef);
+    CK(cudaMalloc(&d_nocc, ng * sizeof(int)));
+    guards.p.push_back(d_nocc);
+    CK(cudaMemcpyAsync(d_nocc, nocc.data(), ng * sizeof(int), cudaMemcpyHostToDevice, st));
+    double *S = buf[S_], *H = buf[H_], *X = buf[X_], *T1 = buf[T1_], *T2 = buf[T2_], *F = buf[F_], *Fx = buf[FX_],
+           *D = buf[D_], *Dold = buf[DO_], *J = buf[J_], *K = buf[K_], *Wm = buf[W_], *Cv = buf[CV_],
+           *eps = buf[EPS_];
+    const size_t esm = eigh_smem_bytes(nmax);
+    CK(cudaFuncSetAttribute(k_scf_eigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esm));
+    const int th = RCHEM_SCF_THREADS;
+    const unsigned eb = (unsigned)((packed + th - 1) / th);
+    const GeomDev *geo = b->d_geom;
+    // S, H = T + V, X = S^-1/2 (the eigenvalues go to eps, the vectors to T1)
+    CKR(onee(b, 0, nullptr, 0, 0, 0, S, RCHEM_DEVICE));
+    CKR(onee(b, 1, nullptr, 0, 0, 0, H, RCHEM_DEVICE));
+    CKR(onee(b, 2, nullptr, 0, 0, 0, T2, RCHEM_DEVICE));
+    k_scf_add<<<eb, th, 0, st>>>(packed, T2, H);
+    k_scf_eigh<<<ng, RCHEM_EIGH_THREADS, esm, st>>>(geo, S, eps, T1);
+    k_scf_invsqrt<<<ng, th, 0, st>>>(geo, eps, T1, X);
+    CK(cudaGetLastError());
+    // F' = X^T F X -> eigenpairs (eps, C' in T1) -> C = X C' (Cv) -> D (and W)
+    auto density = [&](const double *Fin, double *Dd, double *Ww) -> int {
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 1, Fin, 0, T1, 1.0, 0.0);
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, X, 0, T2, 1.0, 0.0);
+        k_scf_eigh<<<ng, RCHEM_EIGH_THREADS, esm, st>>>(geo, T2, eps, T1);
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 0, T1, 0, Cv, 1.0, 0.0);
+        k_scf_density<<<ng, th, 0, st>>>(geo, d_nocc, Cv, eps, Dd, Ww);
+        CK(cudaGetLastError());
+        return RCHEM_OK;
+    };
+    CKR(density(H, D, nullptr));  // core-Hamiltonian guess
+    rchem_jk_opts jo = o.jk;
+    jo.where = RCHEM_DEVICE;
+    std::vector<double> eg(ng), dm(ng), eprev(ng, 0.0);
+    int it = 0, nstored = 0, newest = 0;
+    bool conv = false;
+    for (it = 1; it <= o.max_iter; ++it) {
+        CKR(rchem_jk_direct(b, D, J, K, &jo));
+        k_scf_fock<<<eb, th, 0, st>>>(packed, H, J, K, F);
+        k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, nullptr, d_e, d_dm);
+        const double *Fuse = F;
+        if (o.diis > 0) {
+            // error X^T (FDS - SDF) X into the newest ring slot, F beside it
+            newest = (it - 1) % o.diis;
+            nstored = std::min(nstored + 1, o.diis);
+            k_scf_gemm<<<ng, th, 0, st>>>(geo, F, 0, D, 0, T1, 1.0, 0.0);
+            k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, S, 0, T2, 1.0, 0.0);
+            k_scf_antisym<<<ng, th, 0, st>>>(geo, T2, T1);
+            k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 1, T1, 0, T2, 1.0, 0.0);
+            k_scf_gemm<<<ng, th, 0, st>>>(geo, T2, 0, X, 0, Eh + (size_t)newest * packed, 1.0, 0.0);
+            CK(cudaMemcpyAsync(Fh + (size_t)newest * packed, F, bytes, cudaMemcpyDeviceToDevice, st));
+            if (nstored >= 2) {
+                k_scf_diis<<<ng, th, 0, st>>>(geo, Eh, packed, nstored, d_coef);
+                k_scf_extrapolate<<<ng, th, 0, st>>>(geo, Fh, packed, nstored, newest, d_coef, Fx);
+                Fuse = Fx;
+            }
+            CK(cudaGetLastError());
+        }
+        CK(cudaMemcpyAsync(Dold, D, bytes, cudaMemcpyDeviceToDevice, st));
+        CKR(density(Fuse, D, nullptr));
+        // change of the density: max |D - Dold| (the pass's energy sum lands in scratch)
+        k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, Dold, d_coef, d_dm);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(eg.data(), d_e, ng * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(dm.data(), d_dm, ng * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (it > 1) {
+            bool ok = true;
+            double dmax = 0.0;
+            for (int g = 0; g < ng; ++g) {
+                ok = ok && std::fabs(eg[g] - eprev[g]) < o.thresh_e;
+                dmax = std::max(dmax, dm[g]);
+            }
+            if (ok && dmax < o.thresh_d) {
+                conv = true;
+                break;
+            }
+        }
+        eprev = eg;
+    }
+    if (it > o.max_iter) it = o.max_iter;
+    // energies at the final density with its own Fock matrix; W from that F's orbitals
+    CKR(rchem_jk_direct(b, D, J, K, &jo));
+    k_scf_fock<<<eb, th, 0, st>>>(packed, H, J, K, F);
+    k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, nullptr, d_e, d_dm);
+    CKR(density(F, Fx, Wm));  // the final D stays; Fx takes the unused new density
+    CK(cudaMemcpyAsync(eg.data(), d_e, ng * sizeof(double), cudaMemcpyDeviceToHost, st));
+    const cudaMemcpyKind out = o.jk.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (D_out) CK(cudaMemcpyAsync(D_out, D, bytes, out, st));
+    if (W_out) CK(cudaMemcpyAsync(W_out, Wm, bytes, out, st));
+    CK(cudaStreamSynchronize(st));
+    for (int g = 0; g < ng; ++g) {
+        if (e_elec) e_elec[g] = eg[g];
+        if (e_nuc) {
+            const GeomDev &gm = b->geoms[g];
+            double en = 0.0;
+            for (int a = gm.atom0; a < gm.atom0 + gm.natoms; ++a)
+                for (int c = gm.atom0; c < a; ++c) {
+                    double r2 = 0.0;
+                    for (int x = 0; x < 3; ++x) {
+                        const double d = b->R[3 * a + x] - b->R[3 * c + x];
+                        r2 += d * d;
+                    }
+                    en += (double)b->Z[a] * b->Z[c] / std::sqrt(r2);
+                }
+            e_nuc[g] = en;
+        }
+    }
+    if (iterations) *iterations = it;
+    if (converged) *converged = conv ? 1 : 0;
     return RCHEM_OK;
 }

@@ -112,3 +112,41 @@ def test_batched_gradient_precision_forms(gpu):
     assert np.abs(gem - g64).max() < 1e-10
     assert np.abs(gmx - g64).max() < 1e-7
     bb.close()
+
+
+def test_native_rhf_matches_python_driver(gpu):
+    """rchem_rhf (the SCF loop inside the library) against the Python batched
+    driver: same energies, densities and energy-weighted densities; and the
+    water monomer against the reference-generated STO-3G energy."""
+    import rchem_gb300 as rc
+    from conftest import load_npz
+
+    bb = rc.batch.BatchBasis(_geoms(6, seed=9), "6-31g-fit")
+    rn = rc.batch.rhf_native(bb, thresh_e=1e-12, thresh_d=1e-9)
+    rp = rc.batch.rhf_batch(bb, thresh_e=1e-12, thresh_d=1e-9)
+    assert rn["converged"] and rp["converged"]
+    np.testing.assert_allclose(rn["e_total"], rp["e_total"], atol=1e-9, rtol=0)
+    np.testing.assert_allclose(rn["e_nuc"], rp["e_nuc"], atol=1e-12, rtol=0)
+    assert float((rn["D"] - rp["D"]).abs().max()) < 1e-6
+    assert float((rn["W"] - rp["W"]).abs().max()) < 1e-6
+    # gradients from the native densities equal the Python driver's
+    g_n = np.concatenate(rc.batch.gradient_batch(bb, rn))
+    g_p = np.concatenate(rc.batch.gradient_batch(bb, rp))
+    assert np.abs(g_n - g_p).max() < 1e-6
+    bb.close()
+    g = load_npz("h2o_sto3g")
+    Z, R = rc.geometry.water_monomer()
+    with rc.Basis(Z, R, "sto-3g-fit") as b:
+        r1 = rc.batch.rhf_native(b, thresh_e=1e-12, thresh_d=1e-9)
+    assert r1["converged"]
+    assert abs(r1["e_elec"][0] - float(g["e_elec"])) < 1e-10
+    assert abs(r1["e_nuc"][0] - float(g["e_nuc"])) < 1e-12
+
+
+def test_native_rhf_rejects_large_geometries(gpu):
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config("h2o8_631g")  # 104 functions
+    with rc.Basis(Z, R, bname) as b:
+        with pytest.raises(rc.RchemError):
+            rc.batch.rhf_native(b)
