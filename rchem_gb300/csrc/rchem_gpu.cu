@@ -30,6 +30,7 @@
 #include "grad.cuh"
 #include "scf_batch.cuh"
 #include "md.cuh"
+#include "onee_cls.cuh"
 #include "rchem_types.h"
 
 // ---------------------------------------------------------------------------
@@ -385,13 +386,19 @@ struct rchem_basis_s {
     double gq_tau32 = -1.0;
     double gq_tau = -1.0;
     double *d_W = nullptr, *d_grad = nullptr;
+    // one-electron matrices: shell pairs of every geometry (lower triangle),
+    // grouped by class la*3+lb at [opair_begin[c], opair_begin[c+1])
+    OneePair *d_opairs = nullptr;
+    int opair_begin[10] = {};
+    bool opairs_built = false;
 };
 
 static void free_basis(rchem_basis b) {
     if (!b) return;
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_primsdf, b->d_Ddf, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
                     b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
-                    b->d_shell_atom, b->d_shell_l, b->d_gtasks, b->d_gsegs, b->d_W, b->d_grad, b->d_geom};
+                    b->d_shell_atom, b->d_shell_l, b->d_gtasks, b->d_gsegs, b->d_W, b->d_grad, b->d_geom,
+                    b->d_opairs};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
@@ -1069,10 +1076,69 @@ static int finish_out(rchem_basis b, const double *d_src, double *dst, size_t n,
     return RCHEM_OK;
 }
 
+bool rchem_onee_cls_launch(int kind, const int *begin, const OneePair *pairs, const ShellGrad *sh,
+                           const double *pexp, const double *pcoef, const double *Z, const double *R,
+                           const double *boys, double *out, cudaStream_t st);
+
+// The shell pairs of the one-electron class kernels, built on first use: per
+// geometry every (row shell, column shell) with the row shell's first AO at or
+// after the column shell's, grouped by (l_row, l_col) and, within a class, by
+// primitive-pair count and atom count (lanes of a warp loop alike).
+static int build_onee_pairs(rchem_basis b) {
+    if (b->opairs_built) return RCHEM_OK;
+    std::vector<std::vector<int>> by_geom(b->ngeom);
+    for (int s = 0; s < b->nshells; ++s) by_geom[b->atom_geom[b->shells[s].atom]].push_back(s);
+    std::vector<std::pair<long long, OneePair>> keyed;
+    for (int g = 0; g < b->ngeom; ++g) {
+        const GeomDev &gm = b->geoms[g];
+        for (int s1 : by_geom[g])
+            for (int s2 : by_geom[g]) {
+                const ShellInfo &A = b->shells[s1], &B = b->shells[s2];
+                if (A.ao < B.ao) continue;
+                OneePair o;
+                o.sa = s1;
+                o.sb = s2;
+                o.ra = A.ao - gm.ao0;
+                o.rb = B.ao - gm.ao0;
+                o.moff = gm.moff;
+                o.n = gm.n;
+                o.atom0 = gm.atom0;
+                o.natoms = gm.natoms;
+                const long long cls = A.l * 3 + B.l;
+                const long long cost = (long long)A.nprim * B.nprim * (1 + gm.natoms);
+                keyed.push_back({(cls << 40) - cost, o});
+            }
+    }
+    std::stable_sort(keyed.begin(), keyed.end(),
+                     [](const std::pair<long long, OneePair> &x, const std::pair<long long, OneePair> &y) {
+                         return x.first < y.first;
+                     });
+    std::vector<OneePair> v(keyed.size());
+    int cnt[9] = {};
+    for (size_t i = 0; i < keyed.size(); ++i) {
+        v[i] = keyed[i].second;
+        ++cnt[b->shells[v[i].sa].l * 3 + b->shells[v[i].sb].l];
+    }
+    b->opair_begin[0] = 0;
+    for (int c = 0; c < 9; ++c) b->opair_begin[c + 1] = b->opair_begin[c] + cnt[c];
+    CKR(upload(&b->d_opairs, v, b->stream));
+    b->opairs_built = true;
+    return RCHEM_OK;
+}
+
+// kind: 0 S, 1 T, 2 V, 5 T + V (shell-pair class kernels), 3 moment (element kernel)
 static int onee(rchem_basis b, int kind, const double *center, int ox, int oy, int oz, double *out, int where) {
     if (!b || !out) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     double *dst = (where == RCHEM_DEVICE) ? out : b->d_Jo;
+    if (kind != 3) {
+        CKR(build_onee_pairs(b));
+        if (!rchem_onee_cls_launch(kind, b->opair_begin, b->d_opairs, reinterpret_cast<const ShellGrad *>(b->d_sh),
+                                   b->d_pexp, b->d_pcoef, b->d_Z, b->d_R, b->tabs->boys64, dst, b->stream))
+            return set_err(RCHEM_ERR_INVALID, "one-electron kind %d", kind);
+        CK(cudaGetLastError());
+        return finish_out(b, dst, out, (size_t)b->packed, where);
+    }
     double *d_c = nullptr;
     if (kind == 3) CK(cudaMalloc(&d_c, 3 * sizeof(double)));
     CudaFreeGuard g_c(d_c);
@@ -1825,11 +1891,6 @@ extern "C" int rchem_eigh_batched(int n, int batch, const double *A, double *w, 
 // ---------------------------------------------------------------------------
 // native RHF driver: every geometry of the handle at once (scf_batch.cuh)
 // ---------------------------------------------------------------------------
-__global__ void k_scf_add(long long packed, const double *x, double *y) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < packed) y[i] += x[i];
-}
-
 extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *nocc_in, double *e_elec,
                          double *e_nuc, double *D_out, double *W_out, int *iterations, int *converged) {
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
@@ -1866,7 +1927,7 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     cudaStream_t st = b->stream;
     const size_t bytes = (size_t)packed * sizeof(double);
     // device buffers, freed on every return path
-    enum { S_, H_, X_, T1_, T2_, F_, FX_, D_, DO_, J_, K_, W_, CV_, EPS_, NB_ };
+    enum { S_, H_, X_, T1_, T2_, F_, FX_, D_, DO_, J_, K_, W_, CV_, CV2_, EPS_, NB_ };
     double *buf[NB_] = {};
     CudaFreeList guards;
     for (int k = 0; k < NB_; ++k) {
@@ -1891,26 +1952,31 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     CK(cudaMemcpyAsync(d_nocc, nocc.data(), ng * sizeof(int), cudaMemcpyHostToDevice, st));
     double *S = buf[S_], *H = buf[H_], *X = buf[X_], *T1 = buf[T1_], *T2 = buf[T2_], *F = buf[F_], *Fx = buf[FX_],
            *D = buf[D_], *Dold = buf[DO_], *J = buf[J_], *K = buf[K_], *Wm = buf[W_], *Cv = buf[CV_],
-           *eps = buf[EPS_];
+           *Cn = buf[CV2_], *eps = buf[EPS_];
     const size_t esm = eigh_smem_bytes(nmax);
     CK(cudaFuncSetAttribute(k_scf_eigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esm));
     const int th = RCHEM_SCF_THREADS;
     const unsigned eb = (unsigned)((packed + th - 1) / th);
     const GeomDev *geo = b->d_geom;
     // S, H = T + V, X = S^-1/2 (the eigenvalues go to eps, the vectors to T1)
-    CKR(onee(b, 0, nullptr, 0, 0, 0, S, RCHEM_DEVICE));
-    CKR(onee(b, 1, nullptr, 0, 0, 0, H, RCHEM_DEVICE));
-    CKR(onee(b, 2, nullptr, 0, 0, 0, T2, RCHEM_DEVICE));
-    k_scf_add<<<eb, th, 0, st>>>(packed, T2, H);
+    CKR(onee(b, RCHEM_ONEE_S, nullptr, 0, 0, 0, S, RCHEM_DEVICE));
+    CKR(onee(b, RCHEM_ONEE_H, nullptr, 0, 0, 0, H, RCHEM_DEVICE));
     k_scf_eigh<<<ng, RCHEM_EIGH_THREADS, esm, st>>>(geo, S, eps, T1);
     k_scf_invsqrt<<<ng, th, 0, st>>>(geo, eps, T1, X);
     CK(cudaGetLastError());
-    // F' = X^T F X -> eigenpairs (eps, C' in T1) -> C = X C' (Cv) -> D (and W)
+    // Roothaan step, warm-started: with the previous orbitals C (S-orthonormal;
+    // C = X before the first step) F'' = C^T F C is diagonalised, F'' = V e V^T,
+    // and the new orbitals are C V.  This is X^T F X expressed in the basis of
+    // the previous orbitals, so the eigenpairs are those of the plain step; once
+    // the orbitals settle F'' is nearly diagonal and Jacobi needs 2-3 sweeps
+    // instead of 8-10.  Then D = C_occ C_occ^T (and W).
+    CK(cudaMemcpyAsync(Cv, X, bytes, cudaMemcpyDeviceToDevice, st));
     auto density = [&](const double *Fin, double *Dd, double *Ww) -> int {
-        k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 1, Fin, 0, T1, 1.0, 0.0);
-        k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, X, 0, T2, 1.0, 0.0);
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, Cv, 1, Fin, 0, T1, 1.0, 0.0);
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, Cv, 0, T2, 1.0, 0.0);
         k_scf_eigh<<<ng, RCHEM_EIGH_THREADS, esm, st>>>(geo, T2, eps, T1);
-        k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 0, T1, 0, Cv, 1.0, 0.0);
+        k_scf_gemm<<<ng, th, 0, st>>>(geo, Cv, 0, T1, 0, Cn, 1.0, 0.0);
+        std::swap(Cv, Cn);
         k_scf_density<<<ng, th, 0, st>>>(geo, d_nocc, Cv, eps, Dd, Ww);
         CK(cudaGetLastError());
         return RCHEM_OK;
