@@ -40,6 +40,10 @@ double nuclear_attraction(double x1, double y1, double z1, double norm1, int l1,
                           double x2, double y2, double z2, double norm2, int l2, int m2, int n2, double alpha2,
                           double x3, double y3, double z3);
 
+/* cints.h:72 -- position of (ij|kl) in the 8-fold packed ERI array
+ * (rchem_build_I_packed's layout) */
+int ijkl2intindex(int i, int j, int k, int l);
+
 /* cints.h:69 -- Boys function F_m(x) (exact to ~1e-15 relative; the reference's
  * NR implementation, cints.c:302-373, is accurate to ~1e-7) */
 double Fgamma(double m, double x);

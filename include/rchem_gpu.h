@@ -238,6 +238,15 @@ int rchem_build_I(rchem_basis b, double *I, int where);
 /* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */
 int rchem_jk_inmem(int n, const double *I, const double *D, double *J, double *K, int where);
 
+/* The ERI tensor in the 8-fold packed layout of libpyquante2 (cints.c:375-387,
+ * ijkl2intindex): I[ijkl2intindex(i,j,k,l)] = (ij|kl), npair (npair + 1) / 2
+ * doubles with npair = n (n + 1) / 2 -- an eighth of build_I's n^4, so (H2O)32
+ * in 6-31G* (n = 608, 137 GB) fits in one GB300's memory.  Same integrals as
+ * rchem_build_I; RCHEM_ERR_UNSUPPORTED when the device has no room for it. */
+int rchem_build_I_packed(rchem_basis b, double *I, int where);
+/* J and K (JK_inmem's definitions) from the packed tensor. */
+int rchem_jk_packed(int n, const double *I, const double *D, double *J, double *K, int where);
+
 #ifdef __cplusplus
 }
 #endif

@@ -329,6 +329,27 @@ def JK_inmem(I: np.ndarray, D: np.ndarray):
     return J, K
 
 
+def ijkl2intindex(i, j, k, l):
+    """Packed 8-fold ERI position, restating libpyquante2/cints.c:375-387:
+    order each index pair (larger first), form the pair indices ij, kl, order
+    those, then the pair index of (ij, kl).  Works on numpy integer arrays."""
+    i, j, k, l = (np.asarray(x, dtype=np.int64) for x in (i, j, k, l))
+    ij = np.where(i >= j, i * (i + 1) // 2 + j, j * (j + 1) // 2 + i)
+    kl = np.where(k >= l, k * (k + 1) // 2 + l, l * (l + 1) // 2 + k)
+    return np.where(ij >= kl, ij * (ij + 1) // 2 + kl, kl * (kl + 1) // 2 + ij)
+
+
+def pack_I(I: np.ndarray) -> np.ndarray:
+    """A dense n^4 tensor in the packed layout of ijkl2intindex (each unique
+    integral once; taken from the index quadruple with i >= j, k >= l, ij >= kl)."""
+    n = I.shape[0]
+    npair = n * (n + 1) // 2
+    out = np.zeros(npair * (npair + 1) // 2)
+    i, j, k, l = np.meshgrid(*(np.arange(n),) * 4, indexing="ij")
+    out[ijkl2intindex(i, j, k, l).ravel()] = I.ravel()
+    return out
+
+
 def contracted_eri(b: CGTOBasis, i, j, k, l, lib: Lib | None = None) -> float:
     return port().lib.oq_contracted_eri(*b.args(), _eri_ptr(lib), i, j, k, l)
 

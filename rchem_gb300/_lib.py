@@ -83,6 +83,10 @@ def lib():
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
     L.rchem_jk_inmem.argtypes = [i, vp, vp, vp, vp, i]
+    L.rchem_build_I_packed.argtypes = [vp, vp, i]
+    L.rchem_jk_packed.argtypes = [i, vp, vp, vp, vp, i]
+    L.ijkl2intindex.argtypes = [i, i, i, i]
+    L.ijkl2intindex.restype = i
     L.rchem_eri_prim_batch.argtypes = [i, vp, vp, i]
     L.rchem_onee_prim_batch.argtypes = [i, i, vp, vp, vp, i]
     L.rchem_boys_batch.argtypes = [i, vp, vp, vp, i, i]
@@ -112,7 +116,7 @@ def exported_symbols():
     return [
         "rchem_last_error", "rchem_abi_version", "rchem_basis_create", "rchem_basis_destroy", "rchem_basis_nbf",
         "rchem_basis_set_stream", "rchem_S", "rchem_T", "rchem_V", "rchem_moment", "rchem_jk_direct",
-        "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "coulomb_repulsion", "overlap", "kinetic",
+        "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "rchem_build_I_packed", "rchem_jk_packed", "ijkl2intindex", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
         "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_eigh_batched",

@@ -220,6 +220,49 @@ def build_I(basis: Basis, device=False):
     return out
 
 
+def build_I_packed(basis: Basis, device=False):
+    """The ERI tensor in libpyquante2's 8-fold packed layout: a 1-D array with
+    (ij|kl) at ijkl2intindex(i, j, k, l) (cints.c:375-387)."""
+    n = basis.nbf
+    npair = n * (n + 1) // 2
+    length = npair * (npair + 1) // 2
+    if device:
+        import torch
+
+        out = torch.empty(length, dtype=torch.float64, device="cuda")
+        _after_torch(basis, out)
+    else:
+        out = np.empty(length, dtype=np.float64)
+    _lib.check(_lib.lib().rchem_build_I_packed(basis.handle, C.c_void_p(_ptr(out)),
+                                               _lib.DEVICE if device else _lib.HOST))
+    return out
+
+
+def ijkl2intindex(i, j, k, l):
+    """cints.c:375-387: the packed position of (ij|kl)."""
+    return int(_lib.lib().ijkl2intindex(int(i), int(j), int(k), int(l)))
+
+
+def JK_packed(I, D):
+    """J and K (JK_inmem's definitions) from the packed tensor of build_I_packed."""
+    n = D.shape[0]
+    dev = _is_cuda(D)
+    if dev:
+        import torch
+
+        J = torch.empty((n, n), dtype=torch.float64, device=D.device)
+        K = torch.empty_like(J)
+        I, D = I.contiguous(), D.contiguous()
+    else:
+        I = np.ascontiguousarray(I, dtype=np.float64)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        J = np.empty((n, n))
+        K = np.empty((n, n))
+    _lib.check(_lib.lib().rchem_jk_packed(n, C.c_void_p(_ptr(I)), C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
+                                          C.c_void_p(_ptr(K)), _lib.DEVICE if dev else _lib.HOST))
+    return J, K
+
+
 def JK_inmem(I, D):
     n = D.shape[0]
     dev = _is_cuda(D)

@@ -25,6 +25,34 @@ template <int LA, int LB, int LC, int LD> struct EriClass;
 
 enum { EPI_JK = 0, EPI_STORE = 1, EPI_DIAG = 2 };
 
+// Position of (ij|kl) in the 8-fold packed ERI array (the ordering of
+// libpyquante2/cints.c:375-387): ij = i(i+1)/2 + j with i >= j, kl likewise,
+// then the pair index of (max(ij,kl), min(ij,kl)).  64-bit: n = 608 reaches 1.7e10.
+__host__ __device__ __forceinline__ size_t rchem_eri_pack8(size_t i, size_t j, size_t k, size_t l) {
+    const size_t ij = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+    const size_t kl = k >= l ? k * (k + 1) / 2 + l : l * (l + 1) / 2 + k;
+    return ij >= kl ? ij * (ij + 1) / 2 + kl : kl * (kl + 1) / 2 + ij;
+}
+
+// One contracted integral into the ERI-tensor output: its 8 symmetric
+// positions of the dense n^4 array, or its one packed position.
+__device__ __forceinline__ void eri_put(const EriArgs &a, size_t N1, size_t i, size_t j, size_t k, size_t l,
+                                        double v) {
+    if (a.eri_packed) {
+        a.eri[rchem_eri_pack8(i, j, k, l)] = v;
+        return;
+    }
+    const size_t N2 = N1 * N1, N3 = N2 * N1;
+    a.eri[i * N3 + j * N2 + k * N1 + l] = v;
+    a.eri[j * N3 + i * N2 + k * N1 + l] = v;
+    a.eri[i * N3 + j * N2 + l * N1 + k] = v;
+    a.eri[j * N3 + i * N2 + l * N1 + k] = v;
+    a.eri[k * N3 + l * N2 + i * N1 + j] = v;
+    a.eri[l * N3 + k * N2 + i * N1 + j] = v;
+    a.eri[k * N3 + l * N2 + j * N1 + i] = v;
+    a.eri[l * N3 + k * N2 + j * N1 + i] = v;
+}
+
 template <typename R> struct PrimLoad;
 template <> struct PrimLoad<double> {
     static __device__ __forceinline__ void get(const EriArgs &a, int idx, double &p, double &ohp, double *P,
@@ -180,7 +208,6 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     const int mo = bp.moff;
     if constexpr (EPI == EPI_STORE) {
         if (lead) {
-            const size_t N1 = (size_t)n, N2 = N1 * n, N3 = N2 * n;
 #pragma unroll
             for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -188,18 +215,8 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-                        for (int id = 0; id < ND; ++id) {
-                            const double v = (double)out[IDX(ia, ib, ic, id)];
-                            const size_t i = m0 + ia, j = n0 + ib, k = l0 + ic, l = s0 + id;
-                            a.eri[i * N3 + j * N2 + k * N1 + l] = v;
-                            a.eri[j * N3 + i * N2 + k * N1 + l] = v;
-                            a.eri[i * N3 + j * N2 + l * N1 + k] = v;
-                            a.eri[j * N3 + i * N2 + l * N1 + k] = v;
-                            a.eri[k * N3 + l * N2 + i * N1 + j] = v;
-                            a.eri[l * N3 + k * N2 + i * N1 + j] = v;
-                            a.eri[k * N3 + l * N2 + j * N1 + i] = v;
-                            a.eri[l * N3 + k * N2 + j * N1 + i] = v;
-                        }
+                        for (int id = 0; id < ND; ++id)
+                            eri_put(a, (size_t)n, m0 + ia, n0 + ib, l0 + ic, s0 + id, (double)out[IDX(ia, ib, ic, id)]);
         }
         return;
     }
@@ -493,21 +510,11 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         }
         return;
     }
-    if constexpr (EPI == EPI_STORE) {  // the dense tensor, 8 symmetric positions per integral
-        const size_t N1 = (size_t)bp.mn, N2 = N1 * N1, N3 = N2 * N1;
+    if constexpr (EPI == EPI_STORE) {  // the ERI tensor: dense (8 positions) or packed (one)
         const int i0 = bp.aoA, j0 = bp.aoB, k0 = kp.aoA, l0s = kp.aoB;
         for (int t = lane; t < NA * NB * NC * ND; t += 32) {
             const int id = t % ND, ic = (t / ND) % NC, ib = (t / (ND * NC)) % NB, ia = t / (ND * NC * NB);
-            const double v = (double)A[t];
-            const size_t i = i0 + ia, j = j0 + ib, k = k0 + ic, l = l0s + id;
-            a.eri[i * N3 + j * N2 + k * N1 + l] = v;
-            a.eri[j * N3 + i * N2 + k * N1 + l] = v;
-            a.eri[i * N3 + j * N2 + l * N1 + k] = v;
-            a.eri[j * N3 + i * N2 + l * N1 + k] = v;
-            a.eri[k * N3 + l * N2 + i * N1 + j] = v;
-            a.eri[l * N3 + k * N2 + i * N1 + j] = v;
-            a.eri[k * N3 + l * N2 + j * N1 + i] = v;
-            a.eri[l * N3 + k * N2 + j * N1 + i] = v;
+            eri_put(a, (size_t)bp.mn, i0 + ia, j0 + ib, k0 + ic, l0s + id, (double)A[t]);
         }
         return;
     }

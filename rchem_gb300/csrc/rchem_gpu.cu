@@ -1541,6 +1541,103 @@ extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
     return RCHEM_OK;
 }
 
+// The 8-fold packed tensor: element rchem_eri_pack8(i,j,k,l) holds (ij|kl), one
+// value per unique integral (npair (npair + 1) / 2 of them, npair = n (n + 1) / 2).
+extern "C" int rchem_build_I_packed(rchem_basis b, double *I, int where) {
+    if (!b || !I) return set_err(RCHEM_ERR_INVALID, "null argument");
+    if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
+    if (b->ngeom != 1) return set_err(RCHEM_ERR_UNSUPPORTED, "build_I_packed takes a single-geometry basis");
+    const size_t n = b->nbf, np = n * (n + 1) / 2, len = np * (np + 1) / 2;
+    if (where == RCHEM_HOST) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        if (len * sizeof(double) > fr)
+            return set_err(RCHEM_ERR_UNSUPPORTED, "packed ERI tensor of %zu bytes exceeds the free device memory (%zu)",
+                           len * sizeof(double), fr);
+    }
+    CKR(plan_tasks(b, 0.0, 0.0));  // every quartet, FP64
+    double *d_I = I, *d_tmp = nullptr;
+    if (where == RCHEM_HOST) {
+        CK(cudaMalloc(&d_tmp, len * sizeof(double)));
+        d_I = d_tmp;
+    }
+    CudaFreeGuard g_I(d_tmp);
+    CK(cudaMemsetAsync(d_I, 0, len * sizeof(double), b->stream));
+    EriArgs a = base_args(b);
+    a.eri = d_I;
+    a.eri_packed = 1;
+    CKR(launch_lists(b, a, EPI_STORE, false));
+    if (where == RCHEM_HOST) return finish_out(b, d_I, I, len, RCHEM_HOST);
+    CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
+}
+
+// J and K from the packed tensor, JK_inmem's definitions (src/basis.rs:462-484):
+// J_mn = sum_ls (mn|ls) D_ls, K_mn = sum_ls (ml|ns) D_ls; one warp per m >= n
+__global__ void k_jk_packed(int n, const double *__restrict__ I, const double *__restrict__ D, double *J, double *K) {
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (long long)n * (n + 1) / 2) return;  // whole warps
+    int m = (int)((sqrt(8.0 * (double)w + 1.0) - 1.0) * 0.5);
+    while ((long long)m * (m + 1) / 2 > w) --m;
+    while ((long long)(m + 1) * (m + 2) / 2 <= w) ++m;
+    const int nu = (int)(w - (long long)m * (m + 1) / 2);
+    double j = 0.0, k = 0.0;
+    for (int e = lane; e < n * n; e += 32) {
+        const int l = e / n, s2 = e - l * n;
+        const double d = D[e];
+        j = fma(I[rchem_eri_pack8(m, nu, l, s2)], d, j);
+        k = fma(I[rchem_eri_pack8(m, l, nu, s2)], d, k);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        j += __shfl_xor_sync(0xffffffffu, j, o);
+        k += __shfl_xor_sync(0xffffffffu, k, o);
+    }
+    if (lane == 0) {
+        J[(size_t)m * n + nu] = J[(size_t)nu * n + m] = j;
+        K[(size_t)m * n + nu] = K[(size_t)nu * n + m] = k;
+    }
+}
+
+extern "C" int rchem_jk_packed(int n, const double *I, const double *D, double *J, double *K, int where) {
+    if (n <= 0 || !I || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "bad argument");
+    if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
+    const size_t nn = (size_t)n * n, np = (size_t)n * (n + 1) / 2, len = np * (np + 1) / 2;
+    const double *dI = I, *dD = D;
+    double *dJ = J, *dK = K;
+    CudaFreeList tmp;
+    if (where == RCHEM_HOST) {
+        double *a = nullptr, *d = nullptr, *j = nullptr, *k = nullptr;
+        CK(cudaMalloc(&a, len * sizeof(double)));
+        tmp.p.push_back(a);
+        CK(cudaMalloc(&d, nn * sizeof(double)));
+        tmp.p.push_back(d);
+        CK(cudaMalloc(&j, nn * sizeof(double)));
+        tmp.p.push_back(j);
+        CK(cudaMalloc(&k, nn * sizeof(double)));
+        tmp.p.push_back(k);
+        CK(cudaMemcpy(a, I, len * sizeof(double), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d, D, nn * sizeof(double), cudaMemcpyHostToDevice));
+        dI = a;
+        dD = d;
+        dJ = j;
+        dK = k;
+    }
+    const long long threads = (long long)np * 32;
+    k_jk_packed<<<(unsigned)((threads + 127) / 128), 128>>>(n, dI, dD, dJ, dK);
+    CK(cudaGetLastError());
+    if (where == RCHEM_HOST) {
+        CK(cudaMemcpy(J, dJ, nn * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(K, dK, nn * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        CK(cudaDeviceSynchronize());
+    }
+    return RCHEM_OK;
+}
+
+// libpyquante2/cints.c:375-387 (declared in cints.h:72)
+extern "C" int ijkl2intindex(int i, int j, int k, int l) { return (int)rchem_eri_pack8(i, j, k, l); }
+
 extern "C" int rchem_jk_inmem(int n, const double *I, const double *D, double *J, double *K, int where) {
     if (n <= 0 || !I || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "bad argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);

@@ -96,7 +96,8 @@ struct EriArgs {
     const float2 *Ddf;
     double *J;             // unsymmetrised accumulators (J-hat, K-hat)
     double *K;
-    double *eri;           // dense nbf^4 output (ERI-tensor epilogue)
+    double *eri;           // ERI-tensor epilogue output: dense nbf^4, or packed (eri_packed)
+    int eri_packed;        // 1: one value per unique integral at the 8-fold index (rchem_eri_pack8)
     int wc;                // J/K epilogue of a large class: 1 = warp-cooperative kernel, 0 = one lane group per quartet
 };
 

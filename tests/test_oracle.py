@@ -211,3 +211,33 @@ def test_port_vs_reference_library_random(port):
             assert abs(port.coulomb_repulsion(*args) - sh.coulomb_repulsion(*args)) < 1e-15
         finally:
             port.set_boys(True)
+
+
+def test_packed_index_vs_reference_library(oracle_mod):
+    """The oracle's packed 8-fold index (cints.c:375-387) against the compiled
+    reference's ijkl2intindex where it was built here, and the library's own
+    export (a host function, no GPU call); every permutation of a quadruple
+    lands on one position and distinct unique quadruples on distinct ones."""
+    import ctypes as C
+
+    from rchem_gb300 import _lib, build
+
+    O = oracle_mod
+    n = 9
+    idx = np.array(list(itertools.product(range(n), repeat=4)))
+    pos = O.ijkl2intindex(idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3])
+    for perm in ((1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1), (3, 2, 1, 0)):
+        p2 = O.ijkl2intindex(*(idx[:, q] for q in perm))
+        assert (p2 == pos).all()
+    npair = n * (n + 1) // 2
+    assert sorted(set(pos.tolist())) == list(range(npair * (npair + 1) // 2))
+    build.build()
+    L = _lib.lib()
+    sample = idx[::7]
+    ours = [L.ijkl2intindex(*map(int, q)) for q in sample]
+    assert ours == O.ijkl2intindex(sample[:, 0], sample[:, 1], sample[:, 2], sample[:, 3]).tolist()
+    ref = O.ref("shipped")
+    if ref is not None:
+        f = ref.lib.ijkl2intindex
+        f.argtypes, f.restype = [C.c_int] * 4, C.c_int
+        assert [f(*map(int, q)) for q in sample] == ours
