@@ -171,3 +171,9 @@ def test_invalid_arguments_rejected_without_gpu():
     assert b"not finite" in L.rchem_last_error()
     rc = L.rchem_jk_direct(None, None, None, None, None)
     assert rc == _lib.RCHEM_ERR_INVALID
+    # the native SCF driver, the packed ERI tensor and its J/K: null handles and
+    # bad sizes are refused before any device work
+    assert L.rchem_rhf(None, None, None, None, None, None, None, None, None) == _lib.RCHEM_ERR_INVALID
+    assert L.rchem_build_I_packed(None, None, _lib.HOST) == _lib.RCHEM_ERR_INVALID
+    assert L.rchem_jk_packed(0, None, None, None, None, _lib.HOST) == _lib.RCHEM_ERR_INVALID
+    assert L.rchem_eigh_batched(65, 1, None, None, None, None) == _lib.RCHEM_ERR_UNSUPPORTED
