@@ -8,6 +8,7 @@
 // is sorted by Q, the kets surviving Q_ab Q_cd >= tau for a bra are a prefix
 // of every ket group, found by binary search: no quartet list is ever built.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -71,6 +72,16 @@ struct CudaFreeGuard {
     CudaFreeGuard &operator=(const CudaFreeGuard &) = delete;
 };
 // ... and a list of them
+// NVTX range over one entry point (header-only NVTX v3: a no-op unless a
+// profiler is attached), so a timeline shows each Fock build, gradient, SCF
+// iteration and one-electron matrix.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 struct CudaFreeList {
     std::vector<void *> p;
     ~CudaFreeList() {
@@ -1023,6 +1034,7 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
 extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomnos, const double *coords,
                                   int nshells, const int *shell_atom, const int *shell_l, const int *shell_nprim,
                                   const double *exps, const double *coefs) {
+    NvtxRange nv("rchem_basis_create");
     return create_impl(out, 1, &natoms, natoms, atomnos, coords, nshells, shell_atom, shell_l, shell_nprim, exps,
                        coefs);
 }
@@ -1030,6 +1042,7 @@ extern "C" int rchem_basis_create(rchem_basis *out, int natoms, const int *atomn
 extern "C" int rchem_batch_create(rchem_basis *out, int ngeom, const int *geom_natoms, int natoms, const int *atomnos,
                                   const double *coords, int nshells, const int *shell_atom, const int *shell_l,
                                   const int *shell_nprim, const double *exps, const double *coefs) {
+    NvtxRange nv("rchem_batch_create");
     return create_impl(out, ngeom, geom_natoms, natoms, atomnos, coords, nshells, shell_atom, shell_l, shell_nprim,
                        exps, coefs);
 }
@@ -1128,6 +1141,7 @@ static int build_onee_pairs(rchem_basis b) {
 
 // kind: 0 S, 1 T, 2 V, 5 T + V (shell-pair class kernels), 3 moment (element kernel)
 static int onee(rchem_basis b, int kind, const double *center, int ox, int oy, int oz, double *out, int where) {
+    NvtxRange nv(kind == 0 ? "rchem_S" : kind == 1 ? "rchem_T" : kind == 2 ? "rchem_V" : kind == 3 ? "rchem_moment" : "rchem_H");
     if (!b || !out) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     double *dst = (where == RCHEM_DEVICE) ? out : b->d_Jo;
@@ -1192,6 +1206,7 @@ static int record_build(rchem_basis b, bool any32, bool emul) {
 }
 
 extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts) {
+    NvtxRange nv("rchem_jk_direct");
     if (!b || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "null argument");
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
@@ -1319,6 +1334,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
 }
 extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, double *grad,
                               const rchem_jk_opts *opts) {
+    NvtxRange nv("rchem_gradient");
     if (!b || !D || !W || !grad) return set_err(RCHEM_ERR_INVALID, "null argument");
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
@@ -1427,6 +1443,7 @@ extern "C" int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl) {
 }
 
 extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen) {
+    NvtxRange nv("rchem_autotune");
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
@@ -1520,6 +1537,7 @@ extern "C" int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out) {
 }
 
 extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
+    NvtxRange nv("rchem_build_I");
     if (!b || !I) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     if (b->ngeom != 1) return set_err(RCHEM_ERR_UNSUPPORTED, "build_I takes a single-geometry basis");
@@ -1544,6 +1562,7 @@ extern "C" int rchem_build_I(rchem_basis b, double *I, int where) {
 // The 8-fold packed tensor: element rchem_eri_pack8(i,j,k,l) holds (ij|kl), one
 // value per unique integral (npair (npair + 1) / 2 of them, npair = n (n + 1) / 2).
 extern "C" int rchem_build_I_packed(rchem_basis b, double *I, int where) {
+    NvtxRange nv("rchem_build_I_packed");
     if (!b || !I) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (where != RCHEM_HOST && where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", where);
     if (b->ngeom != 1) return set_err(RCHEM_ERR_UNSUPPORTED, "build_I_packed takes a single-geometry basis");
@@ -1919,6 +1938,7 @@ static int noalloc_scratch(double **out) {
 
 extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J, double *K,
                                        const rchem_jk_opts *opts) {
+    NvtxRange nv("rchem_jk_direct_noalloc");
     if (!b || !D || !J || !K || !opts) return set_err(RCHEM_ERR_INVALID, "null argument");
     if (opts->where != RCHEM_DEVICE)
         return set_err(RCHEM_ERR_INVALID, "rchem_jk_direct_noalloc takes device arrays only (opts->where = RCHEM_DEVICE)");
@@ -1990,6 +2010,7 @@ extern "C" int rchem_eigh_batched(int n, int batch, const double *A, double *w, 
 // ---------------------------------------------------------------------------
 extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *nocc_in, double *e_elec,
                          double *e_nuc, double *D_out, double *W_out, int *iterations, int *converged) {
+    NvtxRange nv("rchem_rhf");
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
     rchem_scf_opts o;
     memset(&o, 0, sizeof(o));
@@ -2085,6 +2106,7 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     int it = 0, nstored = 0, newest = 0;
     bool conv = false;
     for (it = 1; it <= o.max_iter; ++it) {
+        NvtxRange nv_it("scf iteration");
         CKR(rchem_jk_direct(b, D, J, K, &jo));
         k_scf_fock<<<eb, th, 0, st>>>(packed, H, J, K, F);
         k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, nullptr, d_e, d_dm);
