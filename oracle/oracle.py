@@ -1,8 +1,8 @@
 """CPU ORACLE -- test infrastructure only.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
-``bench.py`` import this module, and only as the checker or as the timed CPU
-reference path; the product (``rchem_gb300``) never does.
+``bench.py`` import this module, and only to compare results against or as
+the timed CPU reference path; the product (``rchem_gb300``) never does.
 
 It wraps, through ctypes:
 
