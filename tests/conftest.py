@@ -16,10 +16,21 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running CPU test")
 
 
-@pytest.fixture(scope="session")
-def port():
+def _oracle():
+    """The oracle module.  RCHEM_SANITIZE_PORT names an instrumented (ASan and
+    UBSan) build of oracle/pq2_port.c to load in place of the plain one;
+    tests/test_sanitizers.py runs the oracle tests that way."""
     import oracle
 
+    san = os.environ.get("RCHEM_SANITIZE_PORT")
+    if san:
+        oracle.PORT_SO = san
+    return oracle
+
+
+@pytest.fixture(scope="session")
+def port():
+    oracle = _oracle()
     p = oracle.port()
     p.set_boys(True)
     return p
@@ -27,8 +38,7 @@ def port():
 
 @pytest.fixture(scope="session")
 def oracle_mod():
-    import oracle
-
+    oracle = _oracle()
     oracle.port().set_boys(True)
     return oracle
 

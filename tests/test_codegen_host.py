@@ -40,8 +40,11 @@ def hostlib(tmp_path_factory):
         for c in PROG_CLASSES:
             f.write('#include "%s/eri_prog_%d%d%d%d.inc"\n' % ((str(gen),) + c))
     so = d / "libhost.so"
-    subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", CSRC, "-I", str(d), "-o", str(so),
-                    os.path.join(ROOT, "tests", "host_eri_check.cpp")], check=True)
+    # RCHEM_SANITIZE_FLAGS: extra compiler flags (tests/test_sanitizers.py passes ASan/UBSan ones)
+    extra = os.environ.get("RCHEM_SANITIZE_FLAGS", "").split()
+    env = {k: v for k, v in os.environ.items() if k != "LD_PRELOAD"}  # the compiler itself runs uninstrumented
+    subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", *extra, "-I", CSRC, "-I", str(d), "-o",
+                    str(so), os.path.join(ROOT, "tests", "host_eri_check.cpp")], check=True, env=env)
     L = C.CDLL(str(so))
     L.host_eri_block.argtypes = [C.c_int] * 5 + [C.c_void_p] * 5
     L.host_eri_block_prog.argtypes = [C.c_int] * 4 + [C.c_void_p] * 5
