@@ -129,10 +129,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True):
+def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True, target_s=10.0):
     """The reference's JK_direct loops (2 THO ERIs per primitive quartet) on a
     seeded sample of J/K elements, all host threads; returns builds/s
-    extrapolated to the n^2 elements of a build, threads and sample size."""
+    extrapolated to the n^2 elements of a build, threads and sample size.
+    ``sample`` = 0 sizes the sample from a one-element-per-thread pilot so
+    that each step takes about ``target_s`` seconds."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -147,7 +149,13 @@ def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True):
     rng = np.random.default_rng(17)
     X = rng.normal(size=(n, n))
     D = X @ X.T / n
-    m = sample or max(threads, 2 * threads)
+    m = sample
+    if not m:
+        pm, pn = rng.integers(0, n, threads), rng.integers(0, n, threads)
+        t0 = time.perf_counter()
+        O.JK_direct_elements(ob, D, pm, pn)
+        per_round = max(time.perf_counter() - t0, 1e-6)  # one element on every thread
+        m = threads * int(min(max(1, round(target_s / per_round)), 4096))
     rates = []
     for s in range(steps):
         mus = rng.integers(0, n, m)
@@ -319,8 +327,10 @@ def run_reference(a):
     import oracle as O
 
     O.build_port()
-    cpu_reference_rate(a.workload, a.cpu_sample, steps=max(1, min(a.warmup, 1)))  # warm-up
-    rates, threads, m, n = cpu_reference_rate(a.workload, a.cpu_sample, steps=steps)
+    # each step about 8 s of CPU work, the whole run (steps + one warm-up) within about 2.5 minutes
+    target = min(8.0, 150.0 / (steps + 1))
+    cpu_reference_rate(a.workload, a.cpu_sample or 0, steps=1, target_s=0.2 * target)  # warm-up
+    rates, threads, m, n = cpu_reference_rate(a.workload, a.cpu_sample, steps=steps, target_s=target)
     value = float(np.mean(rates))
     sample = ("%d J/K elements per step (seeded random (mu,nu)) of the %d x %d Fock matrix by the JK_direct loops "
               "(src/basis.rs:392-425), THO ERIs with the Numerical-Recipes Boys function as shipped; "
