@@ -137,6 +137,8 @@ int rchem_jk_class_stats(rchem_basis b, int *class_l, long long *quartets, long 
  * steady-state loop must never allocate.
  *  - D, J and K are device arrays (opts->where must be RCHEM_DEVICE); opts is
  *    required.  Results equal rchem_jk_direct's up to summation order.
+ *    opts->emulated is not honoured: quartets above fp32_tau always run in
+ *    native FP64 here.
  *  - The scratch (J-hat, K-hat, the FP32 copy of D) is a static device array
  *    inside the library sized for at most 640 basis functions (about 8 MiB,
  *    held by every GPU that loads the library until the process exits);
