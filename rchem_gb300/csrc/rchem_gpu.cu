@@ -863,8 +863,40 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
         }
         if (tot != natoms) return set_err(RCHEM_ERR_INVALID, "geometry atom counts sum to %lld, not %d", tot, natoms);
     }
+    // Every shell is checked here, on the host, before any CUDA call or
+    // allocation (the same checks, in the same order, as the set-up loop below).
+    {
+        std::vector<int> atom_geom(natoms, 0);
+        for (int g = 0, a0 = 0; g < ngeom; a0 += geom_natoms[g], ++g)
+            for (int k = 0; k < geom_natoms[g]; ++k) atom_geom[a0 + k] = g;
+        long long pos = 0;
+        int gprev = 0;
+        for (int s = 0; s < nshells; ++s) {
+            const int l = shell_l[s], np = shell_nprim[s], at = shell_atom[s];
+            if (at >= 0 && at < natoms) {
+                if (atom_geom[at] < gprev)
+                    return set_err(RCHEM_ERR_INVALID, "shell %d: shells must come in geometry order", s);
+                gprev = atom_geom[at];
+            }
+            if (l < 0 || l > RCHEM_MAX_L)
+                return set_err(RCHEM_ERR_UNSUPPORTED, "shell %d has l=%d (supported: 0..%d)", s, l, RCHEM_MAX_L);
+            if (np < 1 || np > RCHEM_MAX_NPRIM)
+                return set_err(RCHEM_ERR_UNSUPPORTED, "shell %d has %d primitives (supported: 1..%d)", s, np,
+                               RCHEM_MAX_NPRIM);
+            if (at < 0 || at >= natoms) return set_err(RCHEM_ERR_INVALID, "shell %d on atom %d of %d", s, at, natoms);
+            for (int k = 0; k < np; ++k) {
+                const double e = exps[pos + k], c = coefs[pos + k];
+                if (!(e > 0.0) || !std::isfinite(e) || !std::isfinite(c))
+                    return set_err(RCHEM_ERR_INVALID, "shell %d primitive %d: exponent %g coefficient %g", s, k, e,
+                                   c);
+            }
+            pos += np;
+        }
+    }
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
     rchem_basis b = new rchem_basis_s();
-    CK(cudaGetDevice(&b->dev));
+    b->dev = dev;
     for (int k = 0; k < RCHEM_NCLASS; ++k) {
         b->ppl[k][0] = b->ppl[k][1] = kMinPrimPerLane;
         b->wc[k][0] = b->wc[k][1] = 0;

@@ -177,3 +177,60 @@ def test_invalid_arguments_rejected_without_gpu():
     assert L.rchem_build_I_packed(None, None, _lib.HOST) == _lib.RCHEM_ERR_INVALID
     assert L.rchem_jk_packed(0, None, None, None, None, _lib.HOST) == _lib.RCHEM_ERR_INVALID
     assert L.rchem_eigh_batched(65, 1, None, None, None, None) == _lib.RCHEM_ERR_UNSUPPORTED
+
+
+def test_shell_validation_before_any_device_call():
+    """Every shell is validated on the host before the library touches CUDA:
+    unsupported angular momenta and primitive counts, bad exponents or
+    coefficients, shells on atoms that do not exist, and (for a batch) shells
+    out of geometry order are refused with a status code and a message.  On a
+    host without a GPU each of these calls returns before any CUDA call."""
+    import ctypes as C
+
+    from rchem_gb300 import _lib, build
+
+    build.build()
+    L = _lib.lib()
+    i32 = lambda *v: np.array(v, np.int32)  # noqa: E731
+    f64 = lambda *v: np.array(v, np.float64)  # noqa: E731
+    Z = i32(8, 1)
+    R = f64(0.0, 0.0, 0.0, 0.0, 0.0, 1.8)
+
+    def create(atom, l, nprim, exps, coefs):
+        h = C.c_void_p()
+        atom, l, nprim = i32(*atom), i32(*l), i32(*nprim)
+        exps, coefs = f64(*exps), f64(*coefs)
+        rc = L.rchem_basis_create(C.byref(h), 2, Z.ctypes.data, R.ctypes.data, len(atom), atom.ctypes.data,
+                                  l.ctypes.data, nprim.ctypes.data, exps.ctypes.data, coefs.ctypes.data)
+        assert not h.value  # no handle on failure
+        return rc, L.rchem_last_error().decode()
+
+    rc, msg = create([0, 1], [3, 0], [1, 1], [1.0, 0.5], [1.0, 1.0])  # f shell
+    assert rc == _lib.RCHEM_ERR_UNSUPPORTED and "l=3" in msg
+    rc, msg = create([0, 1], [-1, 0], [1, 1], [1.0, 0.5], [1.0, 1.0])
+    assert rc == _lib.RCHEM_ERR_UNSUPPORTED and "l=-1" in msg
+    rc, msg = create([0, 1], [0, 0], [1, 0], [1.0], [1.0])  # a shell without primitives
+    assert rc == _lib.RCHEM_ERR_UNSUPPORTED and "shell 1 has 0 primitives" in msg
+    rc, msg = create([0], [0], [17], [1.0] * 17, [1.0] * 17)  # more primitives than the kernels hold
+    assert rc == _lib.RCHEM_ERR_UNSUPPORTED and "17 primitives" in msg
+    rc, msg = create([0, 2], [0, 0], [1, 1], [1.0, 0.5], [1.0, 1.0])  # atom 2 of 2
+    assert rc == _lib.RCHEM_ERR_INVALID and "on atom 2 of 2" in msg
+    rc, msg = create([0, 1], [0, 0], [2, 1], [1.0, -0.5, 0.5], [1.0, 1.0, 1.0])  # negative exponent
+    assert rc == _lib.RCHEM_ERR_INVALID and "shell 0 primitive 1" in msg
+    rc, msg = create([0, 1], [0, 1], [1, 1], [1.0, 0.5], [1.0, np.inf])  # non-finite coefficient
+    assert rc == _lib.RCHEM_ERR_INVALID and "shell 1 primitive 0" in msg
+    rc, msg = create([0, 1], [0, 0], [1, 1], [1.0, np.nan], [1.0, 1.0])
+    assert rc == _lib.RCHEM_ERR_INVALID and "shell 1 primitive 0" in msg
+
+    # a batch: two one-atom geometries whose shells come in the wrong order
+    h = C.c_void_p()
+    gn, atom, l, npr = i32(1, 1), i32(1, 0), i32(0, 0), i32(1, 1)
+    e = f64(1.0, 1.0)
+    rc = L.rchem_batch_create(C.byref(h), 2, gn.ctypes.data, 2, Z.ctypes.data, R.ctypes.data, 2, atom.ctypes.data,
+                              l.ctypes.data, npr.ctypes.data, e.ctypes.data, e.ctypes.data)
+    assert rc == _lib.RCHEM_ERR_INVALID and b"geometry order" in L.rchem_last_error()
+    # geometry atom counts that do not add up to the atoms given
+    gn = i32(1, 2)
+    rc = L.rchem_batch_create(C.byref(h), 2, gn.ctypes.data, 2, Z.ctypes.data, R.ctypes.data, 2, atom.ctypes.data,
+                              l.ctypes.data, npr.ctypes.data, e.ctypes.data, e.ctypes.data)
+    assert rc == _lib.RCHEM_ERR_INVALID and b"sum to 3, not 2" in L.rchem_last_error()
