@@ -38,6 +38,37 @@ def _ptr(x):
     return x.ctypes.data
 
 
+def _check_f64(X, name, shape=None, numel=None):
+    """Refuse, before any library call, an array the library would read or
+    write as a dense row-major float64 block of another size or type: a
+    C-contiguous float64 numpy array or a contiguous float64 CUDA tensor with
+    the given shape (or number of elements)."""
+    shp = tuple(int(d) for d in X.shape)
+    if shape is not None and shp != tuple(shape):
+        raise ValueError("%s: expected shape %s, got %s" % (name, tuple(shape), shp))
+    if numel is not None and int(np.prod(shp, dtype=np.int64)) != numel:
+        raise ValueError("%s: expected %d elements, got %d (shape %s)" % (name, numel, int(np.prod(shp)), shp))
+    if _is_cuda(X):
+        import torch
+
+        if X.dtype != torch.float64:
+            raise ValueError("%s must be a float64 tensor, got %s" % (name, X.dtype))
+        if not X.is_contiguous():
+            raise ValueError("%s must be a contiguous tensor" % name)
+    elif not (isinstance(X, np.ndarray) and X.dtype == np.float64 and X.flags.c_contiguous):
+        raise ValueError("%s must be a C-contiguous float64 numpy array or a CUDA tensor" % name)
+
+
+def _same_kind(*xs):
+    """All host arrays or all CUDA tensors on one device; True for CUDA."""
+    dev = _is_cuda(xs[0])
+    if any(_is_cuda(x) != dev for x in xs):
+        raise ValueError("arrays must all be host arrays or all CUDA tensors")
+    if dev and len({str(x.device) for x in xs}) != 1:
+        raise ValueError("CUDA tensors must be on one device")
+    return dev
+
+
 def _after_torch(basis, *xs):
     """The library queues its work on the handle's own stream.  When CUDA
     tensors are passed, work still queued on torch's current stream (producing
@@ -186,20 +217,11 @@ def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=F
     """Fill J and K (in place, like the reference) from the density D.
     ``fp32_tau`` > 0 selects the mixed form; ``emulated`` computes the FP64
     quartets in double-float arithmetic on the FP32 pipe."""
-    dev = _is_cuda(D)
-    if dev != _is_cuda(J) or dev != _is_cuda(K):
-        raise ValueError("D, J and K must all be host arrays or all CUDA tensors")
-    if not dev:
-        D = np.ascontiguousarray(D, dtype=np.float64)
-        for X in (J, K):
-            if not (isinstance(X, np.ndarray) and X.dtype == np.float64 and X.flags.c_contiguous):
-                raise ValueError("J and K must be C-contiguous float64 arrays")
-    else:
-        D = D.contiguous()
+    dev = _same_kind(D, J, K)
+    D = D.contiguous() if dev else np.ascontiguousarray(D, dtype=np.float64)
     n = basis.nbf
-    for X in (D, J, K):
-        if tuple(X.shape) != (n, n):
-            raise ValueError("expected %dx%d matrices" % (n, n))
+    for X, name in ((D, "D"), (J, "J"), (K, "K")):
+        _check_f64(X, name, shape=(n, n))
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
                     where=_lib.DEVICE if dev else _lib.HOST, emulated=1 if emulated else 0)
     _after_torch(basis, D, J, K)
@@ -243,40 +265,40 @@ def ijkl2intindex(i, j, k, l):
     return int(_lib.lib().ijkl2intindex(int(i), int(j), int(k), int(l)))
 
 
-def JK_packed(I, D):
-    """J and K (JK_inmem's definitions) from the packed tensor of build_I_packed."""
-    n = D.shape[0]
-    dev = _is_cuda(D)
+def _jk_tensor_args(I, D, numel_of_n):
+    """Checked (I, D, J, K, n, dev) for the tensor-based J/K entry points."""
+    dev = _same_kind(I, D)
+    if len(D.shape) != 2 or D.shape[0] != D.shape[1] or D.shape[0] < 1:
+        raise ValueError("D must be a square matrix, got shape %s" % (tuple(D.shape),))
+    n = int(D.shape[0])
+    if dev:
+        I, D = I.contiguous(), D.contiguous()
+    else:
+        I = np.ascontiguousarray(I, dtype=np.float64)
+        D = np.ascontiguousarray(D, dtype=np.float64)
+    _check_f64(D, "D", shape=(n, n))
+    _check_f64(I, "I", numel=numel_of_n(n))
     if dev:
         import torch
 
         J = torch.empty((n, n), dtype=torch.float64, device=D.device)
         K = torch.empty_like(J)
-        I, D = I.contiguous(), D.contiguous()
     else:
-        I = np.ascontiguousarray(I, dtype=np.float64)
-        D = np.ascontiguousarray(D, dtype=np.float64)
-        J = np.empty((n, n))
-        K = np.empty((n, n))
+        J, K = np.empty((n, n)), np.empty((n, n))
+    return I, D, J, K, n, dev
+
+
+def JK_packed(I, D):
+    """J and K (JK_inmem's definitions) from the packed tensor of build_I_packed."""
+    I, D, J, K, n, dev = _jk_tensor_args(I, D, lambda n: (n * (n + 1) // 2) * (n * (n + 1) // 2 + 1) // 2)
     _lib.check(_lib.lib().rchem_jk_packed(n, C.c_void_p(_ptr(I)), C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
                                           C.c_void_p(_ptr(K)), _lib.DEVICE if dev else _lib.HOST))
     return J, K
 
 
 def JK_inmem(I, D):
-    n = D.shape[0]
-    dev = _is_cuda(D)
-    if dev:
-        import torch
-
-        J = torch.empty((n, n), dtype=torch.float64, device=D.device)
-        K = torch.empty_like(J)
-        I, D = I.contiguous(), D.contiguous()
-    else:
-        I = np.ascontiguousarray(I, dtype=np.float64)
-        D = np.ascontiguousarray(D, dtype=np.float64)
-        J = np.empty((n, n))
-        K = np.empty((n, n))
+    """J and K from the dense n^4 tensor of build_I (src/basis.rs:462-484)."""
+    I, D, J, K, n, dev = _jk_tensor_args(I, D, lambda n: n ** 4)
     _lib.check(_lib.lib().rchem_jk_inmem(n, C.c_void_p(_ptr(I)), C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
                                          C.c_void_p(_ptr(K)), _lib.DEVICE if dev else _lib.HOST))
     return J, K

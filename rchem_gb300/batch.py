@@ -18,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from .basis import Basis, _after_torch
+from .basis import Basis, _after_torch, _check_f64, _same_kind
 from .bse import expand_shells, load_bse
 
 
@@ -109,6 +109,10 @@ def eigh(A):
 
 def jk(bb: BatchBasis, D, J, K, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
     """One Fock build over every geometry: packed device vectors D -> J, K."""
+    if not _same_kind(D, J, K):
+        raise ValueError("D, J and K must be CUDA tensors")
+    for X, name in ((D, "D"), (J, "J"), (K, "K")):
+        _check_f64(X, name, numel=bb.packed)
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
                     emulated=1 if emulated else 0)
     _after_torch(bb, D, J, K)

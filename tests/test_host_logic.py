@@ -234,3 +234,125 @@ def test_shell_validation_before_any_device_call():
     rc = L.rchem_batch_create(C.byref(h), 2, gn.ctypes.data, 2, Z.ctypes.data, R.ctypes.data, 2, atom.ctypes.data,
                               l.ctypes.data, npr.ctypes.data, e.ctypes.data, e.ctypes.data)
     assert rc == _lib.RCHEM_ERR_INVALID and b"sum to 3, not 2" in L.rchem_last_error()
+
+
+class _FakeCuda:
+    """Stands in for a CUDA tensor in the wrappers' argument checks (no GPU here)."""
+
+    is_cuda = True
+
+    def __init__(self, shape, dtype=None, contiguous=True, device="cuda:0"):
+        import torch
+
+        self.shape = shape
+        self.dtype = dtype or torch.float64
+        self._c = contiguous
+        self.device = device
+
+    def is_contiguous(self):
+        return self._c
+
+    def contiguous(self):
+        return _FakeCuda(self.shape, self.dtype, True, self.device)
+
+
+def test_wrappers_refuse_mis_sized_or_mis_typed_arrays():
+    """The Python mirror of the basis API checks every array's shape, type and
+    layout before the library would read or write it as a dense float64 block;
+    these all raise before any library call, so they run without a GPU."""
+    import types
+
+    import torch
+
+    import rchem_gb300 as rc
+    from rchem_gb300 import batch
+
+    n = 7
+    b = types.SimpleNamespace(nbf=n)  # only nbf is read before the checks
+    ok = np.zeros((n, n))
+    with pytest.raises(ValueError, match="J must be a C-contiguous float64"):
+        rc.JK_direct(np.zeros((n, n), np.float32), ok, b, ok)
+    with pytest.raises(ValueError, match="K must be a C-contiguous float64"):
+        rc.JK_direct(ok, np.asfortranarray(np.zeros((n, n))), b, ok)
+    with pytest.raises(ValueError, match=r"K: expected shape \(7, 7\), got \(8, 7\)"):
+        rc.JK_direct(ok, np.zeros((n + 1, n)), b, ok)
+    with pytest.raises(ValueError, match="D: expected shape"):
+        rc.JK_direct(ok, ok, b, np.zeros((n, n + 1)))
+    with pytest.raises(ValueError, match="all be host arrays or all CUDA"):
+        rc.JK_direct(_FakeCuda((n, n)), ok, b, ok)
+    with pytest.raises(ValueError, match="float64 tensor"):
+        rc.JK_direct(_FakeCuda((n, n), torch.float32), _FakeCuda((n, n)), b, _FakeCuda((n, n)))
+    with pytest.raises(ValueError, match="contiguous tensor"):
+        rc.JK_direct(_FakeCuda((n, n), contiguous=False), _FakeCuda((n, n)), b, _FakeCuda((n, n)))
+    with pytest.raises(ValueError, match="one device"):
+        rc.JK_direct(_FakeCuda((n, n)), _FakeCuda((n, n), device="cuda:1"), b, _FakeCuda((n, n)))
+
+    # the tensor-based J/K: I must hold n^4 (dense) or the packed count of elements
+    npair = n * (n + 1) // 2
+    with pytest.raises(ValueError, match="I: expected 2401 elements"):
+        rc.JK_inmem(np.zeros(n ** 4 - 1), ok)
+    with pytest.raises(ValueError, match="I: expected %d elements" % (npair * (npair + 1) // 2)):
+        rc.JK_packed(np.zeros(n ** 4), ok)
+    with pytest.raises(ValueError, match="square matrix"):
+        rc.JK_inmem(np.zeros(n ** 4), np.zeros((n, n - 1)))
+    with pytest.raises(ValueError, match="float64 tensor"):
+        rc.JK_inmem(_FakeCuda((n ** 4,), torch.float32), _FakeCuda((n, n)))
+
+    # the batched Fock build: packed device vectors of the handle's length
+    bb = types.SimpleNamespace(packed=100)
+    with pytest.raises(ValueError, match="must be CUDA tensors"):
+        batch.jk(bb, np.zeros(100), np.zeros(100), np.zeros(100))
+    with pytest.raises(ValueError, match="J: expected 100 elements"):
+        batch.jk(bb, _FakeCuda((100,)), _FakeCuda((99,)), _FakeCuda((100,)))
+
+
+def test_wrappers_pass_valid_arrays_through(monkeypatch):
+    """Valid host arrays reach the C ABI unchanged: the wrappers pass the
+    arrays' own buffers (no copies of C-contiguous float64 input), the size,
+    the host/device flag and the options, here recorded by a stand-in for the
+    loaded library."""
+    import ctypes as C
+    import types
+
+    import rchem_gb300 as rc
+    from rchem_gb300 import _lib
+
+    calls = []
+
+    class Recorder:
+        def __getattr__(self, name):
+            def f(*args):
+                calls.append((name, args))
+                return 0
+
+            return f
+
+    monkeypatch.setattr(_lib, "lib", lambda: Recorder())
+    n = 5
+    b = types.SimpleNamespace(nbf=n, handle="handle")
+    D = np.eye(n)
+    J, K = np.zeros((n, n)), np.zeros((n, n))
+    rc.JK_direct(J, K, b, D, schwarz_tau=1e-10, fp32_tau=1e-6, emulated=True)
+    name, a = calls[-1]
+    assert name == "rchem_jk_direct" and a[0] == "handle"
+    assert [x.value for x in a[1:4]] == [D.ctypes.data, J.ctypes.data, K.ctypes.data]
+    o = a[4]._obj
+    assert (o.schwarz_tau, o.fp32_tau, o.where, o.emulated) == (1e-10, 1e-6, _lib.HOST, 1)
+    rc.JK_direct(J, K, b, D, schwarz_tau=0.0)  # no screening is passed as a negative threshold
+    assert calls[-1][1][4]._obj.schwarz_tau < 0 and calls[-1][1][4]._obj.emulated == 0
+
+    I = np.zeros(n ** 4)
+    Ji, Ki = rc.JK_inmem(I, D)
+    name, a = calls[-1]
+    assert name == "rchem_jk_inmem" and a[0] == n and a[5] == _lib.HOST
+    assert [x.value for x in a[1:5]] == [I.ctypes.data, D.ctypes.data, Ji.ctypes.data, Ki.ctypes.data]
+    npair = n * (n + 1) // 2
+    Ip = np.zeros(npair * (npair + 1) // 2)
+    Jp, Kp = rc.JK_packed(Ip, D)
+    name, a = calls[-1]
+    assert name == "rchem_jk_packed" and a[0] == n and a[1].value == Ip.ctypes.data
+    assert Jp.shape == Kp.shape == (n, n)
+    # a float32 or strided density is converted on the host, not refused
+    rc.JK_direct(J, K, b, np.eye(n, dtype=np.float32))
+    rc.JK_direct(J, K, b, np.eye(2 * n)[::2, ::2])
+    assert isinstance(calls[-1][1][1], C.c_void_p)
