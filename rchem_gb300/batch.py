@@ -291,6 +291,10 @@ def gradient_batch(bb: BatchBasis, res: dict, schwarz_tau=1e-12, fp32_tau=0.0, e
     (precision options as in scf.gradient); returns a list of (natoms_g x 3) arrays."""
     import torch
 
+    if not _same_kind(res["D"], res["W"]):
+        raise ValueError("D and W must be CUDA tensors")
+    for key in ("D", "W"):
+        _check_f64(res[key], key, numel=bb.packed)
     g = torch.empty(3 * len(bb.atomnos), dtype=torch.float64, device="cuda")
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
                     emulated=1 if emulated else 0)

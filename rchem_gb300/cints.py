@@ -36,8 +36,10 @@ def fgamma(m, x) -> float:
 
 
 def boys_batch(m, x, precision=64) -> np.ndarray:
-    m = np.ascontiguousarray(m, dtype=np.int32)
-    x = np.ascontiguousarray(x, dtype=np.float64)
+    m = np.ascontiguousarray(m, dtype=np.int32).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+    if m.size != x.size:
+        raise ValueError("m and x must have the same length (%d != %d)" % (m.size, x.size))
     out = np.empty(len(m))
     _lib.check(_lib.lib().rchem_boys_batch(len(m), m.ctypes.data, x.ctypes.data, out.ctypes.data, precision,
                                            _lib.HOST))

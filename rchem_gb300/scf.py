@@ -126,8 +126,13 @@ def gradient(basis: _b.Basis, res: dict | None = None, schwarz_tau: float = 1e-1
 
     if res is None:
         res = rhf(basis, schwarz_tau=schwarz_tau, **scf_kw)
+    if not _b._same_kind(res["D"], res["W"]):
+        raise ValueError("D and W must be CUDA tensors")
     D = res["D"].contiguous()
     W = res["W"].contiguous()
+    n = basis.nbf
+    _b._check_f64(D, "D", shape=(n, n))
+    _b._check_f64(W, "W", shape=(n, n))
     g = torch.empty(3 * len(basis.atomnos), dtype=torch.float64, device=D.device)
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau, where=_lib.DEVICE,
                     emulated=1 if emulated else 0)

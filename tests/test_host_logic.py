@@ -356,3 +356,28 @@ def test_wrappers_pass_valid_arrays_through(monkeypatch):
     rc.JK_direct(J, K, b, np.eye(n, dtype=np.float32))
     rc.JK_direct(J, K, b, np.eye(2 * n)[::2, ::2])
     assert isinstance(calls[-1][1][1], C.c_void_p)
+
+
+def test_gradient_and_boys_wrappers_refuse_bad_arrays():
+    """The gradient wrappers check the density and energy-weighted density they
+    are given (a result dict may come from the caller); the Boys batch needs
+    as many orders as arguments."""
+    import types
+
+    import torch
+
+    import rchem_gb300 as rc
+    from rchem_gb300 import batch, cints
+
+    b = types.SimpleNamespace(nbf=4, atomnos=np.array([1, 1]))
+    with pytest.raises(ValueError, match="W: expected shape"):
+        rc.scf.gradient(b, {"D": _FakeCuda((4, 4)), "W": _FakeCuda((5, 5))})
+    with pytest.raises(ValueError, match="D and W must be CUDA tensors"):
+        rc.scf.gradient(b, {"D": np.zeros((4, 4)), "W": np.zeros((4, 4))})
+    with pytest.raises(ValueError, match="all be host arrays or all CUDA tensors"):
+        rc.scf.gradient(b, {"D": _FakeCuda((4, 4)), "W": np.zeros((4, 4))})
+    bb = types.SimpleNamespace(packed=32, atomnos=np.array([1, 1]))
+    with pytest.raises(ValueError, match="float64 tensor"):
+        batch.gradient_batch(bb, {"D": _FakeCuda((32,)), "W": _FakeCuda((32,), torch.float32)})
+    with pytest.raises(ValueError, match="same length"):
+        cints.boys_batch([0, 1, 2], [0.5, 1.0])
