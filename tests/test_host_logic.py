@@ -381,3 +381,21 @@ def test_gradient_and_boys_wrappers_refuse_bad_arrays():
         batch.gradient_batch(bb, {"D": _FakeCuda((32,)), "W": _FakeCuda((32,), torch.float32)})
     with pytest.raises(ValueError, match="same length"):
         cints.boys_batch([0, 1, 2], [0.5, 1.0])
+
+
+def test_c_consumer_links_and_calls_the_abi(tmp_path):
+    """A plain C99 program (tests/abi_check.c) includes the public headers in
+    strict C mode, links librchem_gpu.so and calls the entry points that need
+    no GPU: the headers are valid C for a bindgen/FFI consumer and the
+    exported symbols have C linkage."""
+    from rchem_gb300 import _lib, build
+
+    build.build()
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = tmp_path / "abi_check"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_check.c"), "-o", str(exe), "-L", libdir, "-lrchem_gpu",
+                    "-Wl,-rpath," + libdir], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "abi_check: ok" in r.stdout
