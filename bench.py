@@ -15,6 +15,11 @@ in to the copies of J and K out, so host submission latency is excluded); a
 and K inside the timed region).  The mixed FP32/FP64 form is reported under
 ``forms``.
 
+CPU baselines (rank 0, N=1): ``cpu_baseline`` is the reference's algorithm
+on a bounded sample, as below; ``cpu_baseline_strong`` is a whole build by a
+strong CPU code over the same integrals (8-fold symmetry, Schwarz screen,
+OpenMP), with a one-core figure from a strided sample of the bra pairs.
+
 --impl reference: the reference's algorithm (src/basis.rs:383-428 loops over
 the THO integrals of libpyquante2/cints.c with its own Boys function), run by
 the CPU oracle with all host threads on a bounded sample of J/K elements and
@@ -166,6 +171,60 @@ def cpu_reference_rate(workload, sample, steps=1, boys_shipped=True, target_s=10
         rates.append(m / (dt * n * n))
     port.set_boys(True)
     return rates, threads, m, n
+
+
+def cpu_strong_rate(workload, D, J_ref=None, K_ref=None, tau=1e-12, target_1core_s=4.0):
+    """A strong CPU Fock build with the reference's own integrals (THO ERIs,
+    the shipped Boys function): each unique contracted integral once (8-fold
+    symmetry), quartets with Q_ij Q_kl < tau skipped like the GPU build,
+    OpenMP over all host threads.  All cores: one whole build timed.  One core:
+    a strided subset of the bra pairs timed and extrapolated by the number of
+    integrals that pass the screen."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    import rchem_gb300 as rc
+
+    bname, Z, R = rc.geometry.config(workload)
+    ob = O.expand_basis(Z, R, rc.load_bse(bname))
+    port = O.port()
+    port.set_boys(False)
+    try:
+        threads = port.num_threads()
+        n = ob.n
+        npair = n * (n + 1) // 2
+        t0 = time.perf_counter()
+        Q = O.schwarz(ob)
+        t_q = time.perf_counter() - t0
+        total = O.JK_sym_screened(ob, D, Q, tau, count_only=True)[2]
+        t0 = time.perf_counter()
+        J, K, cnt = O.JK_sym_screened(ob, D, Q, tau)
+        t_all = time.perf_counter() - t0
+        # one core: a pilot over every 97th bra pair sizes a strided sample of about target_1core_s
+        pilot = np.arange(0, npair, 97)
+        t0 = time.perf_counter()
+        c_p = O.JK_sym_screened(ob, D, Q, tau, pairs=pilot, nthreads=1)[2]
+        per_int = (time.perf_counter() - t0) / max(c_p, 1)
+        stride = int(min(max(1, round(total * per_int / target_1core_s)), npair))
+        sample = np.arange(stride // 2, npair, stride)
+        t0 = time.perf_counter()
+        c_1 = O.JK_sym_screened(ob, D, Q, tau, pairs=sample, nthreads=1)[2]
+        t_1 = time.perf_counter() - t0
+    finally:
+        port.set_boys(True)
+    out = {"value": 1.0 / t_all, "unit": "builds/s", "cores": threads, "kind": "port",
+           "algorithm": "each unique contracted integral once (8-fold symmetry), Schwarz screen Q_ij Q_kl >= %g "
+                        "over contracted functions, THO ERIs of libpyquante2/cints.c with the shipped Boys "
+                        "function, OpenMP dynamic over bra pairs" % tau,
+           "sample": "one whole build on all %d threads (%d contracted integrals)" % (threads, cnt),
+           "schwarz_s": t_q,
+           "one_core": {"value": c_1 / (t_1 * total), "unit": "builds/s", "cores": 1,
+                        "sample": "%d of %d bra pairs (every %d-th), %d integrals, extrapolated to the %d of a "
+                                  "build" % (len(sample), npair, stride, c_1, total)}}
+    if J_ref is not None:
+        out["max_abs_dJ_vs_gpu_fp64"] = float(np.abs(J - J_ref).max())
+        out["max_abs_dK_vs_gpu_fp64"] = float(np.abs(K - K_ref).max())
+    return out
 
 
 def _timed_builds(rc, torch, b, D, tau32, reps=3, emulated=False):
@@ -467,12 +526,13 @@ def main():
             traffic = None
 
     # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
-    cpu = None
+    cpu, cpu_strong = None, None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         rates, threads, m, _ = cpu_reference_rate(a.workload, a.cpu_sample, steps=1)
         cpu = {"value": rates[0], "unit": "builds/s", "cores": threads, "kind": "port",
                "sample": "%d J/K elements by the JK_direct loops (src/basis.rs:392-425) with THO ERIs and the "
                          "shipped NR Boys function, extrapolated to the %d^2 elements of a build" % (m, n)}
+        cpu_strong = cpu_strong_rate(a.workload, Dh, J64, K64)
 
     # ---- the larger target workloads (outside the headline timed region) ------
     targets = None
@@ -520,6 +580,7 @@ def main():
         "clocks": clocks,
         "wall_s_timed": wall,
         "cpu_baseline": cpu,
+        "cpu_baseline_strong": cpu_strong,
         "targets": targets,
     }
     if rank == 0:

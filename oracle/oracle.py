@@ -143,6 +143,9 @@ class PortLib(Lib):
         L.oq_jk_sym.argtypes = bargs + [_p, _p, _p, _p]
         L.oq_jk_elements.argtypes = bargs + [_p, _p, _i, _p, _p, _p, _p]
         L.oq_jk_direct_elements.argtypes = bargs + [_p, _p, _i, _p, _p, _p, _p]
+        L.oq_schwarz.argtypes = bargs + [_p, _p]
+        L.oq_jk_sym_screened.argtypes = bargs + [_p, _p, _p, _d, _p, C.c_long, _i, _i, _p, _p]
+        L.oq_jk_sym_screened.restype = C.c_longlong
 
     def set_boys(self, exact: bool):
         self.lib.oq_set_boys_mode(1 if exact else 0)
@@ -287,6 +290,34 @@ def JK_sym(b: CGTOBasis, D: np.ndarray, lib: Lib | None = None):
     K = np.zeros((n, n))
     port().lib.oq_jk_sym(*b.args(), _eri_ptr(lib), D.ctypes.data, J.ctypes.data, K.ctypes.data)
     return J, K
+
+
+def schwarz(b: CGTOBasis, lib: Lib | None = None) -> np.ndarray:
+    """Q[ij] = sqrt(|(ij|ij)|) over contracted function pairs, ij = i(i+1)/2 + j."""
+    Q = np.zeros(b.n * (b.n + 1) // 2)
+    port().lib.oq_schwarz(*b.args(), _eri_ptr(lib), Q.ctypes.data)
+    return Q
+
+
+def JK_sym_screened(b: CGTOBasis, D: np.ndarray, Q: np.ndarray, tau: float, pairs=None, nthreads: int = 0,
+                    count_only: bool = False, lib: Lib | None = None):
+    """J and K with each unique contracted integral once and quartets with
+    Q_ij Q_kl < tau skipped, over the bra pairs ``pairs`` (None: all, the whole
+    build).  Returns (J, K, integrals evaluated); J and K are None when
+    ``count_only``."""
+    n = b.n
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert D.shape == (n, n) and Q.shape == (n * (n + 1) // 2,)
+    ijs = None if pairs is None else np.ascontiguousarray(pairs, dtype=np.int64)
+    if ijs is not None:
+        assert ijs.size == 0 or (ijs.min() >= 0 and ijs.max() < Q.size)
+    J = np.zeros((n, n))
+    K = np.zeros((n, n))
+    cnt = port().lib.oq_jk_sym_screened(*b.args(), _eri_ptr(lib), D.ctypes.data, Q.ctypes.data, float(tau),
+                                        None if ijs is None else ijs.ctypes.data, 0 if ijs is None else ijs.size,
+                                        int(nthreads), 1 if count_only else 0, J.ctypes.data, K.ctypes.data)
+    return (None, None, int(cnt)) if count_only else (J, K, int(cnt))
 
 
 def JK_elements(b: CGTOBasis, D: np.ndarray, mus, nus, lib: Lib | None = None):

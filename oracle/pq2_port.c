@@ -11,6 +11,8 @@
  *   - helpers                         libpyquante2/cints.c:272-300,375-395
  *   - S/T/V, JK_direct, build_I,
  *     JK_inmem matrix semantics       src/basis.rs:214-484
+ *   - J/K with 8-fold symmetry and a Schwarz screen over contracted
+ *     functions (the strong CPU baseline of the Fock build; same integrals)
  *   - multipole moments               src/integrals/os86.rs:775-828 (restated
  *                                     through 1-D overlaps, not the symbolic
  *                                     expansion)
@@ -577,6 +579,94 @@ void oq_jk_sym(OQ_BASIS_ARGS, void *eri, const double *D, double *J, double *K) 
             J[a * n + b] = J[b * n + a] = js;
             K[a * n + b] = K[b * n + a] = ks;
         }
+}
+
+/* pair index ij = i (i + 1) / 2 + j (j <= i) -> (i, j) */
+static void pair_of(long ij, int *i, int *j) {
+    int a = (int)((sqrt(8.0 * ij + 1.0) - 1.0) / 2.0);
+    while ((long)a * (a + 1) / 2 > ij) --a;
+    while ((long)(a + 1) * (a + 2) / 2 <= ij) ++a;
+    *i = a;
+    *j = (int)(ij - (long)a * (a + 1) / 2);
+}
+
+/* Schwarz bounds over contracted functions: Q[ij] = sqrt(|(ij|ij)|), so that
+ * |(ij|kl)| <= Q[ij] Q[kl].  OpenMP over the pairs. */
+void oq_schwarz(OQ_BASIS_ARGS, void *eri, double *Q) {
+    OQ_BASIS_INIT;
+    oq_eri_fn f = eri ? (oq_eri_fn)eri : oq_coulomb_repulsion;
+    long npair = (long)n * (n + 1) / 2;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long ij = 0; ij < npair; ++ij) {
+        int i, j;
+        pair_of(ij, &i, &j);
+        Q[ij] = sqrt(fabs(contr_eri(f, &bs, i, j, i, j)));
+    }
+}
+
+/* oq_jk_sym as a CPU direct-SCF code runs it: each unique contracted integral
+ * once, and a quartet skipped when Q[ij] Q[kl] < tau (tau <= 0: no
+ * screening).  Only the bra pairs listed in ijs[0..nij) are processed (ijs
+ * NULL: all of them, the whole build); a strided subset is a bounded sample
+ * of the build.  J and K receive that subset's contributions, symmetrised as
+ * in oq_jk_sym.  nthreads > 0 fixes the OpenMP team size (0: all threads).
+ * count_only != 0 evaluates nothing and leaves J and K untouched.  Returns
+ * the number of contracted integrals that pass the screen. */
+long long oq_jk_sym_screened(OQ_BASIS_ARGS, void *eri, const double *D, const double *Q, double tau,
+                             const long *ijs, long nij, int nthreads, int count_only, double *J, double *K) {
+    OQ_BASIS_INIT;
+    oq_eri_fn f = eri ? (oq_eri_fn)eri : oq_coulomb_repulsion;
+    size_t nn = (size_t)n * n;
+    long npair = (long)n * (n + 1) / 2;
+    long nb = ijs ? nij : npair;
+    int nthr = 1;
+#ifdef _OPENMP
+    nthr = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+    double *acc = count_only ? NULL : (double *)calloc((size_t)nthr * 2 * nn, sizeof(double));
+    long long count = 0;
+#pragma omp parallel for num_threads(nthr) schedule(dynamic, 1) reduction(+ : count)
+    for (long t = 0; t < nb; ++t) {
+        const long ij = ijs ? ijs[t] : t;
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        int i, j;
+        pair_of(ij, &i, &j);
+        for (long kl = 0; kl <= ij; ++kl) {
+            if (tau > 0.0 && Q[ij] * Q[kl] < tau) continue;
+            ++count;
+            if (count_only) continue;
+            double *Jt = acc + (size_t)tid * 2 * nn, *Kt = Jt + nn;
+            int k, l;
+            pair_of(kl, &k, &l);
+            double v = contr_eri(f, &bs, i, j, k, l);
+            if (i == j) v *= 0.5;
+            if (k == l) v *= 0.5;
+            if (ij == kl) v *= 0.5;
+            Jt[i * n + j] += 2.0 * v * D[k * n + l];
+            Jt[k * n + l] += 2.0 * v * D[i * n + j];
+            Kt[i * n + k] += v * D[j * n + l];
+            Kt[j * n + k] += v * D[i * n + l];
+            Kt[i * n + l] += v * D[j * n + k];
+            Kt[j * n + l] += v * D[i * n + k];
+        }
+    }
+    if (count_only) return count;
+    for (size_t x = 0; x < nn; ++x) { J[x] = 0.0; K[x] = 0.0; }
+    for (int t = 0; t < nthr; ++t) {
+        double *Jt = acc + (size_t)t * 2 * nn, *Kt = Jt + nn;
+        for (size_t x = 0; x < nn; ++x) { J[x] += Jt[x]; K[x] += Kt[x]; }
+    }
+    free(acc);
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b <= a; ++b) {
+            double js = J[a * n + b] + J[b * n + a], ks = K[a * n + b] + K[b * n + a];
+            J[a * n + b] = J[b * n + a] = js;
+            K[a * n + b] = K[b * n + a] = ks;
+        }
+    return count;
 }
 
 /* Selected elements J_mn and K_mn, straight from the definitions of

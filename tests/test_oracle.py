@@ -178,6 +178,44 @@ def test_port_jk_direct_vs_sym(oracle_mod):
     np.testing.assert_allclose(Ke, K1[[0, 3, 6], [1, 3, 2]], atol=1e-13)
 
 
+def test_screened_jk_vs_unscreened(oracle_mod):
+    """The strong CPU baseline's J/K (8-fold symmetry, Schwarz screen over
+    contracted functions): with the screen off it equals the 8-fold oracle;
+    at tau = 1e-12 it stays within the dropped integrals' bound; the
+    count-only pass counts what the full pass evaluates; the bra pairs split
+    into two subsets (one on one thread) add up to the whole build."""
+    from rchem_gb300 import bse, geometry
+
+    O = oracle_mod
+    Z, R = geometry.water_cluster(2, 4.5, seed=3)
+    b = O.expand_basis(Z, R, bse.load_bse("6-31g-fit"))
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(b.n, b.n))
+    D = X @ X.T / b.n
+    npair = b.n * (b.n + 1) // 2
+    J0, K0 = O.JK_sym(b, D)
+    Q = O.schwarz(b)
+    assert Q.shape == (npair,) and np.all(Q >= 0.0)
+    # Q_ii,ii is the square root of a diagonal integral
+    assert abs(Q[2] ** 2 - O.port().lib.oq_contracted_eri(*b.args(), None, 1, 1, 1, 1)) < 1e-14
+    J1, K1, c1 = O.JK_sym_screened(b, D, Q, 0.0)
+    assert c1 == npair * (npair + 1) // 2
+    np.testing.assert_allclose(J1, J0, atol=1e-13, rtol=0)
+    np.testing.assert_allclose(K1, K0, atol=1e-13, rtol=0)
+    J2, K2, c2 = O.JK_sym_screened(b, D, Q, 1e-12)
+    assert 0 < c2 < c1
+    bound = 6 * (c1 - c2) * 1e-12 * np.abs(D).max()  # each dropped |(ij|kl)| < tau feeds at most 6 elements
+    assert np.abs(J2 - J0).max() <= bound and np.abs(K2 - K0).max() <= bound
+    assert O.JK_sym_screened(b, D, Q, 1e-12, count_only=True)[2] == c2
+    pairs = np.arange(npair)
+    a, rest = pairs[::3], np.setdiff1d(pairs, pairs[::3])
+    Ja, Ka, ca = O.JK_sym_screened(b, D, Q, 1e-12, pairs=a, nthreads=1)
+    Jb, Kb, cb = O.JK_sym_screened(b, D, Q, 1e-12, pairs=rest)
+    assert ca + cb == c2
+    np.testing.assert_allclose(Ja + Jb, J2, atol=1e-13, rtol=0)
+    np.testing.assert_allclose(Ka + Kb, K2, atol=1e-13, rtol=0)
+
+
 def test_scf_energy_fixture(oracle_mod):
     from rchem_gb300 import bse, geometry
 
