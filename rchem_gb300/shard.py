@@ -1,4 +1,4 @@
-"""Geometries of a batch sharded over ranks, one process per GPU.
+"""Work of the hot path sharded over ranks, one process per GPU.
 
 The batched workload (hundreds of independent molecules) has no exchange step:
 quartets never couple two geometries.  Rank r takes a shard of the
@@ -17,6 +17,13 @@ The rank and world size come from ``torch.distributed`` when a process group
 is initialised (NCCL on GPUs, gloo on CPUs; only the final gather uses it),
 else the process is a world of one.  Each rank must have selected its own GPU
 (``torch.cuda.set_device(local_rank)``) before creating handles.
+
+One Fock build of a single large system shards instead by bra pairs: the same
+``shard`` over per-pair costs (the kets that pass the Schwarz screen, say)
+gives every rank its bras, each rank accumulates partial J and K over its
+quartets, and ``allreduce_sum`` adds them (2 n^2 doubles per build).  The
+library's Fock build does not take a subset of bra pairs, so on GPUs only the
+batched form runs sharded.
 
 The reference runs one molecule per process and has no distributed layer;
 this is new capability around its energy conventions.
@@ -93,6 +100,27 @@ def run_sharded(items: Sequence, costs: Sequence[float], compute: Callable[[list
         for i, r in part:
             out[i] = r
     return out
+
+
+def allreduce_sum(*arrays, group=None):
+    """Sum each array over the ranks of the process group, in place on torch
+    tensors (CPU tensors under gloo, CUDA tensors under NCCL); numpy arrays are
+    summed through a CPU tensor and written back.  A world of one leaves them
+    as they are.  Returns the arrays."""
+    _, world = _rank_world(group)
+    if world == 1:
+        return arrays
+    import torch
+    import torch.distributed as dist
+
+    for a in arrays:
+        if isinstance(a, np.ndarray):
+            t = torch.from_numpy(np.ascontiguousarray(a))
+            dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+            a[...] = t.numpy()
+        else:
+            dist.all_reduce(a, op=dist.ReduceOp.SUM, group=group)
+    return arrays
 
 
 def rhf_gradient_sharded(geometries, basis_set_name="6-31g-fit", group=None, thresh_e=1e-10, thresh_d=1e-7,

@@ -166,3 +166,72 @@ def test_rhf_gradient_sharded_plumbing(monkeypatch):
     for (Z, _), r in zip(geoms, res):
         assert r["e_total"] == len(Z) - 1.0 and r["e_elec"] == len(Z) - 2.0 and r["e_nuc"] == 1.0
         assert r["gradient"].shape == (len(Z), 3) and r["converged"] is True
+
+
+def _jk_worker(rank, world, port, out_dir):
+    """One rank of a single-system Fock build sharded by bra pairs."""
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch.distributed as dist
+
+    import oracle as O
+
+    from rchem_gb300.shard import allreduce_sum, shard
+
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    try:
+        b, D, Q, costs = _jk_problem(O)
+        mine = shard(costs, world)[rank]
+        J, K, cnt = O.JK_sym_screened(b, D, Q, 1e-12, pairs=mine)
+        c = np.array([float(cnt)])
+        allreduce_sum(J, K, c)
+        np.savez(os.path.join(out_dir, "jk%d.npz" % rank), J=J, K=K, c=c, mine=np.array(mine))
+    finally:
+        dist.destroy_process_group()
+
+
+def _jk_problem(O):
+    import rchem_gb300 as rc
+
+    O.port().set_boys(True)
+    Z, R = rc.geometry.water_cluster(3, 5.0, seed=5)
+    b = O.expand_basis(Z, R, rc.load_bse("6-31g-fit"))
+    rng = np.random.default_rng(2)
+    X = rng.normal(size=(b.n, b.n))
+    D = X @ X.T / b.n
+    Q = O.schwarz(b)
+    # per bra pair ij: the kets kl <= ij that pass the screen
+    costs = np.array([np.count_nonzero(Q[: ij + 1] * Q[ij] >= 1e-12) for ij in range(Q.size)], dtype=float)
+    return b, D, Q, costs
+
+
+def test_fock_build_sharded_by_bra_pairs_over_two_gloo_ranks(tmp_path):
+    """A single system's J and K: bra pairs sharded by their screened ket
+    counts, partial J/K per rank, one sum all-reduce -- equal on both ranks
+    to the whole build, with the integral count split near evenly."""
+    import torch.multiprocessing as mp
+
+    from rchem_gb300.shard import shard
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    world = 2
+    ctx = mp.start_processes(_jk_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=False,
+                             start_method="spawn")
+    deadline = time.time() + 300
+    while not ctx.join(timeout=5):
+        if time.time() > deadline:
+            for p in ctx.processes:
+                p.kill()
+            pytest.fail("gloo ranks did not finish in 300 s")
+    b, D, Q, costs = _jk_problem(O)
+    J0, K0, c0 = O.JK_sym_screened(b, D, Q, 1e-12)
+    loads = []
+    for r in range(world):
+        z = np.load(os.path.join(tmp_path, "jk%d.npz" % r))
+        np.testing.assert_allclose(z["J"], J0, atol=1e-12, rtol=0)
+        np.testing.assert_allclose(z["K"], K0, atol=1e-12, rtol=0)
+        assert int(z["c"][0]) == c0
+        loads.append(costs[z["mine"]].sum())
+    assert sum(loads) == c0 and max(loads) - min(loads) <= costs.max()
