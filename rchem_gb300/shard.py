@@ -65,6 +65,10 @@ def shard(costs: Sequence[float], world: int) -> list:
     return [sorted(p) for p in parts]
 
 
+class ShardError(RuntimeError):
+    """A rank's share of a sharded computation failed (raised on every rank)."""
+
+
 def _rank_world(group=None):
     try:
         import torch.distributed as dist
@@ -81,22 +85,39 @@ def run_sharded(items: Sequence, costs: Sequence[float], compute: Callable[[list
 
     ``compute(list_of_items)`` returns one result per item, in order; results
     must be picklable (they travel through ``all_gather_object``).  A rank with
-    an empty shard does not call ``compute``."""
+    an empty shard does not call ``compute``.
+
+    A failure on one rank (``compute`` raising, or returning the wrong number
+    of results) does not leave the others waiting: that rank still joins the
+    gather, carrying its error, and every rank then raises ``ShardError``
+    naming the failed ranks.  In a world of one the error propagates as it
+    is."""
     if len(costs) != len(items):
         raise ValueError("%d costs for %d items" % (len(costs), len(items)))
     rank, world = _rank_world(group)
     mine = shard(costs, world)[rank]
-    local = list(compute([items[i] for i in mine])) if mine else []
-    if len(local) != len(mine):
-        raise ValueError("compute returned %d results for %d items" % (len(local), len(mine)))
-    if world == 1:
+
+    def run():
+        local = list(compute([items[i] for i in mine])) if mine else []
+        if len(local) != len(mine):
+            raise ValueError("compute returned %d results for %d items" % (len(local), len(mine)))
         return local
+
+    if world == 1:
+        return run()
     import torch.distributed as dist
 
+    try:
+        local, err = run(), None
+    except Exception as e:  # reported to every rank through the gather below
+        local, err = [], "%s: %s" % (type(e).__name__, e)
     parts = [None] * world
-    dist.all_gather_object(parts, list(zip(mine, local)), group=group)
+    dist.all_gather_object(parts, (list(zip(mine, local)), err), group=group)
+    failed = [(r, p[1]) for r, p in enumerate(parts) if p[1] is not None]
+    if failed:
+        raise ShardError("sharded compute failed on rank(s) " + "; ".join("%d (%s)" % f for f in failed))
     out = [None] * len(items)
-    for part in parts:
+    for part, _ in parts:
         for i, r in part:
             out[i] = r
     return out

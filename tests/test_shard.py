@@ -235,3 +235,52 @@ def test_fock_build_sharded_by_bra_pairs_over_two_gloo_ranks(tmp_path):
         assert int(z["c"][0]) == c0
         loads.append(costs[z["mine"]].sum())
     assert sum(loads) == c0 and max(loads) - min(loads) <= costs.max()
+
+
+def _failing_compute(rank):
+    def compute(local):
+        if rank == 1:
+            raise RuntimeError("injected failure on rank 1")
+        return [0.0 for _ in local]
+
+    return compute
+
+
+def _fail_worker(rank, world, port, out_dir):
+    """Rank 1's share raises; both ranks must end with ShardError, not wait."""
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+
+    from rchem_gb300.shard import ShardError, run_sharded
+
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    try:
+        run_sharded(list(range(6)), [1.0] * 6, _failing_compute(rank))
+        msg = "no error"
+    except ShardError as e:
+        msg = "ShardError: %s" % e
+    finally:
+        dist.destroy_process_group()
+    with open(os.path.join(out_dir, "fail%d.txt" % rank), "w") as f:
+        f.write(msg)
+
+
+def test_rank_failure_reported_on_every_rank(tmp_path):
+    """A failure injected on the host in one rank's share (its compute raises)
+    reaches every rank as ShardError naming that rank; no rank waits for it."""
+    import torch.multiprocessing as mp
+
+    world = 2
+    t0 = time.time()
+    ctx = mp.start_processes(_fail_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=False,
+                             start_method="spawn")
+    deadline = time.time() + 120
+    while not ctx.join(timeout=5):
+        if time.time() > deadline:
+            for p in ctx.processes:
+                p.kill()
+            pytest.fail("ranks did not finish in 120 s")
+    for r in range(world):
+        msg = open(os.path.join(tmp_path, "fail%d.txt" % r)).read()
+        assert msg.startswith("ShardError") and "rank(s) 1 (RuntimeError: injected failure on rank 1)" in msg, msg
+    assert time.time() - t0 < 60
