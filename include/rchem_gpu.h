@@ -127,6 +127,14 @@ int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
  * NULL) of the current work plan: the class (l_a,l_b,l_c,l_d), and for {FP64,
  * FP32} the shell quartets, primitive quartets and algorithmic FLOPs. */
 int rchem_jk_class_stats(rchem_basis b, int *class_l, long long *quartets, long long *prim_quartets, double *flops);
+/* Device time of every class list of the Fock build planned for these
+ * options, each list launched alone on the handle's stream (one warm-up launch,
+ * then one launch between CUDA events), J/K epilogue, the density of the last
+ * Fock build (zeros before the first): ms[2*21] in the order of
+ * rchem_jk_class_stats, 0 for an empty list.  No counterpart in the
+ * reference; with rchem_jk_class_stats' FLOPs it gives each kernel's rate.
+ * J-hat/K-hat scratch is overwritten; the next rchem_jk_direct clears it. */
+int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, float *ms);
 
 /*
  * The Fock build of rchem_jk_direct without any device allocation (this entry
@@ -145,8 +153,11 @@ int rchem_jk_class_stats(rchem_basis b, int *class_l, long long *quartets, long 
  *    larger bases get RCHEM_ERR_UNSUPPORTED.
  *  - The basis must already be planned for the same thresholds: call
  *    rchem_jk_direct once with the same options first (planning may allocate).
- *  - The first call on a device looks up the array's device address; make
- *    that first call before any stream capture.
+ *  - The handle's device must be the current device (RCHEM_ERR_INVALID
+ *    otherwise).  The first call on a device looks up the array's device
+ *    address; make that first call before any stream capture.
+ *  - Like rchem_jk_direct, the call is synchronous: it returns once J and K
+ *    are written.
  *  - Every call on a device shares the one array: calls whose GPU work
  *    overlaps (different threads, streams or handles at the same time) race.
  *    Each call clears the accumulators it uses.

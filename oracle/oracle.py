@@ -146,6 +146,10 @@ class PortLib(Lib):
         L.oq_schwarz.argtypes = bargs + [_p, _p]
         L.oq_jk_sym_screened.argtypes = bargs + [_p, _p, _p, _d, _p, C.c_long, _i, _i, _p, _p]
         L.oq_jk_sym_screened.restype = C.c_longlong
+        L.oq_jk_direct_quartets.argtypes = bargs + [_p, _p, _i, _p, _p, _p, _p, _p, _p]
+        L.oq_jk_elements_screened.argtypes = bargs + [_p, _p, _p, _d, _i, _p, _p, _p, _p]
+        L.oq_eri_packed.argtypes = bargs + [_p, _p, _d, _p]
+        L.oq_jk_packed.argtypes = [_i, _p, _p, _p, _p]
 
     def set_boys(self, exact: bool):
         self.lib.oq_set_boys_mode(1 if exact else 0)
@@ -343,6 +347,61 @@ def JK_direct_elements(b: CGTOBasis, D: np.ndarray, mus, nus, lib: Lib | None = 
     return Jo, Ko
 
 
+def JK_direct_quartets(b: CGTOBasis, D: np.ndarray, mus, nus, las, sgs, lib: Lib | None = None):
+    """The innermost block of the literal JK_direct loops (basis.rs:400-421)
+    for sampled quadruples (mu, nu, lambda, sigma): their J and K
+    contributions.  A whole build is the sum over all n^4 quadruples."""
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    idx = [np.ascontiguousarray(x, dtype=np.int32) for x in (mus, nus, las, sgs)]
+    m = len(idx[0])
+    assert all(len(x) == m for x in idx) and all(x.size == 0 or (x.min() >= 0 and x.max() < b.n) for x in idx)
+    Jo, Ko = np.zeros(m), np.zeros(m)
+    port().lib.oq_jk_direct_quartets(*b.args(), _eri_ptr(lib), D.ctypes.data, m, *(x.ctypes.data for x in idx),
+                                     Jo.ctypes.data, Ko.ctypes.data)
+    return Jo, Ko
+
+
+def JK_elements_screened(b: CGTOBasis, D: np.ndarray, Q: np.ndarray, tau: float, mus, nus,
+                         lib: Lib | None = None):
+    """Elements J_mn, K_mn from their definitions (basis.rs:406-417) with
+    contracted integrals, skipping (ab|cd) when Q_ab Q_cd < tau (Q from
+    ``schwarz``); OpenMP over the elements."""
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    mu = np.ascontiguousarray(mus, dtype=np.int32)
+    nu = np.ascontiguousarray(nus, dtype=np.int32)
+    assert Q.shape == (b.n * (b.n + 1) // 2,) and D.shape == (b.n, b.n)
+    assert mu.size == nu.size and (mu.size == 0 or (min(mu.min(), nu.min()) >= 0 and max(mu.max(), nu.max()) < b.n))
+    Jo, Ko = np.zeros(len(mu)), np.zeros(len(mu))
+    port().lib.oq_jk_elements_screened(*b.args(), _eri_ptr(lib), D.ctypes.data, Q.ctypes.data, float(tau), len(mu),
+                                       mu.ctypes.data, nu.ctypes.data, Jo.ctypes.data, Ko.ctypes.data)
+    return Jo, Ko
+
+
+def eri_packed(b: CGTOBasis, Q: np.ndarray | None = None, tau: float = 0.0, lib: Lib | None = None) -> np.ndarray:
+    """The ERI tensor in the packed 8-fold layout of ijkl2intindex; integrals
+    with Q_ij Q_kl < tau stored as zero."""
+    npair = b.n * (b.n + 1) // 2
+    if Q is None:
+        Q, tau = np.zeros(npair), 0.0
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    assert Q.shape == (npair,)
+    out = np.empty(npair * (npair + 1) // 2)
+    port().lib.oq_eri_packed(*b.args(), _eri_ptr(lib), Q.ctypes.data, float(tau), out.ctypes.data)
+    return out
+
+
+def JK_packed(n: int, I: np.ndarray, D: np.ndarray):
+    """J and K (JK_inmem's definitions) from a packed tensor of ``eri_packed``."""
+    npair = n * (n + 1) // 2
+    I = np.ascontiguousarray(I, dtype=np.float64)
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    assert I.shape == (npair * (npair + 1) // 2,) and D.shape == (n, n)
+    J, K = np.zeros((n, n)), np.zeros((n, n))
+    port().lib.oq_jk_packed(n, I.ctypes.data, D.ctypes.data, J.ctypes.data, K.ctypes.data)
+    return J, K
+
+
 def build_I(b: CGTOBasis, lib: Lib | None = None) -> np.ndarray:
     n = b.n
     out = np.zeros((n, n, n, n))
@@ -416,8 +475,15 @@ def nuclear_repulsion(atomnos, coords):
     return e
 
 
-def rhf(b: CGTOBasis, atomnos, coords, nocc, jk=None, thresh_e=1e-11, max_iter=1024, lib=None):
-    """Plain Roothaan iterations as rchem.rs:40-89 (core guess, no DIIS)."""
+def rhf(b: CGTOBasis, atomnos, coords, nocc, jk=None, thresh_e=1e-11, max_iter=1024, lib=None, diis=0,
+        thresh_d=None):
+    """Roothaan iterations as rchem.rs:40-89 (core guess; D = C_occ C_occ^T;
+    F = H + 2J - K; E = sum (H + F) o D; stop when |Delta E| < thresh_e).
+    ``diis`` > 0 extrapolates the Fock matrix by Pulay's DIIS over that many
+    previous iterations (error vector X^T (FDS - SDF) X), which the reference
+    does not do; it changes the path to convergence, not the converged
+    energy.  ``thresh_d`` also requires max |Delta D| below it.  ``e_final``
+    is the energy of the last density with its own Fock matrix."""
     Smat, Tm, Vm = S(b, lib), T(b, lib), V(b, coords, atomnos, lib)
     H = Tm + Vm
     X = symm_orthog(Smat)
@@ -425,14 +491,39 @@ def rhf(b: CGTOBasis, atomnos, coords, nocc, jk=None, thresh_e=1e-11, max_iter=1
     D = build_density(X @ Cp, nocc)
     e_new = elec_energy(D, H, H)
     jk = jk or (lambda Dm: JK_sym(b, Dm, lib))
+    focks, errs = [], []
     it = 0
+    converged = False
     for it in range(max_iter):
         J, K = jk(D)
         F = H + 2.0 * J - K
-        _, Cp = np.linalg.eigh(X.T @ F @ X)
+        Fx = F
+        if diis > 0:
+            focks.append(F)
+            errs.append(X.T @ (F @ D @ Smat - Smat @ D @ F) @ X)
+            del focks[:-diis], errs[:-diis]
+            m = len(focks)
+            if m >= 2:
+                B = -np.ones((m + 1, m + 1))
+                B[m, m] = 0.0
+                for i in range(m):
+                    for j in range(m):
+                        B[i, j] = float(np.sum(errs[i] * errs[j]))
+                rhs = np.zeros(m + 1)
+                rhs[m] = -1.0
+                try:
+                    c = np.linalg.solve(B, rhs)
+                    Fx = sum(c[i] * focks[i] for i in range(m))
+                except np.linalg.LinAlgError:
+                    Fx = F
+        _, Cp = np.linalg.eigh(X.T @ Fx @ X)
+        D_old = D
         D = build_density(X @ Cp, nocc)
         e_old, e_new = e_new, elec_energy(D, H, F)
-        if abs(e_new - e_old) < thresh_e:
+        if abs(e_new - e_old) < thresh_e and (thresh_d is None or np.abs(D - D_old).max() < thresh_d):
+            converged = True
             break
-    return {"e_elec": e_new, "e_nuc": nuclear_repulsion(atomnos, coords), "D": D, "iterations": it + 1,
-            "S": Smat, "T": Tm, "V": Vm}
+    J, K = jk(D)
+    e_final = elec_energy(D, H, H + 2.0 * J - K)
+    return {"e_elec": e_new, "e_final": e_final, "e_nuc": nuclear_repulsion(atomnos, coords), "D": D,
+            "iterations": it + 1, "converged": converged, "S": Smat, "T": Tm, "V": Vm}

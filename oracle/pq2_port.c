@@ -740,3 +740,146 @@ void oq_jk_direct_elements(OQ_BASIS_ARGS, void *eri, const double *D, int m, con
         Kout[e] = kv;
     }
 }
+
+/* The innermost block of JK_direct (basis.rs:400-421) for sampled index
+ * quadruples (mu, nu, lambda, sigma): every primitive quartet, two primitive
+ * ERIs (one for J, one for K), each weighted by D[lambda][sigma].  A Fock
+ * build by the reference's loops is the sum of these blocks over all n^4
+ * quadruples, so the mean time per sampled block times n^4 is the time of a
+ * whole build.  OpenMP over the samples. */
+void oq_jk_direct_quartets(OQ_BASIS_ARGS, void *eri, const double *D, int m, const int *mus, const int *nus,
+                           const int *las, const int *sgs, double *Jout, double *Kout) {
+    OQ_BASIS_INIT;
+    oq_eri_fn f = eri ? (oq_eri_fn)eri : oq_coulomb_repulsion;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int e = 0; e < m; ++e) {
+        const int mu = mus[e], nu = nus[e], la = las[e], sg = sgs[e];
+        const double dls = D[la * n + sg];
+        double jc = 0.0, kc = 0.0;
+        for (int a = 0; a < bs.nprim[mu]; ++a) {
+            int pa = bs.prim_off[mu] + a;
+            for (int b2 = 0; b2 < bs.nprim[nu]; ++b2) {
+                int pb = bs.prim_off[nu] + b2;
+                for (int c = 0; c < bs.nprim[la]; ++c) {
+                    int pc = bs.prim_off[la] + c;
+                    for (int d = 0; d < bs.nprim[sg]; ++d) {
+                        int pd = bs.prim_off[sg] + d;
+                        double cc = bs.coefs[pa] * bs.coefs[pb] * bs.coefs[pc] * bs.coefs[pd];
+                        jc += cc * prim_eri(f, &bs, mu, pa, nu, pb, la, pc, sg, pd) * dls;
+                        kc += cc * prim_eri(f, &bs, mu, pa, la, pc, nu, pb, sg, pd) * dls;
+                    }
+                }
+            }
+        }
+        Jout[e] = jc;
+        Kout[e] = kc;
+    }
+}
+
+static long pair_idx(int i, int j) { return i >= j ? (long)i * (i + 1) / 2 + j : (long)j * (j + 1) / 2 + i; }
+
+/* Elements J_mn and K_mn as oq_jk_elements, but a contracted integral
+ * (ab|cd) is skipped when Q[ab] Q[cd] < tau (Q from oq_schwarz); tau far
+ * below the Fock build's threshold keeps the elements exact to well under
+ * that threshold while skipping the integrals of distant pairs.  OpenMP over
+ * the elements. */
+void oq_jk_elements_screened(OQ_BASIS_ARGS, void *eri, const double *D, const double *Q, double tau, int m,
+                             const int *mus, const int *nus, double *Jout, double *Kout) {
+    OQ_BASIS_INIT;
+    oq_eri_fn f = eri ? (oq_eri_fn)eri : oq_coulomb_repulsion;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int e = 0; e < m; ++e) {
+        const int mu = mus[e], nu = nus[e];
+        const double qmn = Q[pair_idx(mu, nu)];
+        double jv = 0.0, kv = 0.0;
+        for (int la = 0; la < n; ++la) {
+            const double qml = Q[pair_idx(mu, la)];
+            for (int sg = 0; sg < n; ++sg) {
+                const double dls = D[la * n + sg];
+                if (sg <= la && qmn * Q[pair_idx(la, sg)] >= tau) {
+                    double w = (sg == la) ? 1.0 : 2.0;
+                    jv += w * contr_eri(f, &bs, mu, nu, la, sg) * dls;
+                }
+                if (qml * Q[pair_idx(nu, sg)] >= tau) kv += contr_eri(f, &bs, mu, la, nu, sg) * dls;
+            }
+        }
+        Jout[e] = jv;
+        Kout[e] = kv;
+    }
+}
+
+/* The ERI tensor in the 8-fold packed layout of cints.c:375-387
+ * (I[pair(pair(i,j), pair(k,l))] = (ij|kl)), each unique contracted integral
+ * once; integrals with Q[ij] Q[kl] < tau are stored as 0 (tau <= 0: none).
+ * OpenMP over the bra pairs. */
+void oq_eri_packed(OQ_BASIS_ARGS, void *eri, const double *Q, double tau, double *I) {
+    OQ_BASIS_INIT;
+    oq_eri_fn f = eri ? (oq_eri_fn)eri : oq_coulomb_repulsion;
+    long npair = (long)n * (n + 1) / 2;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long ij = 0; ij < npair; ++ij) {
+        int i, j;
+        pair_of(ij, &i, &j);
+        double *row = I + (size_t)ij * (ij + 1) / 2;
+        for (long kl = 0; kl <= ij; ++kl) {
+            if (tau > 0.0 && Q[ij] * Q[kl] < tau) {
+                row[kl] = 0.0;
+                continue;
+            }
+            int k, l;
+            pair_of(kl, &k, &l);
+            row[kl] = contr_eri(f, &bs, i, j, k, l);
+        }
+    }
+}
+
+/* J and K (JK_inmem's definitions, basis.rs:462-484) from the packed tensor
+ * of oq_eri_packed: every unique integral scattered to its symmetric
+ * positions with the degeneracy weights of oq_jk_sym.  D symmetric. */
+void oq_jk_packed(int n, const double *I, const double *D, double *J, double *K) {
+    size_t nn = (size_t)n * n;
+    long npair = (long)n * (n + 1) / 2;
+    int nthr = 1;
+#ifdef _OPENMP
+    nthr = omp_get_max_threads();
+#endif
+    double *acc = (double *)calloc((size_t)nthr * 2 * nn, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long ij = 0; ij < npair; ++ij) {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        double *Jt = acc + (size_t)tid * 2 * nn, *Kt = Jt + nn;
+        int i, j;
+        pair_of(ij, &i, &j);
+        const double *row = I + (size_t)ij * (ij + 1) / 2;
+        for (long kl = 0; kl <= ij; ++kl) {
+            double v = row[kl];
+            if (v == 0.0) continue;
+            int k, l;
+            pair_of(kl, &k, &l);
+            if (i == j) v *= 0.5;
+            if (k == l) v *= 0.5;
+            if (ij == kl) v *= 0.5;
+            Jt[i * n + j] += 2.0 * v * D[k * n + l];
+            Jt[k * n + l] += 2.0 * v * D[i * n + j];
+            Kt[i * n + k] += v * D[j * n + l];
+            Kt[j * n + k] += v * D[i * n + l];
+            Kt[i * n + l] += v * D[j * n + k];
+            Kt[j * n + l] += v * D[i * n + k];
+        }
+    }
+    for (size_t x = 0; x < nn; ++x) { J[x] = 0.0; K[x] = 0.0; }
+    for (int t = 0; t < nthr; ++t) {
+        double *Jt = acc + (size_t)t * 2 * nn, *Kt = Jt + nn;
+        for (size_t x = 0; x < nn; ++x) { J[x] += Jt[x]; K[x] += Kt[x]; }
+    }
+    free(acc);
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b <= a; ++b) {
+            double js = J[a * n + b] + J[b * n + a], ks = K[a * n + b] + K[b * n + a];
+            J[a * n + b] = J[b * n + a] = js;
+            K[a * n + b] = K[b * n + a] = ks;
+        }
+}

@@ -80,6 +80,7 @@ def lib():
     L.rchem_set_tile_shape.argtypes = [vp, i, i, i]
     L.rchem_rhf.argtypes = [vp, p(SCFOpts), vp, vp, vp, vp, vp, vp, vp]
     L.rchem_jk_class_stats.argtypes = [vp, vp, vp, vp, vp]
+    L.rchem_jk_list_times.argtypes = [vp, p(JKOpts), vp]
     L.rchem_jk_stats_get.argtypes = [vp, p(JKStats)]
     L.rchem_build_I.argtypes = [vp, vp, i]
     L.rchem_jk_inmem.argtypes = [i, vp, vp, vp, vp, i]
@@ -119,6 +120,6 @@ def exported_symbols():
         "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "rchem_build_I_packed", "rchem_jk_packed", "ijkl2intindex", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
-        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_eigh_batched",
+        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_jk_list_times", "rchem_eigh_batched",
         "rchem_set_tile_shape", "rchem_rhf",
     ]

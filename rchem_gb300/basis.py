@@ -158,6 +158,16 @@ class Basis:
                  "prim_quartets": (int(pq[2 * k]), int(pq[2 * k + 1])), "flops": (float(fl[2 * k]), float(fl[2 * k + 1]))}
                 for k in range(21)]
 
+    def list_times(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
+        """Device time (ms) of every class list of the Fock build planned for
+        these options, each list launched alone (rchem_jk_list_times):
+        [(class, (FP64/emulated ms, FP32 ms))] in class order."""
+        ms = np.zeros(42, dtype=np.float32)
+        o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
+                        emulated=1 if emulated else 0)
+        _lib.check(_lib.lib().rchem_jk_list_times(self.handle, C.byref(o), ms.ctypes.data))
+        return [(k, (float(ms[2 * k]), float(ms[2 * k + 1]))) for k in range(21)]
+
     def stats(self) -> dict:
         st = _lib.JKStats()
         _lib.check(_lib.lib().rchem_jk_stats_get(self.handle, C.byref(st)))

@@ -4,7 +4,7 @@
 // function (libpyquante2/cints.c:302-373, relative error ~1e-7).  Here:
 //   T < BOYS_TMAX: Taylor expansion about the nearest grid point T_i = i*h,
 //     F_m(T_i + d) = sum_k F_{m+k}(T_i) (-d)^k / k!,  |d| <= h/2,
-//     with NTAY terms (8 in FP64: remainder < 3e-17 F; 4 in FP32: < 5e-8 F).
+//     with NTAY terms (6 in FP64: remainder < 3e-16 F; 4 in FP32: < 2e-10 F).
 //     The tables hold the coefficients already divided by k!, one sub-table per
 //     m (and one for e^{-T} = e^{-T_i} e^{-d}), so an evaluation is a pure
 //     Horner chain in x = -d: NTAY-1 fused multiply-adds.  Small L evaluates

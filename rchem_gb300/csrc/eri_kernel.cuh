@@ -347,7 +347,10 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 }
 
 // prec: 0 = FP64, 1 = FP32 (mixed form), 2 = double-float on the FP32 pipe
-// (emulated FP64; instantiated up to l_a+l_b+l_c+l_d = 4, FP64 above)
+// (emulated FP64): the one-lane-group-per-quartet kernel has a double-float
+// instantiation up to l_a+l_b+l_c+l_d = 4; the larger classes have one in the
+// warp-cooperative kernel below (a list of those classes that runs the
+// one-lane-group kernel stays FP64).
 // ---------------------------------------------------------------------------
 // Warp-cooperative J/K kernel for the large classes (EriClass::WC, total
 // angular momentum 4 and up; double, float and double-float): one warp

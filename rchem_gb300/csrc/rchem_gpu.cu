@@ -1054,6 +1054,10 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
         free_basis(b);
         return set_err(RCHEM_ERR_NOMEM, "work buffers for nbf=%d", ao);
     }
+    if (cudaMemsetAsync(b->d_D, 0, nn * sizeof(double), b->stream) != cudaSuccess) {
+        free_basis(b);
+        return set_err(RCHEM_ERR_CUDA, "clearing the density buffer");
+    }
     if ((rc = build_pairs(b)) != RCHEM_OK) {
         free_basis(b);
         return rc;
@@ -1474,6 +1478,20 @@ extern "C" int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl) {
     return RCHEM_OK;
 }
 
+// One class list alone on the handle's stream: a warm-up launch, then one
+// launch bracketed by CUDA events (its device time in *ms).
+static int time_list(rchem_basis b, EriArgs a, int k, int prec, float *ms) {
+    for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
+        CK(cudaEventRecord(b->ev_t0, b->stream));
+        rchem_eri_launchers[k](a, prec, EPI_JK, b->stream);
+        CK(cudaEventRecord(b->ev_t1, b->stream));
+        CK(cudaEventSynchronize(b->ev_t1));
+        CK(cudaEventElapsedTime(ms, b->ev_t0, b->ev_t1));
+    }
+    CK(cudaGetLastError());
+    return RCHEM_OK;
+}
+
 extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen) {
     NvtxRange nv("rchem_autotune");
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
@@ -1520,14 +1538,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
                 a.ntasks = (int)b->task_cnt[k][p];
                 a.wc = b->wc[k][p];
                 float ms = 0.f;
-                for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
-                    CK(cudaEventRecord(b->ev_t0, b->stream));
-                    rchem_eri_launchers[k](a, p == 1 ? 1 : (o.emulated ? 2 : 0), EPI_JK, b->stream);
-                    CK(cudaEventRecord(b->ev_t1, b->stream));
-                    CK(cudaEventSynchronize(b->ev_t1));
-                    CK(cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1));
-                }
-                CK(cudaGetLastError());
+                CKR(time_list(b, a, k, p == 1 ? 1 : (o.emulated ? 2 : 0), &ms));
                 if (ms < best_ms[k][p]) {
                     best_ms[k][p] = ms;
                     best[k][p] = wc ? kMinPrimPerLane : cand[c];
@@ -1543,6 +1554,39 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         }
     b->planned = false;
     CKR(plan_tasks(b, tau, tau32));
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, float *ms) {
+    NvtxRange nv("rchem_jk_list_times");
+    if (!b || !ms) return set_err(RCHEM_ERR_INVALID, "null argument");
+    rchem_jk_opts o;
+    memset(&o, 0, sizeof(o));
+    if (opts) o = *opts;
+    const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
+    const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
+    CKR(plan_tasks(b, tau, tau32));
+    const size_t nn = (size_t)b->packed;
+    const int th = 256;
+    // the lower-precision copies of the density the FP32 / double-float lists read
+    k_to_f32<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_D32);
+    k_to_df64<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->d_D, b->d_Ddf);
+    CK(cudaGetLastError());
+    EriArgs a = base_args(b);
+    a.segs = b->d_segs;
+    a.D = b->d_D;
+    a.D32 = b->d_D32;
+    a.J = b->d_Jh;
+    a.K = b->d_Kh;
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p) {
+            ms[2 * k + p] = 0.f;
+            if (b->task_cnt[k][p] == 0) continue;
+            a.tasks = b->d_tasks + b->task_off[k][p];
+            a.ntasks = (int)b->task_cnt[k][p];
+            a.wc = b->wc[k][p];
+            CKR(time_list(b, a, k, p == 1 ? 1 : (o.emulated ? 2 : 0), &ms[2 * k + p]));
+        }
     return RCHEM_OK;
 }
 
@@ -1985,6 +2029,12 @@ extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J
         return set_err(RCHEM_ERR_INVALID,
                        "the basis has no work plan for these thresholds: call rchem_jk_direct once with the same "
                        "options first (planning may allocate)");
+    // the scratch address and the handle's stream both belong to the handle's device
+    int cur = -1;
+    CK(cudaGetDevice(&cur));
+    if (cur != b->dev)
+        return set_err(RCHEM_ERR_INVALID, "the current device is %d, the handle's device is %d: make it current first",
+                       cur, b->dev);
     double *scratch = nullptr;
     CKR(noalloc_scratch(&scratch));
     const size_t nn = (size_t)n * n;

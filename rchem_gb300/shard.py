@@ -126,19 +126,23 @@ def run_sharded(items: Sequence, costs: Sequence[float], compute: Callable[[list
 def allreduce_sum(*arrays, group=None):
     """Sum each array over the ranks of the process group, in place on torch
     tensors (CPU tensors under gloo, CUDA tensors under NCCL); numpy arrays are
-    summed through a CPU tensor and written back.  A world of one leaves them
-    as they are.  Returns the arrays."""
+    summed through a tensor on the backend's device (the current CUDA device
+    under NCCL, the CPU otherwise) and written back.  A world of one leaves
+    them as they are.  Returns the arrays."""
     _, world = _rank_world(group)
     if world == 1:
         return arrays
     import torch
     import torch.distributed as dist
 
+    on_gpu = str(dist.get_backend(group)).lower() == "nccl"
     for a in arrays:
         if isinstance(a, np.ndarray):
             t = torch.from_numpy(np.ascontiguousarray(a))
+            if on_gpu:
+                t = t.to(torch.device("cuda", torch.cuda.current_device()))
             dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
-            a[...] = t.numpy()
+            a[...] = t.cpu().numpy()
         else:
             dist.all_reduce(a, op=dist.ReduceOp.SUM, group=group)
     return arrays

@@ -50,6 +50,39 @@ def test_noalloc_matches_jk_direct(gpu, fp32_tau):
             assert (K1 - K0).abs().max().item() < 1e-12, call
 
 
+def test_noalloc_after_emulated_build(gpu):
+    """A handle whose last Fock build (and captured graph) used the emulated
+    form: the no-allocation build still runs native FP64 and equals the
+    allocating entry point's FP64 result."""
+    import torch
+
+    import rchem_gb300 as rc
+    from rchem_gb300 import _lib
+
+    L = _lib.lib()
+    Z, R = rc.geometry.water_cluster(3, 5.5, seed=21)
+    with rc.Basis(Z, R, "6-31gs-fit") as b:
+        n = b.nbf
+        b.autotune(1e-12, 0.0, emulated=True)  # tile shapes chosen for the emulated form
+        D = torch.from_numpy(_density(n, 7)).cuda()
+        J0, K0 = torch.empty_like(D), torch.empty_like(D)
+        Je, Ke = torch.empty_like(D), torch.empty_like(D)
+        J1, K1 = torch.full_like(D, np.nan), torch.full_like(D, np.nan)
+        ptr = lambda x: C.c_void_p(x.data_ptr())  # noqa: E731
+        fp64 = _lib.JKOpts(schwarz_tau=1e-12, where=_lib.DEVICE, emulated=0)
+        emul = _lib.JKOpts(schwarz_tau=1e-12, where=_lib.DEVICE, emulated=1)
+        torch.cuda.synchronize()
+        _lib.check(L.rchem_jk_direct(b.handle, ptr(D), ptr(J0), ptr(K0), C.byref(fp64)))
+        _lib.check(L.rchem_jk_direct(b.handle, ptr(D), ptr(Je), ptr(Ke), C.byref(emul)))
+        for call in range(2):
+            _lib.check(L.rchem_jk_direct_noalloc(b.handle, ptr(D), ptr(J1), ptr(K1), C.byref(emul)))
+            torch.cuda.synchronize()
+            assert (J1 - J0).abs().max().item() < 1e-12, call
+            assert (K1 - K0).abs().max().item() < 1e-12, call
+        # the emulated build itself differs from FP64 only in the last bits
+        assert (Je - J0).abs().max().item() < 1e-12
+
+
 def test_noalloc_rejects_what_it_cannot_do(gpu):
     import torch
 
