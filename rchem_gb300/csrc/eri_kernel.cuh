@@ -357,20 +357,47 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 // per contracted shell quartet, the recurrence intermediates in shared
 // memory.  The generated program (EriProg) lists the VRR terms and the HRR
 // terms level by level of their DAG; within a level the terms are independent
-// and the 32 lanes take them in turn, one __syncwarp between levels.  Terms
-// are sorted by branch shape inside a level so lanes mostly agree on it.
+// (no term reads a slot another term of its level writes) and the 32 lanes
+// take them in turn, one __syncwarp between levels.  Slots of dead values are
+// reused from one level to the next, so a warp's array holds the live values
+// of a level, not the whole DAG; terms are sorted by branch shape inside a
+// level so lanes mostly agree on it.
 template <int LA, int LB, int LC, int LD> struct EriProg;
 
-#define RCHEM_WC_SMEM (96 * 1024)  // shared memory per block the warp count aims at
-#define WC_U 4                     // independent recurrence terms per lane and pass
+#define WC_U 4  // independent recurrence terms per lane and pass
+
+// Shared memory of an SM and of one block (sm_103: 228 KB per SM, at most 227 KB
+// per block, 1 KB of each block's share reserved by the runtime); the warps a
+// kernel of ~128 registers per thread can keep resident (65536 / (32 * 128)).
+#define RCHEM_SM_SMEM (228 * 1024)
+#define RCHEM_BLOCK_SMEM (227 * 1024)
+#define RCHEM_WC_MAX_WARPS 16
 
 template <int LA, int LB, int LC, int LD, typename R>
 struct WcShape {
     using P = EriProg<LA, LB, LC, LD>;
-    static constexpr int PER_WARP = P::SCR + (P::NT > P::NOUT ? P::NT : P::NOUT);  // elements of R
-    static constexpr int FIT = (int)(RCHEM_WC_SMEM / (PER_WARP * sizeof(R)));
-    static constexpr int WARPS = FIT < 1 ? 1 : (FIT > 4 ? 4 : FIT);
-    static constexpr size_t SMEM = (size_t)WARPS * PER_WARP * sizeof(R);
+    static constexpr int PER_WARP = P::SCR;  // elements of R
+    static constexpr size_t BYTES = (size_t)PER_WARP * sizeof(R);
+    // warps per block that keep the most warps resident on an SM (ties: the
+    // larger block, so a block's warps spread over the SM's four schedulers)
+    static constexpr int pick() {
+        int best = 1, best_res = 0;
+        for (int w = 1; w <= 8; ++w) {
+            const size_t blk = (size_t)w * BYTES;
+            if (blk > RCHEM_BLOCK_SMEM) break;
+            int nb = (int)(RCHEM_SM_SMEM / (blk + 1024));
+            int res = nb * w;
+            if (res > RCHEM_WC_MAX_WARPS) res = RCHEM_WC_MAX_WARPS;
+            if (res >= best_res) {
+                best_res = res;
+                best = w;
+            }
+        }
+        return best;
+    }
+    static constexpr int WARPS = pick();
+    static constexpr size_t SMEM = (size_t)WARPS * BYTES;
+    static_assert(BYTES <= RCHEM_BLOCK_SMEM, "a warp's recurrence values exceed a block's shared memory");
 };
 
 template <typename R>
@@ -381,15 +408,16 @@ __device__ __forceinline__ R wc_sel4(int n, const R *v) {  // v[0..3] = 1..4 tim
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int EPI = EPI_JK>
-__global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
+__global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
     using C = EriClass<LA, LB, LC, LD>;
     using P = EriProg<LA, LB, LC, LD>;
     using W = WcShape<LA, LB, LC, LD, R>;
     constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, L = C::L;
     extern __shared__ __align__(16) unsigned char wc_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    R *S = reinterpret_cast<R *>(wc_smem) + wib * W::PER_WARP;  // terms of the recurrences
-    R *A = S + P::SCR;                                           // accumulators, then the integrals
+    // the warp's array: accumulators [0, NT), Boys values and VRR terms above
+    // them; after the HRR the integrals (ab|cd) at [OUTB, OUTB + NOUT)
+    R *S = reinterpret_cast<R *>(wc_smem) + wib * W::PER_WARP;
     const int w = blockIdx.x * W::WARPS + wib;
     if (w >= a.ntasks) return;  // warp-uniform
     const EriTask tk = a.tasks[w];
@@ -401,7 +429,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
     }
     const int bidx = seg.bra, kidx = seg.ket0 + off;
     const ShellPair bp = a.pairs[bidx], kp = a.pairs[kidx];
-    for (int k = lane; k < P::NT; k += 32) A[k] = R(0);
+    for (int k = lane; k < P::NT; k += 32) S[k] = R(0);
     const R *btab = Tabs<R>::boys(a);
     const uint4 *vprog = P::vrr();
     const int *vlev = P::vrrlv();
@@ -427,11 +455,11 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         __syncwarp();  // the previous primitive quartet's terms have been read
 #pragma unroll
         for (int m = 0; m <= L; ++m)
-            if (lane == m) S[m] = F[m];
+            if (lane == m) S[P::NT + m] = F[m];
         __syncwarp();
         // one term: X a + Y b [+ n1 c (c_ - rho d)] [+ n2 ohpq g]
-        auto term = [&](const uint4 op, R ta, R tb, R tc, R td, R tg) {
-            const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
+        auto term = [&](const unsigned wd, R ta, R tb, R tc, R td, R tg) {
+            const int dir = wd & 3, ket = (wd >> 2) & 1, n1 = (wd >> 3) & 7, n2 = (wd >> 6) & 7;
             const R X = ket ? wc_sel3(dir, QC[0], QC[1], QC[2]) : wc_sel3(dir, PA[0], PA[1], PA[2]);
             const R Y = ket ? wc_sel3(dir, WQ[0], WQ[1], WQ[2]) : wc_sel3(dir, WP[0], WP[1], WP[2]);
             R v = rchem_fma(Y, tb, X * ta);
@@ -450,29 +478,30 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
                 for (int u = 0; u < WC_U; ++u) o[u] = t + 32 * u < e ? __ldg(vprog + t + 32 * u) : make_uint4(0, 0, 0, 0);
 #pragma unroll
                 for (int u = 0; u < WC_U; ++u) {
+                    const unsigned n1 = (o[u].w >> 3) & 7, n2 = (o[u].w >> 6) & 7;
                     ta[u] = S[o[u].x >> 16];
                     tb[u] = S[o[u].y & 0xffff];
-                    tc[u] = S[o[u].y >> 16];
-                    td[u] = S[o[u].z & 0xffff];
-                    tg[u] = S[o[u].z >> 16];
+                    tc[u] = n1 ? S[o[u].y >> 16] : R(0);
+                    td[u] = n1 ? S[o[u].z & 0xffff] : R(0);
+                    tg[u] = n2 ? S[o[u].z >> 16] : R(0);
                 }
 #pragma unroll
                 for (int u = 0; u < WC_U; ++u) {
-                    const R v = term(o[u], ta[u], tb[u], tc[u], td[u], tg[u]);
-                    if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
+                    const R v = term(o[u].w, ta[u], tb[u], tc[u], td[u], tg[u]);
+                    if (t + 32 * u < e) {
+                        const unsigned dest = o[u].x & 0xffff, tg1 = o[u].w >> 9;
+                        if (dest != 0xffffu) S[dest] = v;
+                        if (tg1) S[tg1 - 1] += v;  // a target: into its contraction accumulator
+                    }
                 }
             }
             __syncwarp();
         }
-        for (int k = lane; k < P::NT; k += 32) A[k] += S[__ldg(P::tgt() + k)];
     }
-    // HRR on the contracted [e0|f0]
-    __syncwarp();
-    for (int k = lane; k < P::NT; k += 32) S[k] = A[k];
+    // HRR on the contracted [e0|f0], in place
     R AB[3], CD[3];
     Tabs<R>::ab(bp, AB);
     Tabs<R>::ab(kp, CD);
-    __syncwarp();
     const uint2 *hprog = P::hrr();
     const int *hlev = P::hrrlv();
     auto hcoef = [&](const uint2 op) {
@@ -499,14 +528,21 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         }
         __syncwarp();
     }
-    for (int k = lane; k < P::NOUT; k += 32) A[k] = R(__ldg(P::onorm() + k)) * S[__ldg(P::out() + k)];
+    // the integrals (ab|cd) scaled by their component norms, in place (every
+    // output has a slot of its own); A(k) reads integral k
+    const unsigned short *oslot = P::out();
+    for (int k = lane; k < P::NOUT; k += 32) {
+        const int sk = __ldg(oslot + k);
+        S[sk] = R(__ldg(P::onorm() + k)) * S[sk];
+    }
     __syncwarp();
+    auto A = [&](int k) { return S[__ldg(oslot + k)]; };
     if constexpr (EPI == EPI_DIAG) {  // Schwarz bound sqrt(max |(ab|ab)|) of a diagonal quartet
         if constexpr (LA == LC && LB == LD) {
             double m = 0.0;
             for (int t = lane; t < NA * NB; t += 32) {
                 const int ia = t / NB, ib = t - ia * NB;
-                m = fmax(m, fabs((double)A[((ia * NB + ib) * NC + ia) * ND + ib]));
+                m = fmax(m, fabs((double)A(((ia * NB + ib) * NC + ia) * ND + ib)));
             }
             for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
             if (lane == 0) a.J[kidx] = sqrt(m);
@@ -517,7 +553,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         const int i0 = bp.aoA, j0 = bp.aoB, k0 = kp.aoA, l0s = kp.aoB;
         for (int t = lane; t < NA * NB * NC * ND; t += 32) {
             const int id = t % ND, ic = (t / ND) % NC, ib = (t / (ND * NC)) % NB, ia = t / (ND * NC * NB);
-            eri_put(a, (size_t)bp.mn, i0 + ia, j0 + ib, k0 + ic, l0s + id, (double)A[t]);
+            eri_put(a, (size_t)bp.mn, i0 + ia, j0 + ib, k0 + ic, l0s + id, (double)A(t));
         }
         return;
     }
@@ -536,7 +572,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ic = 0; ic < NC; ++ic)
             for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id), sum);
         atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, widen(sum * deg2));
     }
     for (int t = lane; t < NC * ND; t += 32) {  // J-hat ket: 2 (ab|cd) D_ab
@@ -544,7 +580,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ia = 0; ia < NA; ++ia)
             for (int ib = 0; ib < NB; ++ib)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib), sum);
         atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, widen(sum * deg2));
     }
     for (int t = lane; t < NA * NC; t += 32) {  // K-hat[a][c] += (ab|cd) D_bd
@@ -552,7 +588,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ib = 0; ib < NB; ++ib)
             for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id), sum);
         atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, widen(sum * deg));
     }
     for (int t = lane; t < NB * NC; t += 32) {  // K-hat[b][c] += (ab|cd) D_ad
@@ -560,7 +596,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ia = 0; ia < NA; ++ia)
             for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id), sum);
         atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, widen(sum * deg));
     }
     for (int t = lane; t < NA * ND; t += 32) {  // K-hat[a][d] += (ab|cd) D_bc
@@ -568,7 +604,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ib = 0; ib < NB; ++ib)
             for (int ic = 0; ic < NC; ++ic)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic), sum);
         atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, widen(sum * deg));
     }
     for (int t = lane; t < NB * ND; t += 32) {  // K-hat[b][d] += (ab|cd) D_ac
@@ -576,7 +612,7 @@ __global__ void __launch_bounds__(128) eri_wc_kernel(EriArgs a) {
         R sum = R(0);
         for (int ia = 0; ia < NA; ++ia)
             for (int ic = 0; ic < NC; ++ic)
-                sum = rchem_fma(A[WIDX(ia, ib, ic, id)], Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic), sum);
+                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic), sum);
         atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, widen(sum * deg));
     }
 #undef WIDX

@@ -351,7 +351,57 @@ def _levels(depth, order, key):
     return out, bounds
 
 
+def _allocate(levels, last_read, fixed, nfixed):
+    """Level-granular first-fit slot allocation.  ``levels``: node lists, level
+    by level (a node reads only nodes of lower levels); ``last_read[n]``: the
+    last level that reads n (absent: never read); ``fixed``: nodes that hold
+    the slots [0, nfixed) from the start.  A slot is reused once every reader
+    of its value has run, i.e. from the level after its last reader: within a
+    level no term writes a slot another term of that level reads, so the lanes
+    may take a level's terms in any order without synchronising.  Nodes in
+    ``skip`` get no slot.  Returns ({node: slot}, slots used)."""
+    import heapq
+
+    slot = dict(fixed)
+    free = []
+    nslot = nfixed
+    dying = {}
+    for v, lv in last_read.items():
+        dying.setdefault(lv, []).append(v)
+    for k in range(nfixed):
+        if k not in slot.values():
+            heapq.heappush(free, k)
+    for lev, nodes in enumerate(levels, start=1):
+        for v in dying.get(lev - 1, []):
+            if v in slot and slot[v] is not None:
+                heapq.heappush(free, slot[v])
+        for n in nodes:
+            if n not in last_read:
+                slot[n] = None
+                continue
+            if free:
+                slot[n] = heapq.heappop(free)
+            else:
+                slot[n] = nslot
+                nslot += 1
+    return slot, nslot
+
+
 def gen_prog(la, lb, lc, ld, choose_v, choose_h):
+    """The warp-cooperative program of one class.  Per-warp shared memory is
+    one array S of SCR values:
+      VRR phase: S[0, NT) the [e0|f0] contraction accumulators, S[NT + m] the
+        scaled Boys values F_m, the other VRR intermediates in S[NT + L + 1 ..);
+      HRR phase: the accumulators are the inputs in place; intermediates and
+        the outputs (ab|cd) take any dead slot, the outputs keeping theirs to
+        the end (out[k] is the slot of output k).
+    Slots are reused level by level (``_allocate``).  A VRR target is added
+    into its accumulator by the term that computes it; it keeps a slot only
+    if other terms read it.  Program words:
+      VRR uint4: x = dest | a << 16, y = b | c << 16, z = d | g << 16,
+                 w = dir | kind << 2 | n1 << 3 | n2 << 6 | (target + 1) << 9
+                 (dest 0xffff: no store; target + 1 = 0: not a target);
+      HRR uint2: x = dest | x << 16, y = y | dir << 16 | side << 24."""
     E, F = la + lb, lc + ld
     L = E + F
     idx, depth, recs, order = {}, {}, {}, []
@@ -382,6 +432,7 @@ def gen_prog(la, lb, lc, ld, choose_v, choose_h):
         k = L + 1 + len(order)
         kids = [r["a"], r["b"]] + ([r["c"], r["d"]] if r["n1"] else []) + ([r["g"]] if r["n2"] else [])
         depth[k] = 1 + max(depth[c] for c in kids)
+        r["kids"] = kids
         recs[k] = r
         order.append(k)
         idx[key] = k
@@ -389,8 +440,22 @@ def gen_prog(la, lb, lc, ld, choose_v, choose_h):
 
     targets = [(e, f) for e in comps_range(la, E) for f in comps_range(lc, F)]
     tgt = [node(e, f, 0) for (e, f) in targets]
-    vorder, vbounds = _levels(depth, order, lambda n: (recs[n]["kind"], recs[n]["n1"] > 0, recs[n]["n2"] > 0))
     NT = len(targets)
+    tgt_of = {}
+    for t, n in enumerate(tgt):
+        assert n > L, "a target is a Boys value: class too small for a program"
+        tgt_of[n] = t
+    vorder, vbounds = _levels(depth, order, lambda n: (recs[n]["kind"], recs[n]["n1"] > 0, recs[n]["n2"] > 0))
+    vlevels = [vorder[vbounds[i]:vbounds[i + 1]] for i in range(len(vbounds) - 1)]
+    vlast = {}
+    for n in order:
+        for c in recs[n]["kids"]:
+            vlast[c] = max(vlast.get(c, 0), depth[n])
+    for m in range(L + 1):
+        vlast.setdefault(m, 0)
+    vslot, vn = _allocate(vlevels, vlast, {m: m for m in range(L + 1)}, L + 1)
+    vabs = lambda n: NT + vslot[n]  # noqa: E731
+
     eidx = {e: k for k, e in enumerate(comps_range(la, E))}
     fidx = {f: k for k, f in enumerate(comps_range(lc, F))}
     nf = len(fidx)
@@ -434,34 +499,63 @@ def gen_prog(la, lb, lc, ld, choose_v, choose_h):
             for c in ijk_list(lc):
                 for d in ijk_list(ld):
                     outs.append((ket(a, b, c, d), comp_norm(a) * comp_norm(b) * comp_norm(c) * comp_norm(d)))
+    NOUT = len(outs)
     horder2, hbounds = _levels(hdepth, horder, lambda n: hrec[n]["side"])
-    scr = max(L + 1 + len(order), NT + len(horder))
-    assert scr < 65536
+    hlevels = [horder2[hbounds[i]:hbounds[i + 1]] for i in range(len(hbounds) - 1)]
+    assert len({n for n, _ in outs}) == NOUT, "a node is two outputs"
+    hlast = {}
+    for n in horder:
+        for c in (hrec[n]["x"], hrec[n]["y"]):
+            hlast[c] = max(hlast.get(c, 0), hdepth[n])
+    for k in range(NT):
+        hlast.setdefault(k, 0)
+    for n, _ in outs:
+        hlast[n] = len(hlevels) + 1  # outputs keep their slots to the end
+    hslot, hn = _allocate(hlevels, hlast, {k: k for k in range(NT)}, NT)
+    habs = lambda n: hslot[n]  # noqa: E731
+    scr = max(NT + vn, hn)
+    assert scr < 0xffff and NT < 2047
+    # every level: distinct destinations, none of them read by the same level,
+    # VRR destinations outside the accumulators
+    for lv in vlevels:
+        w = [vabs(n) for n in lv if vslot.get(n) is not None]
+        rd = {vabs(c) for n in lv for c in recs[n]["kids"]}
+        assert len(w) == len(set(w)) and not (set(w) & rd) and min(w + [NT]) >= NT
+    for lv in hlevels:
+        w = [habs(n) for n in lv]
+        rd = {habs(c) for n in lv for c in (hrec[n]["x"], hrec[n]["y"])}
+        assert len(w) == len(set(w)) and not (set(w) & rd) and max(w + [0]) < scr
+
     tag = "%d%d%d%d" % (la, lb, lc, ld)
-    lines = ["// warp-cooperative program of class (%d%d|%d%d): %d VRR terms in %d levels, %d HRR terms in %d levels"
-             % (la, lb, lc, ld, len(order), len(vbounds) - 1, len(horder), len(hbounds) - 1)]
+    lines = ["// warp-cooperative program of class (%d%d|%d%d): %d VRR terms in %d levels, %d HRR terms in %d levels,"
+             " %d shared values per warp" % (la, lb, lc, ld, len(order), len(vlevels), len(horder), len(hlevels), scr)]
     lines.append("static __device__ const uint4 rchem_vrr_%s[%d] = {" % (tag, len(vorder)))
     for n in vorder:
         r = recs[n]
-        lines.append("  {%du, %du, %du, %du}," % (n | (r["a"] << 16), r["b"] | (r["c"] << 16), r["d"] | (r["g"] << 16),
-                                                  r["dir"] | (r["kind"] << 8) | (r["n1"] << 16) | (r["n2"] << 24)))
+        dest = vabs(n) if vslot.get(n) is not None else 0xffff
+        g = vabs(r["g"]) if r["n2"] else 0
+        c = vabs(r["c"]) if r["n1"] else 0
+        d = vabs(r["d"]) if r["n1"] else 0
+        t1 = tgt_of[n] + 1 if n in tgt_of else 0
+        lines.append("  {%du, %du, %du, %du}," % (dest | (vabs(r["a"]) << 16), vabs(r["b"]) | (c << 16), d | (g << 16),
+                                                  r["dir"] | (r["kind"] << 2) | (r["n1"] << 3) | (r["n2"] << 6) | (t1 << 9)))
     lines.append("};")
     lines.append("static __device__ const int rchem_vrrlv_%s[%d] = {%s};" % (tag, len(vbounds), ", ".join(map(str, vbounds))))
-    lines.append("static __device__ const unsigned short rchem_tgt_%s[%d] = {%s};" % (tag, NT, ", ".join(map(str, tgt))))
     lines.append("static __device__ const uint2 rchem_hrr_%s[%d] = {" % (tag, max(1, len(horder2))))
     for n in horder2:
         r = hrec[n]
-        lines.append("  {%du, %du}," % (n | (r["x"] << 16), r["y"] | (r["dir"] << 16) | (r["side"] << 24)))
+        lines.append("  {%du, %du}," % (habs(n) | (habs(r["x"]) << 16), habs(r["y"]) | (r["dir"] << 16) | (r["side"] << 24)))
     if not horder2:
         lines.append("  {0u, 0u},")
     lines.append("};")
     lines.append("static __device__ const int rchem_hrrlv_%s[%d] = {%s};" % (tag, len(hbounds), ", ".join(map(str, hbounds))))
-    lines.append("static __device__ const unsigned short rchem_out_%s[%d] = {%s};" % (tag, len(outs), ", ".join(str(o[0]) for o in outs)))
-    lines.append("static __device__ const double rchem_onorm_%s[%d] = {%s};" % (tag, len(outs), ", ".join("%.17g" % o[1] for o in outs)))
+    lines.append("static __device__ const unsigned short rchem_out_%s[%d] = {%s};" % (tag, NOUT, ", ".join(str(habs(o[0])) for o in outs)))
+    lines.append("static __device__ const double rchem_onorm_%s[%d] = {%s};" % (tag, NOUT, ", ".join("%.17g" % o[1] for o in outs)))
     lines.append("template <> struct EriProg<%d,%d,%d,%d> {" % (la, lb, lc, ld))
-    lines.append("  static constexpr int NVL = %d, NHL = %d, NT = %d, NOUT = %d, SCR = %d;" % (len(vbounds) - 1, len(hbounds) - 1, NT, len(outs), scr))
-    for nm in ("vrr", "vrrlv", "tgt", "hrr", "hrrlv", "out", "onorm"):
-        ty = {"vrr": "uint4", "vrrlv": "int", "tgt": "unsigned short", "hrr": "uint2", "hrrlv": "int", "out": "unsigned short", "onorm": "double"}[nm]
+    lines.append("  static constexpr int NVL = %d, NHL = %d, NT = %d, NOUT = %d, SCR = %d;"
+                 % (len(vlevels), len(hlevels), NT, NOUT, scr))
+    for nm in ("vrr", "vrrlv", "hrr", "hrrlv", "out", "onorm"):
+        ty = {"vrr": "uint4", "vrrlv": "int", "hrr": "uint2", "hrrlv": "int", "out": "unsigned short", "onorm": "double"}[nm]
         lines.append("  __device__ static __forceinline__ const %s *%s() { return rchem_%s_%s; }" % (ty, nm, nm, tag))
     lines.append("};")
     return lines

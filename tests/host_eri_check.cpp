@@ -93,7 +93,8 @@ template <int LA, int LB, int LC, int LD>
 static void block_prog(const Sh &A, const Sh &B, const Sh &C, const Sh &D, double *res) {
     using K = EriClass<LA, LB, LC, LD>;
     using P = EriProg<LA, LB, LC, LD>;
-    std::vector<double> S(P::SCR, 0.0), acc(P::NT, 0.0);
+    // one warp's shared array: accumulators S[0, NT), Boys values at S[NT + m]
+    std::vector<double> S(P::SCR, 0.0);
     const double cp = std::sqrt(2.0) * std::pow(M_PI, 1.25);
     for (int i = 0; i < A.n; ++i)
         for (int j = 0; j < B.n; ++j) {
@@ -117,28 +118,32 @@ static void block_prog(const Sh &A, const Sh &B, const Sh &C, const Sh &D, doubl
                     const double T = p * qi * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]);
                     double F[K::L + 1];
                     boys_eval<K::L, double>(T, Kab * Kcd * rs, g_b64.data(), F);
-                    for (int m = 0; m <= K::L; ++m) S[m] = F[m];
+                    for (int m = 0; m <= K::L; ++m) S[P::NT + m] = F[m];
                     const double PA[3] = {Pc[0] - A.R[0], Pc[1] - A.R[1], Pc[2] - A.R[2]};
                     const double QC[3] = {Qc[0] - C.R[0], Qc[1] - C.R[1], Qc[2] - C.R[2]};
                     const double WP[3] = {-qi * PQ[0], -qi * PQ[1], -qi * PQ[2]};
                     const double WQ[3] = {pi * PQ[0], pi * PQ[1], pi * PQ[2]};
                     const double ohp = 0.5 / p, ohq = 0.5 / q, ohpq = 0.5 * ipq;
-                    for (int t = 0; t < P::vrrlv()[P::NVL]; ++t) {
+                    // each level's terms last to first: the GPU's lanes take them in
+                    // any order, so no term may read what another of its level writes
+                    for (int lv = 0; lv < P::NVL; ++lv)
+                    for (int t = P::vrrlv()[lv + 1] - 1; t >= P::vrrlv()[lv]; --t) {
                         const uint4 op = P::vrr()[t];
-                        const int dir = op.w & 3, ket = (op.w >> 8) & 1, n1 = (op.w >> 16) & 255, n2 = op.w >> 24;
+                        const int dir = op.w & 3, ket = (op.w >> 2) & 1, n1 = (op.w >> 3) & 7, n2 = (op.w >> 6) & 7;
+                        const int tg = (int)(op.w >> 9), dest = (int)(op.x & 0xffff);
                         const double X = ket ? QC[dir] : PA[dir], Y = ket ? WQ[dir] : WP[dir];
                         double v = Y * S[op.y & 0xffff] + X * S[op.x >> 16];
                         if (n1) v += n1 * (ket ? ohq : ohp) * (S[op.y >> 16] - (ket ? pi : qi) * S[op.z & 0xffff]);
                         if (n2) v += n2 * ohpq * S[op.z >> 16];
-                        S[op.x & 0xffff] = v;
+                        if (dest != 0xffff) S[dest] = v;
+                        if (tg) S[tg - 1] += v;
                     }
-                    for (int t = 0; t < P::NT; ++t) acc[t] += S[P::tgt()[t]];
                 }
         }
-    for (int t = 0; t < P::NT; ++t) S[t] = acc[t];
     const double AB[3] = {A.R[0] - B.R[0], A.R[1] - B.R[1], A.R[2] - B.R[2]};
     const double CD[3] = {C.R[0] - D.R[0], C.R[1] - D.R[1], C.R[2] - D.R[2]};
-    for (int t = 0; t < P::hrrlv()[P::NHL]; ++t) {
+    for (int lv = 0; lv < P::NHL; ++lv)
+    for (int t = P::hrrlv()[lv + 1] - 1; t >= P::hrrlv()[lv]; --t) {
         const uint2 op = P::hrr()[t];
         const int dir = (op.y >> 16) & 255, side = op.y >> 24;
         S[op.x & 0xffff] = S[op.x >> 16] + (side ? CD[dir] : AB[dir]) * S[op.y & 0xffff];
