@@ -123,6 +123,21 @@ typedef struct {
  */
 int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts);
 int rchem_jk_stats_get(rchem_basis b, rchem_jk_stats *out);
+/*
+ * One share of a Fock build, for splitting a single large system over
+ * nparts processes (one GPU each; no counterpart in the reference, whose
+ * JK_direct, src/basis.rs:383-428, is one serial loop nest): the bra shell
+ * pairs are split into nparts shares of about equal cost (longest-processing-
+ * time assignment of each pair's surviving quartets, deterministic, so every
+ * process computes the same split), and this call computes J and K from the
+ * quartets whose bra pair is in share `part` only -- symmetrised like a whole
+ * build, so the element-wise sum of the nparts results is rchem_jk_direct's J
+ * and K (one sum all-reduce of 2 n^2 doubles).  0 <= part < nparts; nparts = 1
+ * is the whole build.  Same options, arrays and errors as rchem_jk_direct;
+ * the handle replans (and re-captures its graph) when the share changes.
+ */
+int rchem_jk_direct_part(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts, int part,
+                         int nparts);
 /* Per integral class (21 classes, arrays of 21*4 / 21*2 entries, any may be
  * NULL) of the current work plan: the class (l_a,l_b,l_c,l_d), and for {FP64,
  * FP32} the shell quartets, primitive quartets and algorithmic FLOPs. */

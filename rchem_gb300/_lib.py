@@ -74,6 +74,7 @@ def lib():
     L.rchem_moment.argtypes = [vp, vp, i, i, i, vp, i]
     L.rchem_jk_direct.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_jk_direct_noalloc.argtypes = [vp, vp, vp, vp, p(JKOpts)]
+    L.rchem_jk_direct_part.argtypes = [vp, vp, vp, vp, p(JKOpts), i, i]
     L.rchem_gradient.argtypes = [vp, vp, vp, vp, p(JKOpts)]
     L.rchem_autotune.argtypes = [vp, p(JKOpts), vp]
     L.rchem_eigh_batched.argtypes = [i, i, vp, vp, vp, vp]
@@ -120,6 +121,6 @@ def exported_symbols():
         "rchem_jk_stats_get", "rchem_build_I", "rchem_jk_inmem", "rchem_build_I_packed", "rchem_jk_packed", "ijkl2intindex", "coulomb_repulsion", "overlap", "kinetic",
         "nuclear_attraction", "Fgamma", "contr_coulomb", "rchem_eri_prim_batch", "rchem_onee_prim_batch",
         "rchem_boys_batch", "rchem_peak_fma", "rchem_jk_direct_noalloc", "rchem_gradient", "rchem_batch_create",
-        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_jk_list_times", "rchem_eigh_batched",
+        "rchem_basis_layout", "rchem_autotune", "rchem_jk_class_stats", "rchem_jk_list_times", "rchem_jk_direct_part", "rchem_eigh_batched",
         "rchem_set_tile_shape", "rchem_rhf",
     ]

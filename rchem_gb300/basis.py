@@ -223,10 +223,14 @@ def moment(basis: Basis, center, order, device=False):
     return out
 
 
-def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
+def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False, part=0, nparts=1):
     """Fill J and K (in place, like the reference) from the density D.
     ``fp32_tau`` > 0 selects the mixed form; ``emulated`` computes the FP64
-    quartets in double-float arithmetic on the FP32 pipe."""
+    quartets in double-float arithmetic on the FP32 pipe.  ``nparts`` > 1
+    computes only share ``part`` of the bra shell pairs (rchem_jk_direct_part):
+    the sum over the nparts shares is the whole build."""
+    if not (0 <= part < nparts):
+        raise ValueError("part %d of %d" % (part, nparts))
     dev = _same_kind(D, J, K)
     D = D.contiguous() if dev else np.ascontiguousarray(D, dtype=np.float64)
     n = basis.nbf
@@ -235,8 +239,12 @@ def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=F
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
                     where=_lib.DEVICE if dev else _lib.HOST, emulated=1 if emulated else 0)
     _after_torch(basis, D, J, K)
-    _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
-                                          C.c_void_p(_ptr(K)), C.byref(o)))
+    if nparts == 1:
+        _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
+                                              C.c_void_p(_ptr(K)), C.byref(o)))
+    else:
+        _lib.check(_lib.lib().rchem_jk_direct_part(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),
+                                                   C.c_void_p(_ptr(K)), C.byref(o), int(part), int(nparts)))
 
 
 def build_I(basis: Basis, device=False):

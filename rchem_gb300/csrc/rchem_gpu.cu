@@ -362,6 +362,7 @@ struct rchem_basis_s {
     // plan
     bool planned = false;
     double plan_tau = -1.0, plan_tau32 = -1.0;
+    int plan_part = 0, plan_nparts = 1;  // share of the bra pairs the plan covers
     EriTask *d_tasks = nullptr;
     EriSeg *d_segs = nullptr;
     size_t tasks_cap = 0, segs_cap = 0;
@@ -692,8 +693,50 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
 // this many primitive quartets
 static const int kMinPrimPerLane = 16;
 
-static int plan_tasks(rchem_basis b, double tau, double tau32) {
-    if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32) return RCHEM_OK;
+// Split the bra shell pairs of a build into nparts shares of about equal cost:
+// each bra pair's cost is the algorithmic FLOPs of its surviving quartets
+// (both precisions), and the pairs go heaviest first to the least-loaded share
+// (ties: the lower share; equal costs in pair order).  Deterministic, so every
+// process computes the same split for the same basis and thresholds.
+static void split_bras(rchem_basis b, double tau, int nparts, std::vector<int> &owner) {
+    const std::vector<ShellPair> &P = b->pairs;
+    std::vector<double> cost(P.size(), 0.0);
+    for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
+        const PairGroup &gb = b->groups[gbi];
+        for (int gki = b->geom_group_begin[gb.geom]; gki < b->geom_group_end[gb.geom]; ++gki) {
+            const PairGroup &gk = b->groups[gki];
+            if (gk.cls > gb.cls || (gk.cls == gb.cls && gki > gbi)) continue;
+            const int k = quartet_kernel(gb.cls, gk.cls);
+            const double per = rchem_class_flops[k][0] * (double)gb.npp * gk.npp + rchem_class_flops[k][1];
+            for (int ib = gb.begin; ib < gb.end; ++ib) {
+                const double Qb = P[ib].Q;
+                if (!(Qb > 0.0)) continue;
+                int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
+                if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
+                cost[ib] += per * nk;
+            }
+        }
+    }
+    std::vector<int> order(P.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    std::vector<double> load(nparts, 0.0);
+    owner.assign(P.size(), 0);
+    for (int i : order) {
+        int best = 0;
+        for (int r = 1; r < nparts; ++r)
+            if (load[r] < load[best]) best = r;
+        owner[i] = best;
+        load[best] += cost[i];
+    }
+}
+
+// The work plan of a Fock build: every surviving unique quartet (or, with
+// nparts > 1, those whose bra pair belongs to share `part` of split_bras).
+static int plan_tasks(rchem_basis b, double tau, double tau32, int part = 0, int nparts = 1) {
+    if (b->planned && tau == b->plan_tau && tau32 == b->plan_tau32 && part == b->plan_part &&
+        nparts == b->plan_nparts)
+        return RCHEM_OK;
     std::vector<EriSeg> segs[RCHEM_NCLASS][2];
     std::vector<EriTask> lists[RCHEM_NCLASS][2];
     rchem_jk_stats st;
@@ -702,6 +745,8 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
     memset(b->class_quartets, 0, sizeof(b->class_quartets));
     memset(b->class_prims, 0, sizeof(b->class_prims));
     const std::vector<ShellPair> &P = b->pairs;
+    std::vector<int> owner;
+    if (nparts > 1) split_bras(b, tau, nparts, owner);
     for (int gbi = 0; gbi < (int)b->groups.size(); ++gbi) {
         const PairGroup &gb = b->groups[gbi];
         for (int gki = b->geom_group_begin[gb.geom]; gki < b->geom_group_end[gb.geom]; ++gki) {
@@ -717,6 +762,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
                 for (int ib = gb.begin; ib < gb.end; ++ib) {
                     const double Qb = P[ib].Q;
                     if (!(Qb > 0.0)) continue;
+                    if (nparts > 1 && owner[ib] != part) continue;
                     int nk = (tau > 0.0) ? count_ge(P, gk, tau / Qb) : (gk.end - gk.begin);
                     if (gki == gbi) nk = std::min(nk, ib - gb.begin + 1);
                     const int m = (tau32 > 0.0) ? std::min(nk, count_ge(P, gk, tau32 / Qb)) : nk;
@@ -799,6 +845,8 @@ static int plan_tasks(rchem_basis b, double tau, double tau32) {
     b->plan_version += 1;
     b->plan_tau = tau;
     b->plan_tau32 = tau32;
+    b->plan_part = part;
+    b->plan_nparts = nparts;
     return RCHEM_OK;
 }
 
@@ -1241,8 +1289,8 @@ static int record_build(rchem_basis b, bool any32, bool emul) {
     return RCHEM_OK;
 }
 
-extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts) {
-    NvtxRange nv("rchem_jk_direct");
+static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts, int part,
+                          int nparts) {
     if (!b || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "null argument");
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
@@ -1250,7 +1298,7 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
-    CKR(plan_tasks(b, tau, tau32));
+    CKR(plan_tasks(b, tau, tau32, part, nparts));
     const size_t nn = (size_t)b->packed;
     CK(cudaEventRecord(b->ev_t0, b->stream));
     CK(cudaMemcpyAsync(b->d_D, D, nn * sizeof(double),
@@ -1292,6 +1340,19 @@ extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) == cudaSuccess) b->last_stats.gpu_ms = ms;
     return RCHEM_OK;
+}
+
+extern "C" int rchem_jk_direct(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts) {
+    NvtxRange nv("rchem_jk_direct");
+    return jk_direct_impl(b, D, J, K, opts, 0, 1);
+}
+
+extern "C" int rchem_jk_direct_part(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts,
+                                    int part, int nparts) {
+    NvtxRange nv("rchem_jk_direct_part");
+    if (nparts < 1 || part < 0 || part >= nparts)
+        return set_err(RCHEM_ERR_INVALID, "part %d of %d", part, nparts);
+    return jk_direct_impl(b, D, J, K, opts, part, nparts);
 }
 
 // every unique surviving quartet (bra pair >= ket pair in the class order), as
@@ -2025,7 +2086,7 @@ extern "C" int rchem_jk_direct_noalloc(rchem_basis b, const double *D, double *J
                        RCHEM_NOALLOC_MAX_NBF);
     const double tau = (opts->schwarz_tau == 0.0) ? 1e-12 : (opts->schwarz_tau < 0.0 ? 0.0 : opts->schwarz_tau);
     const double tau32 = (opts->fp32_tau > 0.0) ? opts->fp32_tau : 0.0;
-    if (!b->planned || tau != b->plan_tau || tau32 != b->plan_tau32)
+    if (!b->planned || tau != b->plan_tau || tau32 != b->plan_tau32 || b->plan_nparts != 1)
         return set_err(RCHEM_ERR_INVALID,
                        "the basis has no work plan for these thresholds: call rchem_jk_direct once with the same "
                        "options first (planning may allocate)");

@@ -18,12 +18,13 @@ is initialised (NCCL on GPUs, gloo on CPUs; only the final gather uses it),
 else the process is a world of one.  Each rank must have selected its own GPU
 (``torch.cuda.set_device(local_rank)``) before creating handles.
 
-One Fock build of a single large system shards instead by bra pairs: the same
-``shard`` over per-pair costs (the kets that pass the Schwarz screen, say)
-gives every rank its bras, each rank accumulates partial J and K over its
-quartets, and ``allreduce_sum`` adds them (2 n^2 doubles per build).  The
-library's Fock build does not take a subset of bra pairs, so on GPUs only the
-batched form runs sharded.
+One Fock build of a single large system shards instead by bra pairs
+(``jk_sharded``): the library splits the bra shell pairs into one share per
+rank of about equal cost (``rchem_jk_direct_part``, the same deterministic
+split on every rank), each rank computes J and K from its share's quartets on
+its GPU, and ``allreduce_sum`` adds them (2 n^2 doubles per build, the only
+exchange).  ``shard`` applies the same longest-processing-time rule to any
+other per-item costs.
 
 The reference runs one molecule per process and has no distributed layer;
 this is new capability around its energy conventions.
@@ -173,3 +174,19 @@ def rhf_gradient_sharded(geometries, basis_set_name="6-31g-fit", group=None, thr
                  "gradient": np.array(g[k]), "converged": bool(r["converged"])} for k in range(len(local))]
 
     return run_sharded(list(geometries), costs, compute, group)
+
+
+def jk_sharded(basis, D, J, K, group=None, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False):
+    """One Fock build of ``basis`` split over the ranks of the process group:
+    rank r computes J and K from share r of the bra shell pairs
+    (``rchem_jk_direct_part``; every rank must hold the same basis and D),
+    then one sum all-reduce of J and K gives every rank the whole build.
+    Arrays as in ``JK_direct`` (host arrays: through the backend's device);
+    a world of one is a plain build."""
+    from .basis import JK_direct
+
+    rank, world = _rank_world(group)
+    JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau, emulated=emulated, part=rank,
+              nparts=world)
+    allreduce_sum(J, K, group=group)
+    return J, K
