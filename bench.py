@@ -19,7 +19,8 @@ region, wall clock).  ``roofline`` is the dominant class kernel, timed alone
 with CUDA events in this run, against the FP64 FMA peak measured in this run;
 ``roofline.build`` is the whole build.  ``forms`` holds the precision forms:
 FP32 below fp32_tau = 1e-6 and 1e-4 with native FP64 above (the stated mixed
-form), and double-float ("emulated FP64") above the threshold, each with its
+form; the Boys function of the FP32 quartets in FP64, or in FP32), and
+double-float ("emulated FP64") above the threshold, each with its
 converged-SCF energy and density against the FP64 SCF.
 
 CPU baselines (rank 0, N=1): ``cpu_baseline`` is the reference's algorithm
@@ -332,26 +333,31 @@ def fock_forms(rc, torch, b, J, K, Dh, J64, K64, run, steps, warmup, scf_ref):
     """The precision forms on the same workload: time, J/K at the timed
     density against FP64, and the converged SCF against the FP64 SCF."""
     out = {}
-    forms = (("mixed_1e-6", 1e-6, False, "FP32 for quartets with Q_ab Q_cd < 1e-6 (Boys function and recursion in "
-                                         "FP32 there), native FP64 above, FP64 accumulation: the stated mixed form"),
-             ("mixed_1e-4", 1e-4, False, "as mixed_1e-6 with the FP32 threshold at 1e-4"),
-             ("emulated", 0.0, True, "double-float (hi+lo float pairs, ~48-bit significand) on the FP32 pipe for "
-                                     "every quartet of the classes that have it, native FP64 for the rest: an "
-                                     "addition beyond the stated form"),
-             ("emulated_mixed_1e-6", 1e-6, True, "FP32 below 1e-6, double-float above: an addition beyond the "
-                                                 "stated form"))
+    forms = (("mixed_1e-6_boys64", 1e-6, False, True,
+              "FP32 for quartets with Q_ab Q_cd < 1e-6 with the Boys function and its downward recursion in FP64, "
+              "native FP64 above, FP64 accumulation: the stated mixed form, literally"),
+             ("mixed_1e-6", 1e-6, False, False,
+              "as mixed_1e-6_boys64 with the Boys function in FP32 too (its error, <= 2e-6 relative, is that of "
+              "the FP32 argument)"),
+             ("mixed_1e-4", 1e-4, False, False, "as mixed_1e-6 with the FP32 threshold at 1e-4"),
+             ("emulated", 0.0, True, False,
+              "double-float (hi+lo float pairs, ~48-bit significand) on the FP32 pipe for every quartet of the "
+              "classes that have it, native FP64 for the rest: an addition beyond the stated form"),
+             ("emulated_mixed_1e-6", 1e-6, True, False,
+              "FP32 below 1e-6, double-float above: an addition beyond the stated form"))
     ms64 = scf_ref["ms"]
-    for tag, tau32, emul, what in forms:
-        b.autotune(SCHWARZ_TAU, tau32, emulated=emul)
-        ms = float(np.mean(run(tau32, steps, warmup, emulated=emul)))
+    for tag, tau32, emul, b64, what in forms:
+        b.autotune(SCHWARZ_TAU, tau32, emulated=emul, fp32_boys64=b64)
+        ms = float(np.mean(run(tau32, steps, warmup, emulated=emul, fp32_boys64=b64)))
         st = b.stats()
         Jf, Kf = J.cpu().numpy(), K.cpu().numpy()
         t0 = time.perf_counter()
-        r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)
+        r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=emul, fp32_boys64=b64)
         torch.cuda.synchronize()
         t_scf = time.perf_counter() - t0
         out[tag] = {
-            "arithmetic": what, "fp32_tau": tau32, "emulated": emul, "ms": ms, "builds_per_s": 1000.0 / ms,
+            "arithmetic": what, "fp32_tau": tau32, "emulated": emul, "fp32_boys64": b64, "ms": ms,
+            "builds_per_s": 1000.0 / ms,
             "speedup_vs_fp64": ms64 / ms,
             "fp32_quartet_fraction": st["quartets_fp32"] / max(1, st["quartets_fp32"] + st["quartets_fp64"]),
             "dE_fixed_density_Eh": float(np.sum(Dh * (2 * (Jf - J64) - (Kf - K64)))),
@@ -540,17 +546,17 @@ def main():
     K = torch.empty_like(D)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def run(tau32, steps, warmup, emulated=False):
+    def run(tau32, steps, warmup, emulated=False, fp32_boys64=False):
         # device time of each build from the library's own CUDA events on the
         # stream its kernels run on (bracketing the copy of D in, the class
         # kernels and the copies of J and K out); the L2 flush runs before.
         for _ in range(warmup):
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64)
         ms = []
         for _ in range(steps):
             with torch.cuda.stream(stream):
                 flush.fill_(1)
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64)
             ms.append(b.stats()["gpu_ms"])
         torch.cuda.synchronize()
         return ms

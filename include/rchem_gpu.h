@@ -90,16 +90,23 @@ int rchem_V(rchem_basis b, double *out, int where);
  * src/integrals/os86.rs:775-828, normalised like S.  center: 3 host doubles. */
 int rchem_moment(rchem_basis b, const double *center, int ox, int oy, int oz, double *out, int where);
 
+/* Arithmetic flags of rchem_jk_opts.emulated (combinable). */
+#define RCHEM_JK_EMULATED 1    /* the FP64 quartets in double-float arithmetic on the FP32 pipe */
+#define RCHEM_JK_FP32_BOYS64 2 /* the FP32 quartets (below fp32_tau) evaluate the Boys function and its
+                                  downward recursion in FP64, from their FP32 argument and prefactor */
+
 /* Fock-build options.  Zero-initialised options mean: FP64 everywhere,
  * Schwarz threshold 1e-12, host arrays. */
 typedef struct {
     double schwarz_tau; /* drop quartets with Q_ab Q_cd < tau (0 => 1e-12; <0 => no screening) */
     double fp32_tau;    /* quartets with Q_ab Q_cd < fp32_tau in FP32, FP64 accumulation (0 => FP64 only) */
     int where;          /* RCHEM_HOST or RCHEM_DEVICE for D, J, K */
-    int emulated;       /* 1: the FP64 quartets in double-float arithmetic on the FP32 pipe
+    int emulated;       /* flags; 0: native FP64 above fp32_tau, FP32 Boys function below.
+                           RCHEM_JK_EMULATED: the FP64 quartets in double-float arithmetic
                            (~48-bit significand): every class with l_a+l_b+l_c+l_d <= 4, and
                            the larger classes whose list runs the warp-cooperative kernel
-                           (rchem_autotune's choice); the others stay FP64.  0: native FP64 */
+                           (rchem_autotune's choice); the others stay FP64.
+                           RCHEM_JK_FP32_BOYS64: see above.  Other bits: RCHEM_ERR_INVALID */
 } rchem_jk_opts;
 
 /* Work done by the last Fock build of a handle. */

@@ -17,6 +17,9 @@
 // libpyquante2/cints.c:72-115).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
+
 #include "rchem_types.h"
 #include "df64.cuh"
 #include "boys.cuh"
@@ -123,6 +126,23 @@ template <> struct Tabs<float> {
     static __device__ __forceinline__ void ab(const ShellPair &s, float *v) { v[0] = s.AB32[0]; v[1] = s.AB32[1]; v[2] = s.AB32[2]; }
 };
 
+// Scaled Boys values F[0..L] of one primitive quartet.  With a.f32_boys64 the
+// FP32 kernels evaluate the function and its downward recursion in FP64 from
+// the FP32 argument and prefactor, and round the results to FP32.
+template <int L, typename R>
+__device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R *btab, R *F) {
+    if constexpr (std::is_same<R, float>::value) {
+        if (a.f32_boys64) {
+            double Fd[L + 1];
+            boys_eval<L, double>((double)T, (double)pref, a.boys64, Fd);
+#pragma unroll
+            for (int m = 0; m <= L; ++m) F[m] = (float)Fd[m];
+            return;
+        }
+    }
+    boys_eval<L, R>(T, pref, btab, F);
+}
+
 template <int LA, int LB, int LC, int LD, typename R, int EPI>
 __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     using C = EriClass<LA, LB, LC, LD>;
@@ -162,7 +182,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
         const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
         const R pref = Kab * Kcd * rs;
         R F[L + 1];
-        boys_eval<L, R>(T, pref, btab, F);
+        eri_boys<L, R>(a, T, pref, btab, F);
         C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi_ * PQx, -qi_ * PQy, -qi_ * PQz, QC[0], QC[1], QC[2],
                            pi_ * PQx, pi_ * PQy, pi_ * PQz, ohp, ohq, R(0.5) * ipq, qi_, pi_);
     };
@@ -446,7 +466,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         const R qi_ = q * ipq, pi_ = p * ipq;
         const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
         R F[L + 1];
-        boys_eval<L, R>(T, Kab * Kcd * rs, btab, F);
+        eri_boys<L, R>(a, T, Kab * Kcd * rs, btab, F);
         const R WP[3] = {-qi_ * PQx, -qi_ * PQy, -qi_ * PQz}, WQ[3] = {pi_ * PQx, pi_ * PQy, pi_ * PQz};
         const R ohpq = R(0.5) * ipq;
         const R cp[4] = {ohp, ohp + ohp, R(3) * ohp, R(4) * ohp};

@@ -1264,7 +1264,7 @@ extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy,
 // ---------------------------------------------------------------------------
 // The device part of a Fock build on the handle's internal buffers:
 // d_D -> (d_D32) -> class kernels -> J-hat, K-hat -> d_Jo, d_Ko.
-static int record_build(rchem_basis b, bool any32, bool emul) {
+static int record_build(rchem_basis b, bool any32, bool emul, bool boys64 = false) {
     const size_t nn = (size_t)b->packed;
     const int th = 256;
     if (any32) {
@@ -1282,6 +1282,7 @@ static int record_build(rchem_basis b, bool any32, bool emul) {
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
+    a.f32_boys64 = boys64 ? 1 : 0;
     CKR(launch_lists(b, a, EPI_JK, any32, emul));
     k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->ngeom, b->d_geom, b->d_Jh,
                                                                         b->d_Kh, b->d_Jo, b->d_Ko);
@@ -1296,6 +1297,8 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
     memset(&o, 0, sizeof(o));
     if (opts) o = *opts;
     if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
+    if (o.emulated & ~(RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64))
+        return set_err(RCHEM_ERR_INVALID, "emulated=%d (flags RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64)", o.emulated);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     CKR(plan_tasks(b, tau, tau32, part, nparts));
@@ -1307,17 +1310,17 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
     // replay the captured build; capture it again when the plan has changed.
     // The legacy default stream cannot be captured: run the launches directly there.
-    const bool emul = o.emulated != 0;
+    const bool emul = (o.emulated & RCHEM_JK_EMULATED) != 0, boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) != 0;
     const bool capturable = b->stream != nullptr && b->stream != cudaStreamLegacy;
     if (!capturable) {
-        CKR(record_build(b, any32, emul));
-    } else if (b->graph_version != b->plan_version || b->graph_emul != (int)emul) {
+        CKR(record_build(b, any32, emul, boys64));
+    } else if (b->graph_version != b->plan_version || b->graph_emul != o.emulated) {
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
         b->graph_version = -1;
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = record_build(b, any32, emul);
+        const int rc = record_build(b, any32, emul, boys64);
         const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (rc != RCHEM_OK) {
             if (g) cudaGraphDestroy(g);
@@ -1328,7 +1331,7 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
         cudaGraphDestroy(g);
         if (ei != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "instantiating the Fock build: %s", cudaGetErrorString(ei));
         b->graph_version = b->plan_version;
-        b->graph_emul = (int)emul;
+        b->graph_emul = o.emulated;
     }
     if (capturable) CK(cudaGraphLaunch(b->graph, b->stream));
     const cudaMemcpyKind out = o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -1494,7 +1497,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             if (k < 2 * RCHEM_NCLASS) {  // an s/p class: its specialised kernel
                 const int cls = k / 2;
                 const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
-                                        : ((o.emulated && rchem_grad_sp_df64(cls, g, blocks, st)) ||
+                                        : (((o.emulated & RCHEM_JK_EMULATED) && rchem_grad_sp_df64(cls, g, blocks, st)) ||
                                            rchem_grad_sp_f64(cls, g, blocks, st));
                 if (!ok) return set_err(RCHEM_ERR_UNSUPPORTED, "gradient list %d has no specialised kernel", k);
                 CK(cudaGetLastError());
@@ -1592,6 +1595,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         a.Ddf = b->d_Ddf;
         a.J = b->d_Jh;
         a.K = b->d_Kh;
+        a.f32_boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) ? 1 : 0;
         for (int k = 0; k < RCHEM_NCLASS; ++k)
             for (int p = 0; p < 2; ++p) {
                 if (b->task_cnt[k][p] == 0 || (wc && !rchem_class_wc[k])) continue;
@@ -1599,7 +1603,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
                 a.ntasks = (int)b->task_cnt[k][p];
                 a.wc = b->wc[k][p];
                 float ms = 0.f;
-                CKR(time_list(b, a, k, p == 1 ? 1 : (o.emulated ? 2 : 0), &ms));
+                CKR(time_list(b, a, k, p == 1 ? 1 : ((o.emulated & RCHEM_JK_EMULATED) ? 2 : 0), &ms));
                 if (ms < best_ms[k][p]) {
                     best_ms[k][p] = ms;
                     best[k][p] = wc ? kMinPrimPerLane : cand[c];
@@ -1639,6 +1643,7 @@ extern "C" int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, flo
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
+    a.f32_boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) ? 1 : 0;
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
             ms[2 * k + p] = 0.f;
@@ -1646,7 +1651,7 @@ extern "C" int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, flo
             a.tasks = b->d_tasks + b->task_off[k][p];
             a.ntasks = (int)b->task_cnt[k][p];
             a.wc = b->wc[k][p];
-            CKR(time_list(b, a, k, p == 1 ? 1 : (o.emulated ? 2 : 0), &ms[2 * k + p]));
+            CKR(time_list(b, a, k, p == 1 ? 1 : ((o.emulated & RCHEM_JK_EMULATED) ? 2 : 0), &ms[2 * k + p]));
         }
     return RCHEM_OK;
 }
@@ -2165,6 +2170,8 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     if (o.diis < 0 || o.diis > RCHEM_DIIS_MAX) return set_err(RCHEM_ERR_INVALID, "diis = %d (0..%d)", o.diis, RCHEM_DIIS_MAX);
     if (o.max_iter < 1) return set_err(RCHEM_ERR_INVALID, "max_iter = %d", o.max_iter);
     if (o.jk.where != RCHEM_HOST && o.jk.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.jk.where);
+    if (o.jk.emulated & ~(RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64))
+        return set_err(RCHEM_ERR_INVALID, "jk.emulated=%d", o.jk.emulated);
     const int ng = b->ngeom;
     const long long packed = b->packed;
     int nmax = 0;
@@ -2237,7 +2244,7 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
         k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, Cv, 0, T2, 1.0, 0.0);
         k_scf_eigh<<<ng, RCHEM_EIGH_THREADS, esm, st>>>(geo, T2, eps, T1);
         k_scf_gemm<<<ng, th, 0, st>>>(geo, Cv, 0, T1, 0, Cn, 1.0, 0.0);
-        std::swap(Cv, Cn);
+        k_scf_copy<<<ng, th, 0, st>>>(geo, Cn, Cv);  // the new orbitals (a copy keeps the pointers fixed for capture)
         k_scf_density<<<ng, th, 0, st>>>(geo, d_nocc, Cv, eps, Dd, Ww);
         CK(cudaGetLastError());
         return RCHEM_OK;
@@ -2245,54 +2252,118 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     CKR(density(H, D, nullptr));  // core-Hamiltonian guess
     rchem_jk_opts jo = o.jk;
     jo.where = RCHEM_DEVICE;
-    std::vector<double> eg(ng), dm(ng), eprev(ng, 0.0);
-    int it = 0, nstored = 0, newest = 0;
-    bool conv = false;
-    for (it = 1; it <= o.max_iter; ++it) {
-        NvtxRange nv_it("scf iteration");
-        CKR(rchem_jk_direct(b, D, J, K, &jo));
-        k_scf_fock<<<eb, th, 0, st>>>(packed, H, J, K, F);
+    std::vector<double> eg(ng);
+    // the iteration's state lives on the device (ring slot, count, stop flag)
+    ScfState *d_st = nullptr;
+    double *d_eprev = nullptr;
+    CK(cudaMalloc(&d_st, sizeof(ScfState)));
+    guards.p.push_back(d_st);
+    CK(cudaMalloc(&d_eprev, ng * sizeof(double)));
+    guards.p.push_back(d_eprev);
+    CK(cudaMemsetAsync(d_st, 0, sizeof(ScfState), st));
+    CK(cudaMemsetAsync(d_eprev, 0, ng * sizeof(double), st));
+    const double tau = (jo.schwarz_tau == 0.0) ? 1e-12 : (jo.schwarz_tau < 0.0 ? 0.0 : jo.schwarz_tau);
+    const double tau32 = (jo.fp32_tau > 0.0) ? jo.fp32_tau : 0.0;
+    CKR(plan_tasks(b, tau, tau32));
+    bool any32 = false;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
+    const bool emul = (jo.emulated & RCHEM_JK_EMULATED) != 0, boys64 = (jo.emulated & RCHEM_JK_FP32_BOYS64) != 0;
+    // One iteration, every argument fixed (state-driven), so the same launches
+    // can be captured once and replayed:  J, K of D (the Fock build on the
+    // handle's buffers), F = H + 2J - K, the energies, the DIIS step, the
+    // Roothaan step, max |D - Dold|, then k_scf_check.
+    auto iteration = [&](cudaGraphConditionalHandle h, int use_h) -> int {
+        CK(cudaMemcpyAsync(b->d_D, D, bytes, cudaMemcpyDeviceToDevice, st));
+        CKR(record_build(b, any32, emul, boys64));
+        k_scf_fock<<<eb, th, 0, st>>>(packed, H, b->d_Jo, b->d_Ko, F);
         k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, nullptr, d_e, d_dm);
         const double *Fuse = F;
         if (o.diis > 0) {
-            // error X^T (FDS - SDF) X into the newest ring slot, F beside it
-            newest = (it - 1) % o.diis;
-            nstored = std::min(nstored + 1, o.diis);
+            // error X^T (FDS - SDF) X into this iteration's ring slot, F beside it
+            k_scf_diis_slot<<<1, 32, 0, st>>>(d_st, o.diis);
             k_scf_gemm<<<ng, th, 0, st>>>(geo, F, 0, D, 0, T1, 1.0, 0.0);
             k_scf_gemm<<<ng, th, 0, st>>>(geo, T1, 0, S, 0, T2, 1.0, 0.0);
             k_scf_antisym<<<ng, th, 0, st>>>(geo, T2, T1);
             k_scf_gemm<<<ng, th, 0, st>>>(geo, X, 1, T1, 0, T2, 1.0, 0.0);
-            k_scf_gemm<<<ng, th, 0, st>>>(geo, T2, 0, X, 0, Eh + (size_t)newest * packed, 1.0, 0.0);
-            CK(cudaMemcpyAsync(Fh + (size_t)newest * packed, F, bytes, cudaMemcpyDeviceToDevice, st));
-            if (nstored >= 2) {
-                k_scf_diis<<<ng, th, 0, st>>>(geo, Eh, packed, nstored, d_coef);
-                k_scf_extrapolate<<<ng, th, 0, st>>>(geo, Fh, packed, nstored, newest, d_coef, Fx);
-                Fuse = Fx;
-            }
+            k_scf_gemm<<<ng, th, 0, st>>>(geo, T2, 0, X, 0, Eh, 1.0, 0.0, d_st, packed);
+            k_scf_store_slot<<<ng, th, 0, st>>>(geo, F, Fh, packed, d_st);
+            k_scf_diis<<<ng, th, 0, st>>>(geo, Eh, packed, d_st, d_coef);
+            k_scf_extrapolate<<<ng, th, 0, st>>>(geo, Fh, packed, d_st, d_coef, Fx);
+            Fuse = Fx;
             CK(cudaGetLastError());
         }
-        CK(cudaMemcpyAsync(Dold, D, bytes, cudaMemcpyDeviceToDevice, st));
+        k_scf_copy<<<ng, th, 0, st>>>(geo, D, Dold);
         CKR(density(Fuse, D, nullptr));
         // change of the density: max |D - Dold| (the pass's energy sum lands in scratch)
         k_scf_energy<<<ng, th, 0, st>>>(geo, H, F, D, Dold, d_coef, d_dm);
+        k_scf_check<<<1, th, 0, st>>>(d_st, ng, d_e, d_eprev, d_dm, o.thresh_e, o.thresh_d, o.max_iter, h, use_h);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(eg.data(), d_e, ng * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(dm.data(), d_dm, ng * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (it > 1) {
-            bool ok = true;
-            double dmax = 0.0;
-            for (int g = 0; g < ng; ++g) {
-                ok = ok && std::fabs(eg[g] - eprev[g]) < o.thresh_e;
-                dmax = std::max(dmax, dm[g]);
-            }
-            if (ok && dmax < o.thresh_d) {
-                conv = true;
-                break;
-            }
+        return RCHEM_OK;
+    };
+    // The whole loop as one graph launch: the iteration captured into the body
+    // of a WHILE conditional node whose condition k_scf_check clears on
+    // convergence or at max_iter.  Where that cannot be built (the legacy
+    // default stream cannot be captured), the host launches one iteration at a
+    // time and reads the stop flag after each.
+    bool done_in_graph = false;
+    const bool capturable = st != nullptr && st != cudaStreamLegacy;
+    if (capturable) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        cudaGraphConditionalHandle h = 0;
+        bool built = cudaGraphCreate(&g, 0) == cudaSuccess &&
+                     cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        cudaGraph_t body = nullptr;
+        if (built) {
+            // zeroed raw storage: the struct's union of node kinds has no default constructor
+            alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)];
+            memset(npbuf, 0, sizeof(npbuf));
+            cudaGraphNodeParams &np = *reinterpret_cast<cudaGraphNodeParams *>(npbuf);
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = h;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            built = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+            if (built) body = np.conditional.phGraph_out[0];
         }
-        eprev = eg;
+        if (built && cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                         cudaSuccess) {
+            const int rc = iteration(h, 1);
+            const cudaError_t ec = cudaStreamEndCapture(st, &body);
+            built = rc == RCHEM_OK && ec == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        } else {
+            built = false;
+        }
+        if (built) {
+            NvtxRange nv_loop("scf loop (one graph launch)");
+            const cudaError_t el = cudaGraphLaunch(ge, st);
+            const cudaError_t es = el == cudaSuccess ? cudaStreamSynchronize(st) : el;
+            cudaGraphExecDestroy(ge);
+            cudaGraphDestroy(g);
+            if (es != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "SCF loop graph: %s", cudaGetErrorString(es));
+            done_in_graph = true;
+        } else {
+            if (ge) cudaGraphExecDestroy(ge);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();  // clear a construction error; the host-driven loop follows
+        }
     }
+    ScfState hs;
+    memset(&hs, 0, sizeof(hs));
+    if (done_in_graph) {
+        CK(cudaMemcpy(&hs, d_st, sizeof(ScfState), cudaMemcpyDeviceToHost));
+    } else {
+        for (int k = 0; k < o.max_iter && !hs.stop; ++k) {
+            NvtxRange nv_it("scf iteration");
+            CKR(iteration(0, 0));
+            CK(cudaMemcpyAsync(&hs, d_st, sizeof(ScfState), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+        }
+    }
+    b->last_stats = b->plan_stats;
+    int it = hs.it;
+    const bool conv = hs.converged != 0;
     if (it > o.max_iter) it = o.max_iter;
     // energies at the final density with its own Fock matrix; W from that F's orbitals
     CKR(rchem_jk_direct(b, D, J, K, &jo));

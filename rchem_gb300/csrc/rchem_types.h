@@ -99,6 +99,7 @@ struct EriArgs {
     double *eri;           // ERI-tensor epilogue output: dense nbf^4, or packed (eri_packed)
     int eri_packed;        // 1: one value per unique integral at the 8-fold index (rchem_eri_pack8)
     int wc;                // J/K epilogue of a large class: 1 = warp-cooperative kernel, 0 = one lane group per quartet
+    int f32_boys64;        // FP32 quartets: Boys function and downward recursion in FP64
 };
 
 // Shell as the planner sees it.

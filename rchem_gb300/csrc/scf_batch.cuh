@@ -14,15 +14,28 @@
 #define RCHEM_SCF_THREADS 256
 #define RCHEM_DIIS_MAX 8
 
+// The loop's state on the device, so that one captured iteration serves every
+// iteration: the DIIS ring position and length, the iteration count and the
+// stop decision (taken on the device by k_scf_check).
+struct ScfState {
+    int it;         // iterations completed
+    int nstored;    // Fock/error pairs held in the DIIS ring
+    int newest;     // ring slot of this iteration's pair
+    int converged;  // 1 once every geometry met the thresholds
+    int stop;       // 1 once converged or at the iteration cap
+    int pad[3];
+};
+
 // C = alpha op(A) op(B) + beta C for every geometry (op = transpose if tA/tB);
 // A, B, C packed.  n <= 64: operands are read through L1, no tiling needed.
+// With st, C is the DIIS ring slot st->newest of a ring of stride `slot`.
 __global__ void __launch_bounds__(RCHEM_SCF_THREADS)
     k_scf_gemm(const GeomDev *geo, const double *A, int tA, const double *B, int tB, double *C, double alpha,
-               double beta) {
+               double beta, const ScfState *st = nullptr, long long slot = 0) {
     const GeomDev g = geo[blockIdx.x];
     const int n = g.n;
     const double *a = A + g.moff, *b = B + g.moff;
-    double *c = C + g.moff;
+    double *c = C + g.moff + (st ? (long long)st->newest * slot : 0);
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         const int i = e / n, j = e - i * n;
         double s = 0.0;
@@ -83,15 +96,39 @@ __global__ void k_scf_antisym(const GeomDev *geo, const double *T, double *C) {
     }
 }
 
-// DIIS: B_ij = <e_i, e_j> over the m stored error matrices (slots of the ring
-// buffers, stride `packed`), then the (m+1) x (m+1) Pulay system solved by
-// Gaussian elimination with partial pivoting (one thread); a singular system
-// keeps the newest Fock matrix.  coef[g][0..m) receives the coefficients in
-// slot order.
+// This iteration's DIIS ring slot (one thread).
+__global__ void k_scf_diis_slot(ScfState *st, int diis) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->newest = st->it % diis;
+        st->nstored = min(st->nstored + 1, diis);
+    }
+}
+
+// F into the DIIS ring slot st->newest (stride `packed`)
+__global__ void k_scf_store_slot(const GeomDev *geo, const double *F, double *Fh, long long packed,
+                                 const ScfState *st) {
+    const GeomDev g = geo[blockIdx.x];
+    double *dst = Fh + (long long)st->newest * packed + g.moff;
+    for (int e = threadIdx.x; e < g.n * g.n; e += blockDim.x) dst[e] = F[g.moff + e];
+}
+
+// B = A over every geometry's block
+__global__ void k_scf_copy(const GeomDev *geo, const double *A, double *B) {
+    const GeomDev g = geo[blockIdx.x];
+    for (int e = threadIdx.x; e < g.n * g.n; e += blockDim.x) B[g.moff + e] = A[g.moff + e];
+}
+
+// DIIS: B_ij = <e_i, e_j> over the m = st->nstored stored error matrices
+// (slots of the ring buffers, stride `packed`), then the (m+1) x (m+1) Pulay
+// system solved by Gaussian elimination with partial pivoting (one thread); a
+// singular system keeps the newest Fock matrix.  coef[g][0..m) receives the
+// coefficients in slot order.  Nothing to do before two pairs are stored.
 __global__ void __launch_bounds__(RCHEM_SCF_THREADS)
-    k_scf_diis(const GeomDev *geo, const double *E, long long packed, int m, double *coef) {
+    k_scf_diis(const GeomDev *geo, const double *E, long long packed, const ScfState *st, double *coef) {
     __shared__ double red[RCHEM_SCF_THREADS / 32];
     __shared__ double Bm[RCHEM_DIIS_MAX + 1][RCHEM_DIIS_MAX + 2];
+    const int m = st->nstored;
+    if (m < 2) return;  // block-uniform
     const GeomDev g = geo[blockIdx.x];
     const int nn = g.n * g.n;
     for (int i = 0; i < m; ++i)
@@ -145,14 +182,16 @@ __global__ void __launch_bounds__(RCHEM_SCF_THREADS)
 }
 
 // Fx = sum_i coef[g][i] F_i (ring buffer slots), or F_newest when every
-// coefficient is zero (a singular DIIS system)
+// coefficient is zero (a singular DIIS system) or fewer than two pairs are stored
 __global__ void __launch_bounds__(RCHEM_SCF_THREADS)
-    k_scf_extrapolate(const GeomDev *geo, const double *Fh, long long packed, int m, int newest, const double *coef,
+    k_scf_extrapolate(const GeomDev *geo, const double *Fh, long long packed, const ScfState *st, const double *coef,
                       double *Fx) {
     const GeomDev g = geo[blockIdx.x];
+    const int m = st->nstored, newest = st->newest;
     const double *cg = coef + (size_t)blockIdx.x * RCHEM_DIIS_MAX;
     bool any = false;
-    for (int i = 0; i < m; ++i) any |= cg[i] != 0.0;
+    if (m >= 2)
+        for (int i = 0; i < m; ++i) any |= cg[i] != 0.0;
     for (int k = threadIdx.x; k < g.n * g.n; k += blockDim.x) {
         const long long o = g.moff + k;
         double s = 0.0;
@@ -203,5 +242,39 @@ __global__ void k_scf_density(const GeomDev *geo, const int *nocc, const double 
         }
         D[g.moff + e] = d;
         if (W) W[g.moff + e] = wv;
+    }
+}
+
+// End of an iteration (one block): this iteration's energies e against the
+// previous ones and the density change dm against the thresholds, as the
+// host-side loop tests them (no test on the first iteration); eprev = e; the
+// iteration count; the stop decision (converged, or the iteration cap).  In a
+// graph with a WHILE node, the loop continues while the node's condition is
+// non-zero: the decision goes there too (use_handle), so the loop always ends
+// by max_iter.
+__global__ void __launch_bounds__(RCHEM_SCF_THREADS)
+    k_scf_check(ScfState *st, int ng, const double *e, double *eprev, const double *dm, double thresh_e,
+                double thresh_d, int max_iter, cudaGraphConditionalHandle h, int use_handle) {
+    __shared__ double red[RCHEM_SCF_THREADS / 32];
+    int ok = 1;
+    double m = 0.0;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        ok &= fabs(e[g] - eprev[g]) < thresh_e ? 1 : 0;
+        m = fmax(m, dm[g]);
+    }
+    ok = __syncthreads_and(ok);
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) eprev[g] = e[g];
+    if (threadIdx.x == 0) {
+        double mm = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) mm = fmax(mm, red[k]);
+        const int it = st->it + 1;
+        const int conv = (it > 1 && ok && mm < thresh_d) ? 1 : 0;
+        st->it = it;
+        st->converged = conv;
+        st->stop = (conv || it >= max_iter) ? 1 : 0;
+        if (use_handle) cudaGraphSetConditional(h, st->stop ? 0u : 1u);
     }
 }

@@ -3,7 +3,9 @@ then print the per-class work of the plan (``python -m rchem_gb300.profile_build
 
 Workloads: the single-geometry configurations of ``rchem_gb300.geometry``
 (h2o_sto3g, h2o8_631g, h2o4_631gss, h2o32_631gs) and ``batch512_631g`` (512
-water monomers/dimers/trimers in one batched handle).  The density (and, with
+water monomers/dimers/trimers in one batched handle).  ``--onee`` builds S, T
+and V instead; ``--scf`` (batch only) runs the library's SCF loop, one
+iteration per host launch so every kernel is an ordinary launch.  The density (and, with
 ``--gradient``, the energy-weighted density) is a seeded random symmetric
 matrix: the kernels do the same work for any density.
 
@@ -32,13 +34,19 @@ def main(argv=None):
     ap.add_argument("--emulated", action="store_true", help="double-float arithmetic for the FP64 quartets")
     ap.add_argument("--gradient", action="store_true", help="run the nuclear gradient instead of Fock builds")
     ap.add_argument("--autotune", action="store_true", help="autotune the tile shapes before the builds")
+    ap.add_argument("--onee", action="store_true", help="build S, T and V (the one-electron class kernels) instead")
+    ap.add_argument("--scf", action="store_true",
+                    help="run the library's SCF loop (rchem_rhf) on the legacy default stream, one iteration per "
+                         "host launch, instead")
     a = ap.parse_args(argv)
     import numpy as np
     import torch
 
-    from . import batch, geometry
-    from .basis import Basis, JK_direct
+    from . import _lib, batch, geometry
+    from .basis import S, T, V, Basis, JK_direct
     from .scf import gradient
+
+    L = _lib.lib()
 
     rng = np.random.default_rng(0)
     if a.workload == "batch512_631g":
@@ -51,8 +59,15 @@ def main(argv=None):
         D, W = torch.from_numpy(Dh).cuda(), torch.from_numpy(Wh).cuda()
         if a.autotune:
             b.autotune(1e-12, a.fp32_tau, emulated=a.emulated)
+        if a.scf:
+            b.set_stream(0)
         for _ in range(a.builds):
-            if a.gradient:
+            if a.scf:
+                batch.rhf_native(b, fp32_tau=a.fp32_tau, emulated=a.emulated)
+            elif a.onee:
+                for fn in (L.rchem_S, L.rchem_T, L.rchem_V):
+                    batch._packed_matrix(fn, b)
+            elif a.gradient:
                 batch.gradient_batch(b, {"D": D, "W": W})
             else:
                 J, K = torch.empty_like(D), torch.empty_like(D)
@@ -70,12 +85,14 @@ def main(argv=None):
             b.autotune(1e-12, a.fp32_tau, emulated=a.emulated)
         torch.cuda.synchronize()
         for _ in range(a.builds):
-            if a.gradient:
+            if a.onee:
+                S(b, device=True), T(b, device=True), V(b, device=True)
+            elif a.gradient:
                 gradient(b, {"D": D, "W": W})
             else:
                 JK_direct(J, K, b, D, fp32_tau=a.fp32_tau, emulated=a.emulated)
     torch.cuda.synchronize()
-    if not a.gradient:
+    if not (a.gradient or a.onee or a.scf):
         print(json.dumps(b.class_stats()))
     b.close()
 

@@ -143,6 +143,34 @@ def test_native_rhf_matches_python_driver(gpu):
     assert abs(r1["e_nuc"][0] - float(g["e_nuc"])) < 1e-12
 
 
+def test_native_rhf_graph_loop_equals_host_loop(gpu):
+    """rchem_rhf runs its loop as one graph launch (a WHILE conditional node
+    whose condition the device-side convergence check clears) on a capturable
+    stream, and one iteration per host launch on the legacy default stream,
+    which cannot be captured: the same iterations, energies and densities."""
+    import torch
+
+    import rchem_gb300 as rc
+
+    side = torch.cuda.Stream()  # a capturable stream of the caller's
+    for emulated, tau32 in ((False, 0.0), (True, 1e-6)):
+        bb = rc.batch.BatchBasis(_geoms(9, seed=4), "6-31g-fit")
+        try:
+            rg = rc.batch.rhf_native(bb, thresh_e=1e-11, thresh_d=1e-8, fp32_tau=tau32, emulated=emulated)
+            bb.set_stream(0)  # the legacy default stream: the host-driven loop
+            rh = rc.batch.rhf_native(bb, thresh_e=1e-11, thresh_d=1e-8, fp32_tau=tau32, emulated=emulated)
+            assert rg["converged"] and rh["converged"]
+            assert rg["iterations"] == rh["iterations"]
+            np.testing.assert_allclose(rg["e_total"], rh["e_total"], atol=1e-11, rtol=0)
+            assert float((rg["D"] - rh["D"]).abs().max()) < 1e-10
+            # an iteration cap ends the graph loop too, unconverged
+            bb.set_stream(side.cuda_stream)
+            rc_ = rc.batch.rhf_native(bb, max_iter=3)
+            assert rc_["iterations"] == 3 and not rc_["converged"]
+        finally:
+            bb.close()
+
+
 def test_native_rhf_rejects_large_geometries(gpu):
     import rchem_gb300 as rc
 
