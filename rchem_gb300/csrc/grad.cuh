@@ -14,6 +14,8 @@
 // and only the 9 centre derivatives leave the thread (translational
 // invariance gives the fourth centre).
 #pragma once
+#include <type_traits>
+
 #include "boys.cuh"
 #include "df64.cuh"
 #include "md.cuh"
@@ -117,21 +119,25 @@ __device__ __forceinline__ double gr_cnorm(const int *p) {
 
 // Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
 // Hermite index with t+u+v <= bmax (stored compactly in md_tuv order): the ket of one component
-// contracted with the Coulomb integrals once, reused by every bra component.
+// contracted with the Coulomb integrals once, reused by every bra component.  The sum is
+// nested one direction at a time (one FMA per term instead of a product and an FMA).
 template <typename T>
 __device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
                                         int bmax, T *Z) {
+    const T *ex = Ek[0][c[0]][d[0]], *ey = Ek[1][c[1]][d[1]], *ez = Ek[2][c[2]][d[2]];
+    const int nx = c[0] + d[0], ny = c[1] + d[1], nz = c[2] + d[2];
     for (int t = 0; t <= bmax; ++t)
         for (int u = 0; u <= bmax - t; ++u)
             for (int v = 0; v <= bmax - t - u; ++v) {
                 T z = T(0);
-                for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
-                    const T fx = Ek[0][c[0]][d[0]][tt];
-                    for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
-                        const T fy = fx * Ek[1][c[1]][d[1]][uu];
-                        for (int vv = 0; vv <= c[2] + d[2]; ++vv)
-                            z = rchem_fma(fy * Ek[2][c[2]][d[2]][vv], R[md_tuv(t + tt, u + uu, v + vv)], z);
+                for (int tt = 0; tt <= nx; ++tt) {
+                    T zy = T(0);
+                    for (int uu = 0; uu <= ny; ++uu) {
+                        T zz = T(0);
+                        for (int vv = 0; vv <= nz; ++vv) zz = rchem_fma(ez[vv], R[md_tuv(t + tt, u + uu, v + vv)], zz);
+                        zy = rchem_fma(ey[uu], zz, zy);
                     }
+                    z = rchem_fma(ex[tt], zy, z);
                 }
                 Z[md_tuv(t, u, v)] = z;  // compact (t,u,v) order: only t+u+v <= bmax is stored
             }
@@ -247,7 +253,12 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
         gr_comp(ld, k, cD[k]);
         nD[k] = gr_cnorm(cD[k]);
     }
-    R Gam[GR_MAXC4];
+    // FP64: Gamma is formed where it is used (five density loads and a few FMAs
+    // per bra pair, against a 10 KB local array per thread); the narrower
+    // forms keep the array, formed once in FP64 and rounded.
+    constexpr bool kGamArray = !std::is_same<R, double>::value;
+    R Gam[kGamArray ? GR_MAXC4 : 1];
+    if constexpr (kGamArray)
     for (int kc = 0; kc < nc; ++kc)
         for (int kd = 0; kd < nd; ++kd) {
             const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
@@ -268,7 +279,7 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int L1 = la + lb + lc + ld + 1;
     R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
-    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN];
+    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN], H0[GR_ZN];
     // work units: (primitive quartet, ket component pair); the G lanes split them
     // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
     const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
@@ -299,56 +310,112 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
                         for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
             }
         }
-        int s[3];
         const int kc = kcd / nd, kd = kcd - kc * nd;
-        const R *Gq = Gam + (kc * nd + kd) * na * nb;
-        // ket contracted with R: unshifted (bra may be shifted by one) and C-shifted
-        gr_zvec<R>(Ek, cC[kc], cD[kd], Rt, la + lb + 1, Z0);
+        const R *Gq = Gam + (kGamArray ? (kc * nd + kd) * na * nb : 0);
+        const int *Cc = cC[kc];
+        const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
+        const double Dls = Dg[l_ * n + s_], wcd = deg * nC[kc] * nD[kd];
+        // ket contracted with R: unshifted (the bra may be shifted by one) and C-shifted
+        gr_zvec<R>(Ek, Cc, cD[kd], Rt, la + lb + 1, Z0);
         for (int x = 0; x < 3; ++x) {
-            s[0] = cC[kc][0];
-            s[1] = cC[kc][1];
-            s[2] = cC[kc][2];
+            int s[3] = {Cc[0], Cc[1], Cc[2]};
             s[x] += 1;
             gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
-            if (cC[kc][x] > 0) {
+            if (Cc[x] > 0) {
                 s[x] -= 2;
                 gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
             }
         }
+        // centre C through the bra Hermite density H0_tuv = sum_ab Gamma_ab E^{ab}_tuv
+        const int hb = la + lb, nh = (hb + 1) * (hb + 2) * (hb + 3) / 6;
+        for (int i = 0; i < nh; ++i) H0[i] = R(0);
         for (int ka = 0; ka < na; ++ka) {
             const int *A = cA[ka];
             for (int kb = 0; kb < nb; ++kb) {
-                const R Gm = Gq[ka * nb + kb];
+                R Gm;
+                if constexpr (kGamArray) {
+                    Gm = Gq[ka * nb + kb];
+                } else {
+                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
+                    Gm = wcd * nA[ka] * nB[kb] *
+                         (2.0 * Dg[mu * n + nu] * Dls -
+                          0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                }
                 const int *B = cB[kb];
+                const R *ex = Eb[0][A[0]][B[0]], *ey = Eb[1][A[1]][B[1]], *ez = Eb[2][A[2]][B[2]];
+                const int mx = A[0] + B[0], my = A[1] + B[1], mz = A[2] + B[2];
+                for (int t = 0; t <= mx; ++t) {
+                    const R gx = Gm * ex[t];
+                    for (int u = 0; u <= my; ++u) {
+                        const R gy = gx * ey[u];
+                        for (int v = 0; v <= mz; ++v) H0[md_tuv(t, u, v)] = rchem_fma(gy, ez[v], H0[md_tuv(t, u, v)]);
+                    }
+                }
+                // centres A and B along x, y, z: the derivative shifts one direction's E by one, so
+                // the sums over the two other directions are formed once and shared (S_x, S_y, S_z)
+                R P[GR_NT][GR_NT], Sx[GR_NT], Sy[GR_NT], Sz[GR_NT];
+                for (int t = 0; t <= mx + 1; ++t)
+                    for (int u = 0; u <= my + (t <= mx ? 1 : 0); ++u) {
+                        R acc = R(0);
+                        for (int v = 0; v <= mz; ++v) acc = rchem_fma(ez[v], Z0[md_tuv(t, u, v)], acc);
+                        P[t][u] = acc;
+                    }
+                for (int t = 0; t <= mx + 1; ++t) {
+                    R acc = R(0);
+                    for (int u = 0; u <= my; ++u) acc = rchem_fma(ey[u], P[t][u], acc);
+                    Sx[t] = acc;
+                }
+                for (int u = 0; u <= my + 1; ++u) {
+                    R acc = R(0);
+                    for (int t = 0; t <= mx; ++t) acc = rchem_fma(ex[t], P[t][u], acc);
+                    Sy[u] = acc;
+                }
+                for (int v = 0; v <= mz + 1; ++v) {
+                    R acc = R(0);
+                    for (int t = 0; t <= mx; ++t) {
+                        R m = R(0);
+                        for (int u = 0; u <= my; ++u) m = rchem_fma(ey[u], Z0[md_tuv(t, u, v)], m);
+                        acc = rchem_fma(ex[t], m, acc);
+                    }
+                    Sz[v] = acc;
+                }
+                const R *Sd[3] = {Sx, Sy, Sz};
                 for (int x = 0; x < 3; ++x) {
-                    // centre A: 2 alpha_a (a+1|..) - a_x (a-1|..)
-                    s[0] = A[0];
-                    s[1] = A[1];
-                    s[2] = A[2];
-                    s[x] += 1;
-                    R v = a2 * gr_dot<R>(Eb, s, B, Z0);
-                    if (A[x] > 0) {
-                        s[x] -= 2;
-                        v = v - R(A[x]) * gr_dot<R>(Eb, s, B, Z0);
+                    const R *S = Sd[x];
+                    const int ax = A[x], bx = B[x], m = ax + bx;
+                    // 2 alpha (a+1|..) - a_x (a-1|..)
+                    const R *ep = Eb[x][ax + 1][bx];
+                    R v = R(0);
+                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(ep[t], S[t], v);
+                    v = a2 * v;
+                    if (ax > 0) {
+                        const R *em = Eb[x][ax - 1][bx];
+                        R w = R(0);
+                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(em[t], S[t], w);
+                        v = v - R(ax) * w;
                     }
                     gA[x] = rchem_fma(Gm, v, gA[x]);
-                    // centre B
-                    s[0] = B[0];
-                    s[1] = B[1];
-                    s[2] = B[2];
-                    s[x] += 1;
-                    v = b2 * gr_dot<R>(Eb, A, s, Z0);
-                    if (B[x] > 0) {
-                        s[x] -= 2;
-                        v = v - R(B[x]) * gr_dot<R>(Eb, A, s, Z0);
+                    // 2 beta (..b+1|..) - b_x (..b-1|..)
+                    const R *fp = Eb[x][ax][bx + 1];
+                    v = R(0);
+                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(fp[t], S[t], v);
+                    v = b2 * v;
+                    if (bx > 0) {
+                        const R *fm = Eb[x][ax][bx - 1];
+                        R w = R(0);
+                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(fm[t], S[t], w);
+                        v = v - R(bx) * w;
                     }
                     gB[x] = rchem_fma(Gm, v, gB[x]);
-                    // centre C
-                    v = c2 * gr_dot<R>(Eb, A, B, Zp[x]);
-                    if (cC[kc][x] > 0) v = v - R(cC[kc][x]) * gr_dot<R>(Eb, A, B, Zm[x]);
-                    gC[x] = rchem_fma(Gm, v, gC[x]);
                 }
             }
+        }
+        for (int x = 0; x < 3; ++x) {
+            R vp = R(0), vm = R(0);
+            for (int i = 0; i < nh; ++i) vp = rchem_fma(H0[i], Zp[x][i], vp);
+            if (Cc[x] > 0)
+                for (int i = 0; i < nh; ++i) vm = rchem_fma(H0[i], Zm[x][i], vm);
+            gC[x] = gC[x] + c2 * vp - R(Cc[x]) * vm;
         }
     }
     for (int o = G >> 1; o > 0; o >>= 1)
