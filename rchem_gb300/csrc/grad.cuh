@@ -11,8 +11,8 @@
 // run-time angular momenta: compact code for every class up to (dd|dd)
 // (shifted to l = 3 on one centre).  The derivative integrals are never
 // stored: each contracted shell quartet is contracted with Gamma on the fly
-// and only the 9 centre derivatives leave the thread (translational
-// invariance gives the fourth centre).
+// and only the 9 centre derivatives leave the warp (translational invariance
+// gives the fourth centre).
 #pragma once
 #include <type_traits>
 
@@ -117,46 +117,6 @@ __device__ __forceinline__ double gr_cnorm(const int *p) {
     return sqrt(f2[p[0] + p[1] + p[2]] / (f2[p[0]] * f2[p[1]] * f2[p[2]]));
 }
 
-// Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
-// Hermite index with t+u+v <= bmax (stored compactly in md_tuv order): the ket of one component
-// contracted with the Coulomb integrals once, reused by every bra component.  The sum is
-// nested one direction at a time (one FMA per term instead of a product and an FMA).
-template <typename T>
-__device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
-                                        int bmax, T *Z) {
-    const T *ex = Ek[0][c[0]][d[0]], *ey = Ek[1][c[1]][d[1]], *ez = Ek[2][c[2]][d[2]];
-    const int nx = c[0] + d[0], ny = c[1] + d[1], nz = c[2] + d[2];
-    for (int t = 0; t <= bmax; ++t)
-        for (int u = 0; u <= bmax - t; ++u)
-            for (int v = 0; v <= bmax - t - u; ++v) {
-                T z = T(0);
-                for (int tt = 0; tt <= nx; ++tt) {
-                    T zy = T(0);
-                    for (int uu = 0; uu <= ny; ++uu) {
-                        T zz = T(0);
-                        for (int vv = 0; vv <= nz; ++vv) zz = rchem_fma(ez[vv], R[md_tuv(t + tt, u + uu, v + vv)], zz);
-                        zy = rchem_fma(ey[uu], zz, zy);
-                    }
-                    z = rchem_fma(ex[tt], zy, z);
-                }
-                Z[md_tuv(t, u, v)] = z;  // compact (t,u,v) order: only t+u+v <= bmax is stored
-            }
-}
-
-// sum_{tuv} E^{ab}_{tuv} Z_{tuv}
-template <typename R>
-__device__ __forceinline__ R gr_dot(const R (*Eb)[GR_NI][GR_NI][GR_NT], const int *a, const int *b, const R *Z) {
-    R s = R(0);
-    for (int t = 0; t <= a[0] + b[0]; ++t) {
-        const R ex = Eb[0][a[0]][b[0]][t];
-        for (int u = 0; u <= a[1] + b[1]; ++u) {
-            const R ey = ex * Eb[1][a[1]][b[1]][u];
-            for (int v = 0; v <= a[2] + b[2]; ++v) s = rchem_fma(ey * Eb[2][a[2]][b[2]][v], Z[md_tuv(t, u, v)], s);
-        }
-    }
-    return s;
-}
-
 // primitive pair in the kernel's arithmetic: p, 1/(2p), P, P-A, K and the
 // exponent on the pair's first shell (the derivative weight 2 alpha)
 template <typename R> struct GradPrim;
@@ -198,26 +158,65 @@ __device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x;
 __device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
 __device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
 
-#define GR_ZN 56  // (t,u,v) with t+u+v <= la+lb+1 <= 5
+// ---------------------------------------------------------------------------
+// The classes with a d shell (run-time angular momenta): one contracted quartet
+// per warp.
+// Per primitive quartet the warp builds the Hermite tables (E of bra and ket,
+// the Coulomb table R) once in shared memory; per chunk of ket component
+// pairs it builds the ket vectors Z0 = sum E^{cd} R (for the centre-A/B
+// derivatives) and W_x = 2 gamma Z(c+1_x) - c_x Z(c-1_x) (centre C) in shared
+// memory; then every lane takes (ket pair, bra pair) items: Gamma in place,
+// the A/B derivatives through the x/y/z partial sums of E^{ab} against Z0, the
+// C derivative as E^{ab} . W_x.  Per-lane state is a few scalars, so nothing
+// spills; the tables are formed once per warp instead of once per lane.
+#define GW_WARPS 2      // warps per block
+#define GW_CHUNK 12     // ket component pairs whose vectors are held at once
+#define GW_ZSLOT 161    // Z0 (t+u+v <= 5: 56) + three W_x (t+u+v <= 4: 35 each)
+#define GW_ETAB (3 * GR_NI * GR_NI * GR_NT)
+#define GW_PER_WARP (2 * GW_ETAB + 2 * GR_NR + GW_CHUNK * GW_ZSLOT)
 
-#define GR_MAXC4 1296  // components of a (dd|dd) quartet
-
-// One warp task: up to 32 >> lg unique shell quartets, G = 2^lg lanes each
-// (the segment/task layout of the Fock build).  Run-time angular momenta (the
-// classes with a d shell).  The G lanes split (primitive quartet, ket component
-// pair) units; Gamma (degeneracy and component norms folded in) is formed once
-// per quartet in FP64 and rounded to R; the 9 centre derivatives are reduced
-// over the G lanes with warp shuffles and added to the gradient by one lane.
+__device__ __forceinline__ int gr_cnt(int N) { return (N + 1) * (N + 2) * (N + 3) / 6; }
+// (t,u,v) of compact Hermite index i (the inverse of md_tuv)
+__device__ __forceinline__ void gr_decode(int i, int &t, int &u, int &v) {
+    int n = 0;
+    while (gr_cnt(n) <= i) ++n;
+    const int r = i - (n >= 1 ? gr_cnt(n - 1) : 0);
+    int s = 0;
+    while ((s + 1) * (s + 2) / 2 <= r) ++s;
+    v = r - s * (s + 1) / 2;
+    u = s - v;
+    t = n - s;
+}
+// sum_{t'u'v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} (ket signs folded into E)
 template <typename R>
-__global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
-    const int lane = threadIdx.x & 31;
-    const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    if (w >= g.ntasks) return;  // warp-uniform
+__device__ __forceinline__ R gr_zsum(const R (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const R *Rt,
+                                     int t, int u, int v) {
+    const R *ex = Ek[0][c[0]][d[0]], *ey = Ek[1][c[1]][d[1]], *ez = Ek[2][c[2]][d[2]];
+    R z = R(0);
+    for (int tt = 0; tt <= c[0] + d[0]; ++tt) {
+        R zy = R(0);
+        for (int uu = 0; uu <= c[1] + d[1]; ++uu) {
+            R zz = R(0);
+            for (int vv = 0; vv <= c[2] + d[2]; ++vv) zz = rchem_fma(ez[vv], Rt[md_tuv(t + tt, u + uu, v + vv)], zz);
+            zy = rchem_fma(ey[uu], zz, zy);
+        }
+        z = rchem_fma(ex[tt], zy, z);
+    }
+    return z;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32 * GW_WARPS) k_grad2e_wc(GradArgs g) {
+    extern __shared__ __align__(16) unsigned char gw_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    R *base = reinterpret_cast<R *>(gw_smem) + (size_t)wib * GW_PER_WARP;
+    R(*Eb)[GR_NI][GR_NI][GR_NT] = reinterpret_cast<R(*)[GR_NI][GR_NI][GR_NT]>(base);
+    R(*Ek)[GR_NI][GR_NI][GR_NT] = reinterpret_cast<R(*)[GR_NI][GR_NI][GR_NT]>(base + GW_ETAB);
+    R *Ra = base + 2 * GW_ETAB, *Rb = Ra + GR_NR, *Zc = Rb + GR_NR;
+    const int w = blockIdx.x * GW_WARPS + wib;
+    if (w >= g.ntasks) return;  // warp-uniform; the kernel has no block-wide barrier
     const EriTask tk = g.tasks[w];
-    const int lgG = (tk.nq_lg >> 8) & 7, nqt = tk.nq_lg & 255;
-    const int G = 1 << lgG, r = lane & (G - 1), qi = lane >> lgG;
-    const bool active = qi < nqt;
-    int sg = tk.seg, off = tk.off + (active ? qi : 0);
+    int sg = tk.seg, off = tk.off;
     EriSeg seg = g.segs[sg];
     while (off >= seg.count) {
         off -= seg.count;
@@ -228,205 +227,186 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     const int la = g.shell_l[bp.A], lb = g.shell_l[bp.B], lc = g.shell_l[kp.A], ld = g.shell_l[kp.B];
     const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2, nc = (lc + 1) * (lc + 2) / 2,
               nd = (ld + 1) * (ld + 2) / 2;
-    const int n = bp.mn;  // the quartet's geometry block of the packed D
+    const int n = bp.mn;
     const double *Dg = g.D + bp.moff;
     double deg = 8.0;
     if (bp.diag) deg *= 0.5;
     if (kp.diag) deg *= 0.5;
     if (same) deg *= 0.5;
-    // Cartesian components and Gamma, once per quartet
-    int cA[6][3], cB[6][3], cC[6][3], cD[6][3];
-    double nA[6], nB[6], nC[6], nD[6];
-    for (int k = 0; k < na; ++k) {
-        gr_comp(la, k, cA[k]);
-        nA[k] = gr_cnorm(cA[k]);
-    }
-    for (int k = 0; k < nb; ++k) {
-        gr_comp(lb, k, cB[k]);
-        nB[k] = gr_cnorm(cB[k]);
-    }
-    for (int k = 0; k < nc; ++k) {
-        gr_comp(lc, k, cC[k]);
-        nC[k] = gr_cnorm(cC[k]);
-    }
-    for (int k = 0; k < nd; ++k) {
-        gr_comp(ld, k, cD[k]);
-        nD[k] = gr_cnorm(cD[k]);
-    }
-    // FP64: Gamma is formed where it is used (five density loads and a few FMAs
-    // per bra pair, against a 10 KB local array per thread); the narrower
-    // forms keep the array, formed once in FP64 and rounded.
-    constexpr bool kGamArray = !std::is_same<R, double>::value;
-    R Gam[kGamArray ? GR_MAXC4 : 1];
-    if constexpr (kGamArray)
-    for (int kc = 0; kc < nc; ++kc)
-        for (int kd = 0; kd < nd; ++kd) {
-            const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
-            for (int ka = 0; ka < na; ++ka)
-                for (int kb = 0; kb < nb; ++kb) {
-                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    Gam[((kc * nd + kd) * na + ka) * nb + kb] = gt_narrow(
-                        deg * nA[ka] * nB[kb] * nC[kc] * nD[kd] *
-                            (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
-                             0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
-                        (R *)nullptr);
-                }
-        }
     R AB[3], CD[3];
     Tabs<R>::ab(bp, AB);
     Tabs<R>::ab(kp, CD);
     const R *btab = GradPrim<R>::boys(g);
-    R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int L1 = la + lb + lc + ld + 1;
-    R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
-    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN], H0[GR_ZN];
-    // work units: (primitive quartet, ket component pair); the G lanes split them
-    // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
-    const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
-    const int nunits = active ? ntot * ncd : 0;  // idle lanes only join the reduction
-    int cur = -1;
-    R a2 = R(0), b2 = R(0), c2 = R(0);
-    for (int u = r; u < nunits; u += G) {
-        const int tq = u / ncd, kcd = u - tq * ncd;
-        if (tq != cur) {  // primitive-quartet tables, kept while the lane stays on it
-            cur = tq;
-            const int ia = tq / nk, ic = tq - ia * nk;
-            R p, ohp, Pc[3], PA[3], Kab, aa, q, ohq, Qc[3], QC[3], Kcd, ac;
-            GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
-            GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
-            a2 = aa + aa;
-            b2 = (p - aa) + (p - aa);
-            c2 = ac + ac;
-            const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
-            const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
-            const R T = rho * (X * X + Y * Y + Zc * Zc);
-            boys_eval_rt<R>(L1, T, Kab * Kcd * rs, btab, F);
-            gr_R<R>(L1, rho, X, Y, Zc, F, Rt);
-            for (int dd = 0; dd < 3; ++dd) {
-                gr_herm<R>(la + 1, lb + 1, PA[dd], AB[dd], ohp, Eb[dd]);
-                gr_herm<R>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
-                for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
-                    for (int j = 0; j <= ld; ++j)
-                        for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
-            }
+    const int nab = na * nb, ncd = nc * nd;
+    const int nz0 = gr_cnt(la + lb + 1), nzb = gr_cnt(la + lb), zs = nz0 + 3 * nzb;
+    R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
+    const int nk = kp.npp, ntot = bp.npp * nk;
+    for (int tq = 0; tq < ntot; ++tq) {
+        const int ia = tq / nk, ic = tq - ia * nk;
+        R p, ohp, Pc[3], PA[3], Kab, aa, q, ohq, Qc[3], QC[3], Kcd, ac;
+        GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
+        GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
+        const R a2 = aa + aa, b2 = (p - aa) + (p - aa), c2 = ac + ac;
+        const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+        const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zq = Pc[2] - Qc[2];
+        R F[GR_LMAX + 1];
+        boys_eval_rt<R>(L1, rho * (X * X + Y * Y + Zq * Zq), Kab * Kcd * rs, btab, F);
+        __syncwarp();  // the previous primitive quartet's tables have been read
+        // Hermite E tables: lanes 0-2 the bra directions, 3-5 the ket (ket signs folded in)
+        if (lane < 3) {
+            gr_herm<R>(la + 1, lb + 1, PA[lane], AB[lane], ohp, Eb[lane]);
+        } else if (lane < 6) {
+            const int dd = lane - 3;
+            gr_herm<R>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
+            for (int i = 0; i <= lc + 1; ++i)
+                for (int j = 0; j <= ld; ++j)
+                    for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
         }
-        const int kc = kcd / nd, kd = kcd - kc * nd;
-        const R *Gq = Gam + (kGamArray ? (kc * nd + kd) * na * nb : 0);
-        const int *Cc = cC[kc];
-        const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
-        const double Dls = Dg[l_ * n + s_], wcd = deg * nC[kc] * nD[kd];
-        // ket contracted with R: unshifted (the bra may be shifted by one) and C-shifted
-        gr_zvec<R>(Ek, Cc, cD[kd], Rt, la + lb + 1, Z0);
-        for (int x = 0; x < 3; ++x) {
-            int s[3] = {Cc[0], Cc[1], Cc[2]};
-            s[x] += 1;
-            gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
-            if (Cc[x] > 0) {
-                s[x] -= 2;
-                gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
-            }
+        // Coulomb table R_tuv (t+u+v <= L1), level by level of the recursion, the
+        // entries of a level over the lanes
+        const R m2a = R(-2) * rho;
+        R *cur = Ra, *nxt = Rb;
+        if (lane == 0) {
+            R pw = R(1);
+            for (int k = 0; k < L1; ++k) pw = pw * m2a;
+            cur[0] = pw * F[L1];
         }
-        // centre C through the bra Hermite density H0_tuv = sum_ab Gamma_ab E^{ab}_tuv
-        const int hb = la + lb, nh = (hb + 1) * (hb + 2) * (hb + 3) / 6;
-        for (int i = 0; i < nh; ++i) H0[i] = R(0);
-        for (int ka = 0; ka < na; ++ka) {
-            const int *A = cA[ka];
-            for (int kb = 0; kb < nb; ++kb) {
-                R Gm;
-                if constexpr (kGamArray) {
-                    Gm = Gq[ka * nb + kb];
+        __syncwarp();
+        for (int lv = L1 - 1; lv >= 0; --lv) {
+            R pw = R(1);
+            for (int k = 0; k < lv; ++k) pw = pw * m2a;
+            const int cnt = gr_cnt(L1 - lv);
+            for (int i = lane; i < cnt; i += 32) {
+                int t, u, v;
+                gr_decode(i, t, u, v);
+                R r;
+                if (t + u + v == 0) r = pw * F[lv];
+                else if (t > 0) r = rchem_fma(X, cur[md_tuv(t - 1, u, v)], t > 1 ? R(t - 1) * cur[md_tuv(t - 2, u, v)] : R(0));
+                else if (u > 0) r = rchem_fma(Y, cur[md_tuv(0, u - 1, v)], u > 1 ? R(u - 1) * cur[md_tuv(0, u - 2, v)] : R(0));
+                else r = rchem_fma(Zq, cur[md_tuv(0, 0, v - 1)], v > 1 ? R(v - 1) * cur[md_tuv(0, 0, v - 2)] : R(0));
+                nxt[i] = r;
+            }
+            __syncwarp();
+            R *tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+        }
+        const R *Rt = cur;
+        for (int c0 = 0; c0 < ncd; c0 += GW_CHUNK) {
+            const int nch = min(GW_CHUNK, ncd - c0);
+            // ket vectors of the chunk: slot k holds Z0 (nz0 values) then W_x (nzb each)
+            for (int e = lane; e < nch * zs; e += 32) {
+                const int k = e / zs, j = e - k * zs;
+                const int kcd = c0 + k, kc = kcd / nd, kd = kcd - kc * nd;
+                int cc[3], dd[3];
+                gr_comp(lc, kc, cc);
+                gr_comp(ld, kd, dd);
+                int t, u, v;
+                R val;
+                if (j < nz0) {
+                    gr_decode(j, t, u, v);
+                    val = gr_zsum<R>(Ek, cc, dd, Rt, t, u, v);
                 } else {
-                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
-                    Gm = wcd * nA[ka] * nB[kb] *
-                         (2.0 * Dg[mu * n + nu] * Dls -
-                          0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                    const int jj = j - nz0, x = jj / nzb;
+                    gr_decode(jj - x * nzb, t, u, v);
+                    int s[3] = {cc[0], cc[1], cc[2]};
+                    s[x] += 1;
+                    val = c2 * gr_zsum<R>(Ek, s, dd, Rt, t, u, v);
+                    if (cc[x] > 0) {
+                        s[x] -= 2;
+                        val = val - R(cc[x]) * gr_zsum<R>(Ek, s, dd, Rt, t, u, v);
+                    }
                 }
-                const int *B = cB[kb];
+                Zc[e] = val;
+            }
+            __syncwarp();
+            for (int it = lane; it < nch * nab; it += 32) {
+                const int k = it / nab, ab = it - k * nab;
+                const int kcd = c0 + k, kc = kcd / nd, kd = kcd - kc * nd;
+                const int ka = ab / nb, kb = ab - ka * nb;
+                int A[3], B[3], Cc[3], Dd[3];
+                gr_comp(la, ka, A);
+                gr_comp(lb, kb, B);
+                gr_comp(lc, kc, Cc);
+                gr_comp(ld, kd, Dd);
+                // Gamma (degeneracy and component norms folded in), in FP64
+                const int mu = bp.aoA + ka, nu = bp.aoB + kb, l_ = kp.aoA + kc, s_ = kp.aoB + kd;
+                const double gam = deg * gr_cnorm(A) * gr_cnorm(B) * gr_cnorm(Cc) * gr_cnorm(Dd) *
+                                   (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
+                                    0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                const R Gm = gt_narrow(gam, (R *)nullptr);
+                const R *Z0 = Zc + k * zs, *W = Z0 + nz0;
                 const R *ex = Eb[0][A[0]][B[0]], *ey = Eb[1][A[1]][B[1]], *ez = Eb[2][A[2]][B[2]];
                 const int mx = A[0] + B[0], my = A[1] + B[1], mz = A[2] + B[2];
-                for (int t = 0; t <= mx; ++t) {
-                    const R gx = Gm * ex[t];
-                    for (int u = 0; u <= my; ++u) {
-                        const R gy = gx * ey[u];
-                        for (int v = 0; v <= mz; ++v) H0[md_tuv(t, u, v)] = rchem_fma(gy, ez[v], H0[md_tuv(t, u, v)]);
-                    }
-                }
-                // centres A and B along x, y, z: the derivative shifts one direction's E by one, so
-                // the sums over the two other directions are formed once and shared (S_x, S_y, S_z)
-                R P[GR_NT][GR_NT], Sx[GR_NT], Sy[GR_NT], Sz[GR_NT];
-                for (int t = 0; t <= mx + 1; ++t)
-                    for (int u = 0; u <= my + (t <= mx ? 1 : 0); ++u) {
-                        R acc = R(0);
-                        for (int v = 0; v <= mz; ++v) acc = rchem_fma(ez[v], Z0[md_tuv(t, u, v)], acc);
-                        P[t][u] = acc;
-                    }
-                for (int t = 0; t <= mx + 1; ++t) {
-                    R acc = R(0);
-                    for (int u = 0; u <= my; ++u) acc = rchem_fma(ey[u], P[t][u], acc);
-                    Sx[t] = acc;
-                }
-                for (int u = 0; u <= my + 1; ++u) {
-                    R acc = R(0);
-                    for (int t = 0; t <= mx; ++t) acc = rchem_fma(ex[t], P[t][u], acc);
-                    Sy[u] = acc;
-                }
-                for (int v = 0; v <= mz + 1; ++v) {
-                    R acc = R(0);
-                    for (int t = 0; t <= mx; ++t) {
-                        R m = R(0);
-                        for (int u = 0; u <= my; ++u) m = rchem_fma(ey[u], Z0[md_tuv(t, u, v)], m);
-                        acc = rchem_fma(ex[t], m, acc);
-                    }
-                    Sz[v] = acc;
-                }
-                const R *Sd[3] = {Sx, Sy, Sz};
+                // centres A and B: for each direction the sum over the two others is
+                // formed for every index of this one and dotted with four E vectors
                 for (int x = 0; x < 3; ++x) {
-                    const R *S = Sd[x];
                     const int ax = A[x], bx = B[x], m = ax + bx;
-                    // 2 alpha (a+1|..) - a_x (a-1|..)
-                    const R *ep = Eb[x][ax + 1][bx];
-                    R v = R(0);
-                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(ep[t], S[t], v);
-                    v = a2 * v;
-                    if (ax > 0) {
-                        const R *em = Eb[x][ax - 1][bx];
-                        R w = R(0);
-                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(em[t], S[t], w);
-                        v = v - R(ax) * w;
+                    const R *ep = Eb[x][ax + 1][bx], *fp = Eb[x][ax][bx + 1];
+                    const R *em = ax > 0 ? Eb[x][ax - 1][bx] : ep, *fm = bx > 0 ? Eb[x][ax][bx - 1] : fp;
+                    R dap = R(0), dam = R(0), dbp = R(0), dbm = R(0);
+                    for (int i = 0; i <= m + 1; ++i) {
+                        R si = R(0);
+                        if (x == 0) {
+                            for (int u = 0; u <= my; ++u) {
+                                R sv = R(0);
+                                for (int v = 0; v <= mz; ++v) sv = rchem_fma(ez[v], Z0[md_tuv(i, u, v)], sv);
+                                si = rchem_fma(ey[u], sv, si);
+                            }
+                        } else if (x == 1) {
+                            for (int t = 0; t <= mx; ++t) {
+                                R sv = R(0);
+                                for (int v = 0; v <= mz; ++v) sv = rchem_fma(ez[v], Z0[md_tuv(t, i, v)], sv);
+                                si = rchem_fma(ex[t], sv, si);
+                            }
+                        } else {
+                            for (int t = 0; t <= mx; ++t) {
+                                R su = R(0);
+                                for (int u = 0; u <= my; ++u) su = rchem_fma(ey[u], Z0[md_tuv(t, u, i)], su);
+                                si = rchem_fma(ex[t], su, si);
+                            }
+                        }
+                        dap = rchem_fma(ep[i], si, dap);
+                        dbp = rchem_fma(fp[i], si, dbp);
+                        if (i < m) {
+                            dam = rchem_fma(em[i], si, dam);
+                            dbm = rchem_fma(fm[i], si, dbm);
+                        }
                     }
-                    gA[x] = rchem_fma(Gm, v, gA[x]);
-                    // 2 beta (..b+1|..) - b_x (..b-1|..)
-                    const R *fp = Eb[x][ax][bx + 1];
-                    v = R(0);
-                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(fp[t], S[t], v);
-                    v = b2 * v;
-                    if (bx > 0) {
-                        const R *fm = Eb[x][ax][bx - 1];
-                        R w = R(0);
-                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(fm[t], S[t], w);
-                        v = v - R(bx) * w;
+                    R va = a2 * dap, vb = b2 * dbp;
+                    if (ax > 0) va = va - R(ax) * dam;
+                    if (bx > 0) vb = vb - R(bx) * dbm;
+                    gA[x] = rchem_fma(Gm, va, gA[x]);
+                    gB[x] = rchem_fma(Gm, vb, gB[x]);
+                }
+                // centre C: E^{ab} . W_x
+                for (int x = 0; x < 3; ++x) {
+                    const R *Wx = W + x * nzb;
+                    R sc = R(0);
+                    for (int t = 0; t <= mx; ++t) {
+                        R su = R(0);
+                        for (int u = 0; u <= my; ++u) {
+                            R sv = R(0);
+                            for (int v = 0; v <= mz; ++v) sv = rchem_fma(ez[v], Wx[md_tuv(t, u, v)], sv);
+                            su = rchem_fma(ey[u], sv, su);
+                        }
+                        sc = rchem_fma(ex[t], su, sc);
                     }
-                    gB[x] = rchem_fma(Gm, v, gB[x]);
+                    gC[x] = rchem_fma(Gm, sc, gC[x]);
                 }
             }
-        }
-        for (int x = 0; x < 3; ++x) {
-            R vp = R(0), vm = R(0);
-            for (int i = 0; i < nh; ++i) vp = rchem_fma(H0[i], Zp[x][i], vp);
-            if (Cc[x] > 0)
-                for (int i = 0; i < nh; ++i) vm = rchem_fma(H0[i], Zm[x][i], vm);
-            gC[x] = gC[x] + c2 * vp - R(Cc[x]) * vm;
+            __syncwarp();  // the chunk's vectors have been read
         }
     }
-    for (int o = G >> 1; o > 0; o >>= 1)
+    for (int o = 16; o > 0; o >>= 1)
         for (int x = 0; x < 3; ++x) {
             gA[x] += __shfl_xor_sync(0xffffffffu, gA[x], o);
             gB[x] += __shfl_xor_sync(0xffffffffu, gB[x], o);
             gC[x] += __shfl_xor_sync(0xffffffffu, gC[x], o);
         }
-    if (!active || r != 0) return;
-    const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A],
-              atD = g.shell_atom[kp.B];
+    if (lane != 0) return;
+    const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A], atD = g.shell_atom[kp.B];
     for (int x = 0; x < 3; ++x) {
         const double a = widen(gA[x]), b = widen(gB[x]), c = widen(gC[x]);
         atomicAdd(g.grad + 3 * atA + x, a);

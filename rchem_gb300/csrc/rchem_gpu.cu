@@ -181,7 +181,7 @@ static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
 bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
-void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_wc_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
@@ -1387,6 +1387,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             const long long units = sp ? nprimq : nprimq * ncart(gk.la) * ncart(gk.lb);
             int lg = 0;
             while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
+            if (!sp) lg = 5;  // the d-class kernel: one quartet per warp
             const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
             for (int prec = 0; prec < 2; ++prec) {
                 const int s0 = (int)segs.size();
@@ -1493,8 +1494,8 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             cudaStream_t st = b->aux[best];
             g.tasks = b->d_gtasks + b->gtask_off[k];
             g.ntasks = (int)b->gtask_cnt[k];
-            const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
             if (k < 2 * RCHEM_NCLASS) {  // an s/p class: its specialised kernel
+                const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
                 const int cls = k / 2;
                 const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
                                         : (((o.emulated & RCHEM_JK_EMULATED) && rchem_grad_sp_df64(cls, g, blocks, st)) ||
@@ -1503,11 +1504,18 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
                 CK(cudaGetLastError());
                 continue;
             }
-            // classes with d shells: run-time angular momenta, FP32 below tau32 and FP64
-            // above, also in the emulated form (this kernel is bound by its local-memory
-            // tables, not the FP64 pipe: double-float measured slower)
-            if (k & 1) rchem_grad_rt_f32(g, blocks, st);
-            else k_grad2e_rt<double><<<blocks, 64, 0, st>>>(g);
+            // classes with d shells: the warp-cooperative kernel (run-time angular momenta,
+            // one quartet per warp), FP32 below tau32 and FP64 above (also in the
+            // emulated form, which keeps these classes in FP64)
+            const unsigned blocks = (unsigned)((b->gtask_cnt[k] + GW_WARPS - 1) / GW_WARPS);
+            if (k & 1) {
+                if (!rchem_grad_wc_f32(g, blocks, st))
+                    return set_err(RCHEM_ERR_CUDA, "shared memory for the d-class gradient kernel");
+            } else {
+                const size_t smem = (size_t)GW_WARPS * GW_PER_WARP * sizeof(double);
+                CK(cudaFuncSetAttribute(k_grad2e_wc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                k_grad2e_wc<double><<<blocks, 32 * GW_WARPS, smem, st>>>(g);
+            }
             CK(cudaGetLastError());
         }
         for (int i = 0; i < nuse; ++i) {
