@@ -158,9 +158,273 @@ __device__ __forceinline__ float gt_narrow(double x, float *) { return (float)x;
 __device__ __forceinline__ double gt_narrow(double x, double *) { return x; }
 __device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
 
+// Z_{tuv} = sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'} R_{t+t',u+u',v+v'} for every bra
+// Hermite index with t+u+v <= bmax (stored compactly in md_tuv order): the ket of one component
+// contracted with the Coulomb integrals once, reused by every bra component.  The sum is
+// nested one direction at a time (one FMA per term instead of a product and an FMA).
+template <typename T>
+__device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
+                                        int bmax, T *Z) {
+    const T *ex = Ek[0][c[0]][d[0]], *ey = Ek[1][c[1]][d[1]], *ez = Ek[2][c[2]][d[2]];
+    const int nx = c[0] + d[0], ny = c[1] + d[1], nz = c[2] + d[2];
+    for (int t = 0; t <= bmax; ++t)
+        for (int u = 0; u <= bmax - t; ++u)
+            for (int v = 0; v <= bmax - t - u; ++v) {
+                T z = T(0);
+                for (int tt = 0; tt <= nx; ++tt) {
+                    T zy = T(0);
+                    for (int uu = 0; uu <= ny; ++uu) {
+                        T zz = T(0);
+                        for (int vv = 0; vv <= nz; ++vv) zz = rchem_fma(ez[vv], R[md_tuv(t + tt, u + uu, v + vv)], zz);
+                        zy = rchem_fma(ey[uu], zz, zy);
+                    }
+                    z = rchem_fma(ex[tt], zy, z);
+                }
+                Z[md_tuv(t, u, v)] = z;  // compact (t,u,v) order: only t+u+v <= bmax is stored
+            }
+}
+
+#define GR_ZN 56  // (t,u,v) with t+u+v <= la+lb+1 <= 5
+
+#define GR_MAXC4 1296  // components of a (dd|dd) quartet
+
+// The smaller classes with a d shell (run-time angular momenta; the larger
+// ones run k_grad2e_wc below).  One warp task: up to 32 >> lg unique shell
+// quartets, G = 2^lg lanes each (the segment/task layout of the Fock build).  The G lanes split (primitive quartet, ket component
+// pair) units; Gamma (degeneracy and component norms folded in) is formed once
+// per quartet in FP64 and rounded to R; the 9 centre derivatives are reduced
+// over the G lanes with warp shuffles and added to the gradient by one lane.
+template <typename R>
+__global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
+    const int lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (w >= g.ntasks) return;  // warp-uniform
+    const EriTask tk = g.tasks[w];
+    const int lgG = (tk.nq_lg >> 8) & 7, nqt = tk.nq_lg & 255;
+    const int G = 1 << lgG, r = lane & (G - 1), qi = lane >> lgG;
+    const bool active = qi < nqt;
+    int sg = tk.seg, off = tk.off + (active ? qi : 0);
+    EriSeg seg = g.segs[sg];
+    while (off >= seg.count) {
+        off -= seg.count;
+        seg = g.segs[++sg];
+    }
+    const ShellPair bp = g.pairs[seg.bra], kp = g.pairs[seg.ket0 + off];
+    const bool same = seg.bra == seg.ket0 + off;
+    const int la = g.shell_l[bp.A], lb = g.shell_l[bp.B], lc = g.shell_l[kp.A], ld = g.shell_l[kp.B];
+    const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2, nc = (lc + 1) * (lc + 2) / 2,
+              nd = (ld + 1) * (ld + 2) / 2;
+    const int n = bp.mn;  // the quartet's geometry block of the packed D
+    const double *Dg = g.D + bp.moff;
+    double deg = 8.0;
+    if (bp.diag) deg *= 0.5;
+    if (kp.diag) deg *= 0.5;
+    if (same) deg *= 0.5;
+    // Cartesian components and Gamma, once per quartet
+    int cA[6][3], cB[6][3], cC[6][3], cD[6][3];
+    double nA[6], nB[6], nC[6], nD[6];
+    for (int k = 0; k < na; ++k) {
+        gr_comp(la, k, cA[k]);
+        nA[k] = gr_cnorm(cA[k]);
+    }
+    for (int k = 0; k < nb; ++k) {
+        gr_comp(lb, k, cB[k]);
+        nB[k] = gr_cnorm(cB[k]);
+    }
+    for (int k = 0; k < nc; ++k) {
+        gr_comp(lc, k, cC[k]);
+        nC[k] = gr_cnorm(cC[k]);
+    }
+    for (int k = 0; k < nd; ++k) {
+        gr_comp(ld, k, cD[k]);
+        nD[k] = gr_cnorm(cD[k]);
+    }
+    // FP64: Gamma is formed where it is used (five density loads and a few FMAs
+    // per bra pair, against a 10 KB local array per thread); the narrower
+    // forms keep the array, formed once in FP64 and rounded.
+    constexpr bool kGamArray = !std::is_same<R, double>::value;
+    R Gam[kGamArray ? GR_MAXC4 : 1];
+    if constexpr (kGamArray)
+    for (int kc = 0; kc < nc; ++kc)
+        for (int kd = 0; kd < nd; ++kd) {
+            const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
+            for (int ka = 0; ka < na; ++ka)
+                for (int kb = 0; kb < nb; ++kb) {
+                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
+                    Gam[((kc * nd + kd) * na + ka) * nb + kb] = gt_narrow(
+                        deg * nA[ka] * nB[kb] * nC[kc] * nD[kd] *
+                            (2.0 * Dg[mu * n + nu] * Dg[l_ * n + s_] -
+                             0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
+                        (R *)nullptr);
+                }
+        }
+    R AB[3], CD[3];
+    Tabs<R>::ab(bp, AB);
+    Tabs<R>::ab(kp, CD);
+    const R *btab = GradPrim<R>::boys(g);
+    R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
+    const int L1 = la + lb + lc + ld + 1;
+    R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
+    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN], H0[GR_ZN];
+    // work units: (primitive quartet, ket component pair); the G lanes split them
+    // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
+    const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
+    const int nunits = active ? ntot * ncd : 0;  // idle lanes only join the reduction
+    int cur = -1;
+    R a2 = R(0), b2 = R(0), c2 = R(0);
+    for (int u = r; u < nunits; u += G) {
+        const int tq = u / ncd, kcd = u - tq * ncd;
+        if (tq != cur) {  // primitive-quartet tables, kept while the lane stays on it
+            cur = tq;
+            const int ia = tq / nk, ic = tq - ia * nk;
+            R p, ohp, Pc[3], PA[3], Kab, aa, q, ohq, Qc[3], QC[3], Kcd, ac;
+            GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
+            GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
+            a2 = aa + aa;
+            b2 = (p - aa) + (p - aa);
+            c2 = ac + ac;
+            const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+            const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
+            const R T = rho * (X * X + Y * Y + Zc * Zc);
+            boys_eval_rt<R>(L1, T, Kab * Kcd * rs, btab, F);
+            gr_R<R>(L1, rho, X, Y, Zc, F, Rt);
+            for (int dd = 0; dd < 3; ++dd) {
+                gr_herm<R>(la + 1, lb + 1, PA[dd], AB[dd], ohp, Eb[dd]);
+                gr_herm<R>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
+                for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
+                    for (int j = 0; j <= ld; ++j)
+                        for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
+            }
+        }
+        const int kc = kcd / nd, kd = kcd - kc * nd;
+        const R *Gq = Gam + (kGamArray ? (kc * nd + kd) * na * nb : 0);
+        const int *Cc = cC[kc];
+        const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
+        const double Dls = Dg[l_ * n + s_], wcd = deg * nC[kc] * nD[kd];
+        // ket contracted with R: unshifted (the bra may be shifted by one) and C-shifted
+        gr_zvec<R>(Ek, Cc, cD[kd], Rt, la + lb + 1, Z0);
+        for (int x = 0; x < 3; ++x) {
+            int s[3] = {Cc[0], Cc[1], Cc[2]};
+            s[x] += 1;
+            gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
+            if (Cc[x] > 0) {
+                s[x] -= 2;
+                gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
+            }
+        }
+        // centre C through the bra Hermite density H0_tuv = sum_ab Gamma_ab E^{ab}_tuv
+        const int hb = la + lb, nh = (hb + 1) * (hb + 2) * (hb + 3) / 6;
+        for (int i = 0; i < nh; ++i) H0[i] = R(0);
+        for (int ka = 0; ka < na; ++ka) {
+            const int *A = cA[ka];
+            for (int kb = 0; kb < nb; ++kb) {
+                R Gm;
+                if constexpr (kGamArray) {
+                    Gm = Gq[ka * nb + kb];
+                } else {
+                    const int mu = bp.aoA + ka, nu = bp.aoB + kb;
+                    Gm = wcd * nA[ka] * nB[kb] *
+                         (2.0 * Dg[mu * n + nu] * Dls -
+                          0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_]));
+                }
+                const int *B = cB[kb];
+                const R *ex = Eb[0][A[0]][B[0]], *ey = Eb[1][A[1]][B[1]], *ez = Eb[2][A[2]][B[2]];
+                const int mx = A[0] + B[0], my = A[1] + B[1], mz = A[2] + B[2];
+                for (int t = 0; t <= mx; ++t) {
+                    const R gx = Gm * ex[t];
+                    for (int u = 0; u <= my; ++u) {
+                        const R gy = gx * ey[u];
+                        for (int v = 0; v <= mz; ++v) H0[md_tuv(t, u, v)] = rchem_fma(gy, ez[v], H0[md_tuv(t, u, v)]);
+                    }
+                }
+                // centres A and B along x, y, z: the derivative shifts one direction's E by one, so
+                // the sums over the two other directions are formed once and shared (S_x, S_y, S_z)
+                R P[GR_NT][GR_NT], Sx[GR_NT], Sy[GR_NT], Sz[GR_NT];
+                for (int t = 0; t <= mx + 1; ++t)
+                    for (int u = 0; u <= my + (t <= mx ? 1 : 0); ++u) {
+                        R acc = R(0);
+                        for (int v = 0; v <= mz; ++v) acc = rchem_fma(ez[v], Z0[md_tuv(t, u, v)], acc);
+                        P[t][u] = acc;
+                    }
+                for (int t = 0; t <= mx + 1; ++t) {
+                    R acc = R(0);
+                    for (int u = 0; u <= my; ++u) acc = rchem_fma(ey[u], P[t][u], acc);
+                    Sx[t] = acc;
+                }
+                for (int u = 0; u <= my + 1; ++u) {
+                    R acc = R(0);
+                    for (int t = 0; t <= mx; ++t) acc = rchem_fma(ex[t], P[t][u], acc);
+                    Sy[u] = acc;
+                }
+                for (int v = 0; v <= mz + 1; ++v) {
+                    R acc = R(0);
+                    for (int t = 0; t <= mx; ++t) {
+                        R m = R(0);
+                        for (int u = 0; u <= my; ++u) m = rchem_fma(ey[u], Z0[md_tuv(t, u, v)], m);
+                        acc = rchem_fma(ex[t], m, acc);
+                    }
+                    Sz[v] = acc;
+                }
+                const R *Sd[3] = {Sx, Sy, Sz};
+                for (int x = 0; x < 3; ++x) {
+                    const R *S = Sd[x];
+                    const int ax = A[x], bx = B[x], m = ax + bx;
+                    // 2 alpha (a+1|..) - a_x (a-1|..)
+                    const R *ep = Eb[x][ax + 1][bx];
+                    R v = R(0);
+                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(ep[t], S[t], v);
+                    v = a2 * v;
+                    if (ax > 0) {
+                        const R *em = Eb[x][ax - 1][bx];
+                        R w = R(0);
+                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(em[t], S[t], w);
+                        v = v - R(ax) * w;
+                    }
+                    gA[x] = rchem_fma(Gm, v, gA[x]);
+                    // 2 beta (..b+1|..) - b_x (..b-1|..)
+                    const R *fp = Eb[x][ax][bx + 1];
+                    v = R(0);
+                    for (int t = 0; t <= m + 1; ++t) v = rchem_fma(fp[t], S[t], v);
+                    v = b2 * v;
+                    if (bx > 0) {
+                        const R *fm = Eb[x][ax][bx - 1];
+                        R w = R(0);
+                        for (int t = 0; t <= m - 1; ++t) w = rchem_fma(fm[t], S[t], w);
+                        v = v - R(bx) * w;
+                    }
+                    gB[x] = rchem_fma(Gm, v, gB[x]);
+                }
+            }
+        }
+        for (int x = 0; x < 3; ++x) {
+            R vp = R(0), vm = R(0);
+            for (int i = 0; i < nh; ++i) vp = rchem_fma(H0[i], Zp[x][i], vp);
+            if (Cc[x] > 0)
+                for (int i = 0; i < nh; ++i) vm = rchem_fma(H0[i], Zm[x][i], vm);
+            gC[x] = gC[x] + c2 * vp - R(Cc[x]) * vm;
+        }
+    }
+    for (int o = G >> 1; o > 0; o >>= 1)
+        for (int x = 0; x < 3; ++x) {
+            gA[x] += __shfl_xor_sync(0xffffffffu, gA[x], o);
+            gB[x] += __shfl_xor_sync(0xffffffffu, gB[x], o);
+            gC[x] += __shfl_xor_sync(0xffffffffu, gC[x], o);
+        }
+    if (!active || r != 0) return;
+    const int atA = g.shell_atom[bp.A], atB = g.shell_atom[bp.B], atC = g.shell_atom[kp.A],
+              atD = g.shell_atom[kp.B];
+    for (int x = 0; x < 3; ++x) {
+        const double a = widen(gA[x]), b = widen(gB[x]), c = widen(gC[x]);
+        atomicAdd(g.grad + 3 * atA + x, a);
+        atomicAdd(g.grad + 3 * atB + x, b);
+        atomicAdd(g.grad + 3 * atC + x, c);
+        atomicAdd(g.grad + 3 * atD + x, -(a + b + c));
+    }
+}
+
 // ---------------------------------------------------------------------------
-// The classes with a d shell (run-time angular momenta): one contracted quartet
-// per warp.
+// The larger classes with a d shell (run-time angular momenta): one contracted
+// quartet per warp.
 // Per primitive quartet the warp builds the Hermite tables (E of bra and ket,
 // the Coulomb table R) once in shared memory; per chunk of ket component
 // pairs it builds the ket vectors Z0 = sum E^{cd} R (for the centre-A/B
@@ -454,7 +718,7 @@ __device__ __forceinline__ double gr_dot_r(const double (*E)[GR_NI][GR_NI][GR_NT
     return s;
 }
 
-#define GR1_MAXNUC 128  // nuclei of one geometry accumulated in registers/local memory
+#define GR1_NUCCHUNK 2  // nuclei per thread of k_grad1e (grid y runs over the chunks)
 
 // 1-D overlap factors S[i][j] = int x_A^i x_B^j exp(-p x_P^2) dx (Obara--Saika),
 // i <= imax, j <= jmax
@@ -476,28 +740,31 @@ __device__ __forceinline__ double gr_t1d(int i, int j, double b, const double (*
 }
 
 #ifndef RCHEM_GRAD_NO_KERNELS
-// One thread per ordered function pair (mu, nu) of a geometry.  Per primitive
-// pair the Gaussian product, the 1-D overlap table (shared by S and T and by
-// every shifted component) and the Hermite tables are formed once; per
-// nucleus one Boys evaluation and one Hermite Coulomb table serve both shifts
-// in all three directions.  The nuclei's terms are summed over the primitive
-// pairs before any atomic (in a per-thread array for up to GR1_MAXNUC nuclei).
+// One thread per ordered function pair (mu, nu) of a geometry and chunk of
+// GR1_NUCCHUNK nuclei (grid y), so a small system still fills the GPU.  Per
+// primitive pair the Gaussian product and the Hermite tables are formed once
+// (and, in chunk 0, the 1-D overlap table shared by S, T and every shifted
+// component); per nucleus one Boys evaluation and one Hermite Coulomb table
+// serve both shifts in all three directions.  The chunk's nuclei's terms are
+// summed over the primitive pairs before any atomic.
 __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const AOGrad *ao, const ShellGrad *sh,
                          const double *pexp, const double *pcoef, int natoms_total, const double *Z,
                          const double *Ratoms, const double *boys, const double *D, const double *W, double *grad) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= packed) return;
     const GeomDev gm = geo[geom_of(geo, ngeom, idx)];
+    // this thread's nuclei: chunk blockIdx.y; chunk 0 also takes the overlap and kinetic terms
+    const int c0 = blockIdx.y * GR1_NUCCHUNK, c1 = min(gm.natoms, c0 + GR1_NUCCHUNK);
+    const bool first = blockIdx.y == 0;
+    if (!first && c0 >= gm.natoms) return;
     const int loc = (int)(idx - gm.moff), mu = gm.ao0 + loc / gm.n, nu = gm.ao0 + loc % gm.n;
     const double Dmn = D[idx], Wmn = W[idx];
     if (Dmn == 0.0 && Wmn == 0.0) return;
     const AOGrad a = ao[mu], b = ao[nu];
     const ShellGrad sa = sh[a.shell], sb = sh[b.shell];
-    const bool local_nuc = gm.natoms <= GR1_MAXNUC;
     double gH[3] = {0, 0, 0}, gS[3] = {0, 0, 0};
-    double gN[GR1_MAXNUC][3];
-    if (local_nuc)
-        for (int c = 0; c < gm.natoms; ++c) gN[c][0] = gN[c][1] = gN[c][2] = 0.0;
+    double gN[GR1_NUCCHUNK][3];
+    for (int c = 0; c < GR1_NUCCHUNK; ++c) gN[c][0] = gN[c][1] = gN[c][2] = 0.0;
     const int L1 = a.lmn[0] + a.lmn[1] + a.lmn[2] + b.lmn[0] + b.lmn[1] + b.lmn[2] + 1;
     double AB[3], rab2 = 0.0;
     for (int d = 0; d < 3; ++d) {
@@ -515,9 +782,10 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
             for (int d = 0; d < 3; ++d) {
                 P[d] = (ea * sa.R[d] + eb * sb.R[d]) / p;
                 PA[d] = P[d] - sa.R[d];
-                gr_s1d(a.lmn[d] + 1, b.lmn[d] + 2, PA[d], P[d] - sb.R[d], ohp, p, S1[d]);
                 gr_herm<double>(a.lmn[d] + 1, b.lmn[d], PA[d], AB[d], ohp, E[d]);
             }
+            if (first) {
+            for (int d = 0; d < 3; ++d) gr_s1d(a.lmn[d] + 1, b.lmn[d] + 2, PA[d], P[d] - sb.R[d], ohp, p, S1[d]);
             // overlap and kinetic of the unshifted and shifted components
             double s0[3], t0[3];
             for (int d = 0; d < 3; ++d) {
@@ -536,9 +804,10 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
                 gS[x] += Kab * ds * sy;
                 gH[x] += Kab * dt;
             }
-            // nuclear attraction: one Boys evaluation and R table per nucleus
+            }
+            // nuclear attraction: one Boys evaluation and R table per nucleus of the chunk
             const double vpref = -2.0 * 3.14159265358979323846 / p * Kab;
-            for (int c = 0; c < gm.natoms; ++c) {
+            for (int c = c0; c < c1; ++c) {
                 const int cn = gm.atom0 + c;
                 const double X = P[0] - Ratoms[3 * cn], Y = P[1] - Ratoms[3 * cn + 1], Zc = P[2] - Ratoms[3 * cn + 2];
                 double F[GR_LMAX + 1], R[GR_NR];
@@ -559,17 +828,12 @@ __global__ void k_grad1e(long long packed, int ngeom, const GeomDev *geo, const 
                     v3[x] = v * vpref * Z[cn];
                     gH[x] += v3[x];
                 }
-                if (local_nuc) {
-                    for (int x = 0; x < 3; ++x) gN[c][x] += v3[x];
-                } else {
-                    for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * cn + x, -4.0 * Dmn * v3[x]);
-                }
+                for (int x = 0; x < 3; ++x) gN[c - c0][x] += v3[x];
             }
         }
     }
-    if (local_nuc)
-        for (int c = 0; c < gm.natoms; ++c)
-            for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * (gm.atom0 + c) + x, -4.0 * Dmn * gN[c][x]);
+    for (int c = c0; c < c1; ++c)
+        for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * (gm.atom0 + c) + x, -4.0 * Dmn * gN[c - c0][x]);
     for (int x = 0; x < 3; ++x) atomicAdd(grad + 3 * sa.atom + x, 4.0 * Dmn * gH[x] - 4.0 * Wmn * gS[x]);
     (void)natoms_total;
 }

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -176,12 +177,16 @@ static int pair_cls(int la, int lb) {
 }
 static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
 // gradient work lists: (s/p class, precision) pairs, then (every class with a d shell, precision)
-#define GRAD_NLIST (2 * RCHEM_NCLASS + 2)
+// gradient lists: 2k + prec for the s/p class k; 2 NCLASS + prec for the smaller
+// classes with a d shell (per-lane kernel), 2 NCLASS + 2 + prec for the larger ones
+// (warp-cooperative kernel)
+#define GRAD_NLIST (2 * RCHEM_NCLASS + 4)
 // the specialised s/p gradient kernels, one translation unit per arithmetic (grad_sp_*.cu)
 bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_wc_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
+void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // generic kernels (scalar cints entry points, one-electron matrices)
@@ -1364,6 +1369,16 @@ extern "C" int rchem_jk_direct_part(rchem_basis b, const double *D, double *J, d
 // (bra group, ket group) combination as segments, packed into warp tasks with
 // G lanes per quartet (at least kGradPrimPerLane primitive quartets per lane:
 // a derivative primitive quartet is ~100x a Fock one), heaviest tasks first.
+// Component quartets from which a d class's gradient runs the warp-cooperative
+// kernel (RCHEM_GRAD_WC_MIN overrides it, for tuning).
+static long long grad_wc_min() {
+    static const long long v = [] {
+        const char *e = getenv("RCHEM_GRAD_WC_MIN");
+        return e ? atoll(e) : 108LL;
+    }();
+    return v;
+}
+
 static int plan_gradient(rchem_basis b, double tau, double tau32) {
     if (b->d_gtasks && b->gq_tau == tau && b->gq_tau32 == tau32) return RCHEM_OK;
     constexpr long long kGradPrimPerLane = 2;
@@ -1387,7 +1402,13 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             const long long units = sp ? nprimq : nprimq * ncart(gk.la) * ncart(gk.lb);
             int lg = 0;
             while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
-            if (!sp) lg = 5;  // the d-class kernel: one quartet per warp
+            // the larger d classes (at least kGradWcMin component quartets) run the
+            // warp-cooperative kernel, one quartet per warp; the smaller ones keep
+            // whole quartets per lane group, whose lanes the cooperative kernel
+            // could not fill
+            const bool wc = !sp && (long long)ncart(gb.la) * ncart(gb.lb) * ncart(gk.la) * ncart(gk.lb) >=
+                                       grad_wc_min();
+            if (wc) lg = 5;
             const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
             for (int prec = 0; prec < 2; ++prec) {
                 const int s0 = (int)segs.size();
@@ -1405,7 +1426,7 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
                 }
                 if (total == 0) continue;
                 pack_tasks(segs, s0, total, lg, ((units + (1 << lg) - 1) >> lg) * work,
-                           per_class[sp ? 2 * k + prec : 2 * RCHEM_NCLASS + prec]);
+                           per_class[sp ? 2 * k + prec : 2 * RCHEM_NCLASS + (wc ? 2 : 0) + prec]);
             }
         }
     }
@@ -1504,9 +1525,16 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
                 CK(cudaGetLastError());
                 continue;
             }
-            // classes with d shells: the warp-cooperative kernel (run-time angular momenta,
-            // one quartet per warp), FP32 below tau32 and FP64 above (also in the
-            // emulated form, which keeps these classes in FP64)
+            // classes with d shells (run-time angular momenta), FP32 below tau32 and FP64
+            // above (also in the emulated form, which keeps these classes in FP64): the
+            // smaller ones one lane group per quartet, the larger warp-cooperatively
+            if (k < 2 * RCHEM_NCLASS + 2) {
+                const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
+                if (k & 1) rchem_grad_rt_f32(g, blocks, st);
+                else k_grad2e_rt<double><<<blocks, 64, 0, st>>>(g);
+                CK(cudaGetLastError());
+                continue;
+            }
             const unsigned blocks = (unsigned)((b->gtask_cnt[k] + GW_WARPS - 1) / GW_WARPS);
             if (k & 1) {
                 if (!rchem_grad_wc_f32(g, blocks, st))
@@ -1524,7 +1552,10 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         }
     }
     const int th = 128;
-    k_grad1e<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>(
+    int maxnuc = 1;
+    for (const GeomDev &gm : b->geoms) maxnuc = std::max(maxnuc, gm.natoms);
+    const dim3 g1((unsigned)((nn + th - 1) / th), (unsigned)((maxnuc + GR1_NUCCHUNK - 1) / GR1_NUCCHUNK));
+    k_grad1e<<<g1, th, 0, b->stream>>>(
         (long long)nn, b->ngeom, b->d_geom, reinterpret_cast<const AOGrad *>(b->d_ao),
         reinterpret_cast<const ShellGrad *>(b->d_sh), b->d_pexp, b->d_pcoef, na, b->d_Z, b->d_R, b->tabs->boys64,
         b->d_D, b->d_W, b->d_grad);
