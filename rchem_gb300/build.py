@@ -60,7 +60,8 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         return LIB
     _generate()
     srcs = [os.path.join(CSRC, f) for f in ("rchem_gpu.cu", "peak.cu", "grad_sp_f64.cu", "grad_sp_f32.cu",
-                                            "grad_sp_df64.cu", "grad_sp_df64b.cu", "onee_cls.cu")]
+                                            "grad_sp_df64.cu", "grad_sp_df64b.cu", "grad_sd_f64.cu",
+                                            "grad_sd_f32.cu", "onee_cls.cu")]
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("eri_") and f.endswith(".cu"))
     nvcc = _nvcc()
 

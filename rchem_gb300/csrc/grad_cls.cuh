@@ -1,6 +1,8 @@
 // grad_cls.cuh -- the two-electron gradient kernel specialised per integral
-// class for s and p shells (l <= 1 on every centre), in FP64, FP32 (the mixed
-// form's small quartets) or double-float (the emulated form).
+// class, in FP64, FP32 (the mixed form's small quartets) or double-float (the
+// emulated form): every class of s and p shells, and the smallest classes with a
+// d shell ((ds|ss), (ds|ps), (ds|ds), (dp|ss)), whose unrolled code still fits
+// the registers; the larger d classes run the run-time-l kernels of grad.cuh.
 //
 // Same mathematics and work layout as k_grad2e (grad.cuh): McMurchie--Davidson
 // Hermite integrals, the shifted-angular-momentum derivative relation, Gamma
@@ -32,6 +34,13 @@ constexpr int comp(int l, int k, int axis) {
         for (int b = 1; b <= a; ++b, ++idx)
             if (idx == k) return axis == 0 ? l + 1 - a : (axis == 1 ? a - b : b - 1);
     return 0;
+}
+
+// N(alpha,l,m,n) / N(alpha,L,0,0) of component k of angular momentum l
+// (src/basis.rs:140-149): sqrt((2L-1)!! / ((2l-1)!! (2m-1)!! (2n-1)!!))
+__device__ __forceinline__ double cnorm(int l, int k) {
+    const double f2[5] = {1.0, 1.0, 3.0, 15.0, 105.0};  // (2j-1)!! for j = 0..4
+    return sqrt(f2[l] / (f2[comp(l, k, 0)] * f2[comp(l, k, 1)] * f2[comp(l, k, 2)]));
 }
 
 template <typename F, int... I>
@@ -196,8 +205,9 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
     if (bp.diag) deg *= 0.5;
     if (kp.diag) deg *= 0.5;
     if (seg.bra == seg.ket0 + off) deg *= 0.5;
-    // Gamma with the degeneracy and the component norms (l <= 1: all norms are 1),
+    // Gamma with the degeneracy and the component norms (1 for s and p shells),
     // formed in FP64 and then rounded to the kernel's arithmetic
+    constexpr bool kNorms = LA > 1 || LB > 1 || LC > 1 || LD > 1;
     R Gam[NC * ND * NA * NB];
     sfor<NC>([&](auto kc_) {
         sfor<ND>([&](auto kd_) {
@@ -208,9 +218,12 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
                 sfor<NB>([&](auto kb_) {
                     constexpr int ka = decltype(ka_)::value, kb = decltype(kb_)::value;
                     const int mu = bp.aoA + ka, nu = bp.aoB + kb;
+                    double w = deg;
+                    if constexpr (kNorms)
+                        w *= cnorm(LA, ka) * cnorm(LB, kb) * cnorm(LC, kc) * cnorm(LD, kd);
                     Gam[((kc * ND + kd) * NA + ka) * NB + kb] = gt_narrow(
-                        deg * (2.0 * Dg[mu * n + nu] * Dls -
-                               0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
+                        w * (2.0 * Dg[mu * n + nu] * Dls -
+                             0.5 * (Dg[mu * n + l_] * Dg[nu * n + s_] + Dg[mu * n + s_] * Dg[nu * n + l_])),
                         (R *)nullptr);
                 });
             });

@@ -185,6 +185,8 @@ static int quartet_kernel(int cb, int ck) { return cb * (cb + 1) / 2 + ck; }
 bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_sd_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_sd_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_wc_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
 void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
 
@@ -1370,14 +1372,10 @@ extern "C" int rchem_jk_direct_part(rchem_basis b, const double *D, double *J, d
 // G lanes per quartet (at least kGradPrimPerLane primitive quartets per lane:
 // a derivative primitive quartet is ~100x a Fock one), heaviest tasks first.
 // Component quartets from which a d class's gradient runs the warp-cooperative
-// kernel (RCHEM_GRAD_WC_MIN overrides it, for tuning).
-static long long grad_wc_min() {
-    static const long long v = [] {
-        const char *e = getenv("RCHEM_GRAD_WC_MIN");
-        return e ? atoll(e) : 108LL;
-    }();
-    return v;
-}
+// kernel: (dd|dp) and (dd|dd).  Measured on (H2O)4 6-31G**-shaped: every
+// threshold from 1 to "never" gave 75 ms (1) ... 44 ms (216) ... 42.7 ms (648),
+// 43.3 ms (never); below that the lanes of one quartet's warp stay idle.
+static long long grad_wc_min() { return 648; }
 
 static int plan_gradient(rchem_basis b, double tau, double tau32) {
     if (b->d_gtasks && b->gq_tau == tau && b->gq_tau32 == tau32) return RCHEM_OK;
@@ -1398,7 +1396,9 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             // FP64 (or double-float) above tau32, FP32 below
             const int k = quartet_kernel(gb.cls, gk.cls);
             const int *l = rchem_class_l[k];
-            const bool sp = l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1;
+            // the s/p classes and the smallest d classes have compile-time kernels
+            const bool sp = (l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1) || k == 6 || k == 7 || k == 9 ||
+                            k == 10;
             const long long units = sp ? nprimq : nprimq * ncart(gk.la) * ncart(gk.lb);
             int lg = 0;
             while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
@@ -1518,9 +1518,9 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
             if (k < 2 * RCHEM_NCLASS) {  // an s/p class: its specialised kernel
                 const unsigned blocks = (unsigned)((b->gtask_cnt[k] + 1) / 2);  // one warp per task
                 const int cls = k / 2;
-                const bool ok = (k & 1) ? rchem_grad_sp_f32(cls, g, blocks, st)
+                const bool ok = (k & 1) ? (rchem_grad_sp_f32(cls, g, blocks, st) || rchem_grad_sd_f32(cls, g, blocks, st))
                                         : (((o.emulated & RCHEM_JK_EMULATED) && rchem_grad_sp_df64(cls, g, blocks, st)) ||
-                                           rchem_grad_sp_f64(cls, g, blocks, st));
+                                           rchem_grad_sp_f64(cls, g, blocks, st) || rchem_grad_sd_f64(cls, g, blocks, st));
                 if (!ok) return set_err(RCHEM_ERR_UNSUPPORTED, "gradient list %d has no specialised kernel", k);
                 CK(cudaGetLastError());
                 continue;
