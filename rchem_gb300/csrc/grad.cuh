@@ -272,7 +272,10 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     const int nunits = active ? ntot * ncd : 0;  // idle lanes only join the reduction
     int cur = -1;
     R a2 = R(0), b2 = R(0), c2 = R(0);
-    for (int u = r; u < nunits; u += G) {
+    // each lane a contiguous run of units, so consecutive units mostly share a
+    // primitive quartet and its tables are built once per run, not per unit
+    const int per = (nunits + G - 1) / G, u0 = r * per, u1 = min(nunits, u0 + per);
+    for (int u = u0; u < u1; ++u) {
         const int tq = u / ncd, kcd = u - tq * ncd;
         if (tq != cur) {  // primitive-quartet tables, kept while the lane stays on it
             cur = tq;

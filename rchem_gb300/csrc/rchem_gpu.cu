@@ -1400,8 +1400,13 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             const bool sp = (l[0] <= 1 && l[1] <= 1 && l[2] <= 1 && l[3] <= 1) || k == 6 || k == 7 || k == 9 ||
                             k == 10;
             const long long units = sp ? nprimq : nprimq * ncart(gk.la) * ncart(gk.lb);
+            // lanes per quartet: at least kGradPrimPerLane units per lane (for the run-time
+            // d-class kernel at least one primitive quartet's ket component pairs, so a
+            // lane's run of units shares its primitive-quartet tables)
+            const long long per_lane = sp ? kGradPrimPerLane
+                                          : std::max<long long>(kGradPrimPerLane, ncart(gk.la) * ncart(gk.lb));
             int lg = 0;
-            while (lg < 5 && units >= kGradPrimPerLane << (lg + 1)) ++lg;
+            while (lg < 5 && units >= per_lane << (lg + 1)) ++lg;
             // the larger d classes (at least kGradWcMin component quartets) run the
             // warp-cooperative kernel, one quartet per warp; the smaller ones keep
             // whole quartets per lane group, whose lanes the cooperative kernel
