@@ -13,8 +13,8 @@
 //   T >= BOYS_TMAX: F_0 = sqrt(pi/T)/2 (erfc(sqrt T) < 4e-19 there) and the
 //     upward recursion F_{m+1} = ((2m+1) F_m - e^{-T}) / (2T), stable for T > m.
 // All F values come out multiplied by the caller's prefactor.
-// The grid index uses the add-2^52+2^51 rounding, so no int<->double
-// conversions run on the (narrow) FP64 pipe.
+// The FP64 grid index and the T < TMAX test use integer operations on T's bits,
+// so only the Taylor chains and one subtraction run on the (narrow) FP64 pipe.
 #pragma once
 #include <math.h>
 #include <string.h>
@@ -41,6 +41,17 @@ template <> struct BoysPrec<float> { static constexpr int NTAY = BOYS_NT32; };
 template <typename R> RCHEM_HD constexpr R rchem_recip(int k) { return R(1.0 / (double)k); }
 template <> RCHEM_HD constexpr float rchem_recip<float>(int k) { return 1.0f / (float)k; }
 RCHEM_HD inline bool rchem_lt(double a, double b) { return a < b; }
+// T < BOYS_TMAX for T >= 0 (or -0), compared on the bit pattern: an integer
+// compare keeps the test off the narrow FP64 pipe (NaN goes to the T >= TMAX
+// branch, as with the floating-point compare)
+RCHEM_HD inline bool boys_small(double T) {
+#ifdef __CUDA_ARCH__
+    return __double_as_longlong(T) < 0x4044000000000000LL;  // bits of 40.0
+#else
+    return T < BOYS_TMAX;
+#endif
+}
+RCHEM_HD inline bool boys_small(float T) { return T < (float)BOYS_TMAX; }
 RCHEM_HD inline bool rchem_lt(float a, float b) { return a < b; }
 RCHEM_HD inline float rchem_tofloat(double a) { return (float)a; }
 RCHEM_HD inline float rchem_tofloat(float a) { return a; }
@@ -79,18 +90,33 @@ RCHEM_HD inline R rchem_ldg(const R *p) {
 #endif
 }
 
-// nearest grid row i and x = T_i - T, for 0 <= T < BOYS_TMAX
+// nearest grid row i and x = T_i - T, for 0 <= T < BOYS_TMAX.  On the device
+// the row comes from T's bits with integer operations (T = m 2^(e-52), so
+// T/h = m 2^(e-46), rounded half up) and T_i = i h is assembled as a double
+// from i's bits, leaving one FP64 subtraction; the host rounds with the
+// 2^52 + 2^51 addition.  Either rounding keeps |x| <= h/2.
 RCHEM_HD inline void boys_grid(double T, int &i, double &x) {
+#ifdef __CUDA_ARCH__
+    const long long bits = __double_as_longlong(T);
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;  // T < 40: e <= 5
+    const int sh = 46 - e;                              // >= 41
+    const long long m = (bits & 0xfffffffffffffLL) | 0x10000000000000LL;
+    i = (e < -1022 || sh >= 63) ? 0 : (int)((m + (1LL << (sh - 1))) >> sh);
+    double Ti = 0.0;
+    if (i > 0) {
+        const int msb = 31 - __clz(i);  // i h = i 2^-6: exponent msb - 6, mantissa i's lower bits
+        Ti = __longlong_as_double(((long long)(msb - 6 + 1023) << 52) |
+                                  (((long long)i << (52 - msb)) & 0xfffffffffffffLL));
+    }
+    x = Ti - T;
+#else
     const double magic = 6755399441055744.0;  // 2^52 + 2^51
     const double t = fma(T, BOYS_INVH, magic);
-#ifdef __CUDA_ARCH__
-    i = __double2loint(t);
-#else
     long long bits;
     memcpy(&bits, &t, sizeof(bits));
     i = (int)(bits & 0xffffffffLL);
-#endif
     x = fma(t - magic, BOYS_H, -T);
+#endif
 }
 RCHEM_HD inline void boys_grid(float T, int &i, float &x) {
     const float magic = 12582912.0f;  // 2^23 + 2^22
@@ -122,7 +148,7 @@ RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
 // F[0..L] = pref * F_m(T).
 template <int L, typename R>
 RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
-    if (rchem_lt(T, R(BOYS_TMAX))) {
+    if (boys_small(T)) {
         int i;
         R x;
         boys_grid(T, i, x);

@@ -78,6 +78,7 @@ __device__ __forceinline__ df64 &operator*=(df64 &a, df64 b) {
     return a;
 }
 __device__ __forceinline__ bool rchem_lt(df64 a, df64 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool boys_small(df64 T) { return rchem_lt(T, df64(40.0f)); }
 __device__ __forceinline__ float rchem_tofloat(df64 a) { return a.hi; }
 __device__ __forceinline__ df64 rchem_fma(df64 a, df64 b, df64 c) { return df_fma(a, b, c); }
 __device__ __forceinline__ df64 rchem_rsqrt(df64 x) { return df_rsqrt(x); }
