@@ -165,10 +165,16 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
     } else {
         const R rs = rchem_rsqrt(T);
         const R inv2T = R(0.5) * rs * rs;
-        const R ex = R(rchem_expf(-rchem_tofloat(T))) * pref;
         F[0] = R(0.88622692545275801365) * rs * pref;
+        if (L <= 1) {
+            // e^{-T} / F_0 < 3e-17 for T >= 40: the correction is below FP64 rounding
 #pragma unroll
-        for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;
+            for (int m = 1; m <= L; ++m) F[m] = F[m - 1] * inv2T;
+        } else {
+            const R ex = R(rchem_expf(-rchem_tofloat(T))) * pref;
+#pragma unroll
+            for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;
+        }
     }
 }
 
