@@ -145,19 +145,21 @@ RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
 // Direct evaluation of every F_m is cheaper up to this L.
 #define BOYS_DIRECT_MAXL 1
 
-// F[0..L] = pref * F_m(T).
-template <int L, typename R>
+// F[0..L] = pref * F_m(T); with SCALE false, F[0..L] = F_m(T) (pref unused), for
+// callers that fold the prefactor into their own products.
+template <int L, typename R, bool SCALE = true>
 RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
+    auto sc = [&](R v) { return SCALE ? v * pref : v; };
     if (boys_small(T)) {
         int i;
         R x;
         boys_grid(T, i, x);
         if (L <= BOYS_DIRECT_MAXL) {
 #pragma unroll
-            for (int m = 0; m <= L; ++m) F[m] = boys_horner(tab, m + 1, i, x) * pref;
+            for (int m = 0; m <= L; ++m) F[m] = sc(boys_horner(tab, m + 1, i, x));
         } else {
-            const R ex = boys_horner(tab, 0, i, x) * pref;
-            F[L] = boys_horner(tab, L + 1, i, x) * pref;
+            const R ex = sc(boys_horner(tab, 0, i, x));
+            F[L] = sc(boys_horner(tab, L + 1, i, x));
             const R T2 = T + T;
 #pragma unroll
             for (int m = L - 1; m >= 0; --m) F[m] = rchem_fma(T2, F[m + 1], ex) * rchem_recip<R>(2 * m + 1);
@@ -165,13 +167,13 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
     } else {
         const R rs = rchem_rsqrt(T);
         const R inv2T = R(0.5) * rs * rs;
-        F[0] = R(0.88622692545275801365) * rs * pref;
+        F[0] = sc(R(0.88622692545275801365) * rs);
         if (L <= 1) {
             // e^{-T} / F_0 < 3e-17 for T >= 40: the correction is below FP64 rounding
 #pragma unroll
             for (int m = 1; m <= L; ++m) F[m] = F[m - 1] * inv2T;
         } else {
-            const R ex = R(rchem_expf(-rchem_tofloat(T))) * pref;
+            const R ex = sc(R(rchem_expf(-rchem_tofloat(T))));
 #pragma unroll
             for (int m = 1; m <= L; ++m) F[m] = (R(2 * m - 1) * F[m - 1] - ex) * inv2T;
         }

@@ -129,18 +129,54 @@ template <> struct Tabs<float> {
 // Scaled Boys values F[0..L] of one primitive quartet.  With a.f32_boys64 the
 // FP32 kernels evaluate the function and its downward recursion in FP64 from
 // the FP32 argument and prefactor, and round the results to FP32.
-template <int L, typename R>
+template <int L, typename R, bool SCALE = true>
 __device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R *btab, R *F) {
     if constexpr (std::is_same<R, float>::value) {
         if (a.f32_boys64) {
             double Fd[L + 1];
-            boys_eval<L, double>((double)T, (double)pref, a.boys64, Fd);
+            boys_eval<L, double, SCALE>((double)T, (double)pref, a.boys64, Fd);
 #pragma unroll
             for (int m = 0; m <= L; ++m) F[m] = (float)Fd[m];
             return;
         }
     }
-    boys_eval<L, R>(T, pref, btab, F);
+    boys_eval<L, R, SCALE>(T, pref, btab, F);
+}
+
+// The factors of a primitive quartet that depend only on the two exponents p
+// and q: rs = 1/sqrt(p+q), ipq = 1/(p+q), rho = pq/(p+q), qi = q/(p+q),
+// pi = p/(p+q).  With a table (a.npq > 0; FP64 and double-float) they are two
+// loads indexed by the primitive pairs' exponent numbers, which takes the
+// reciprocal square root and four products off the FP64 pipe; FP32 computes them.
+template <typename R> struct PqLoad;
+template <> struct PqLoad<double> {
+    static __device__ __forceinline__ void get(const EriArgs &a, int e, double &rs, double &rho, double &qi,
+                                               double &pi) {
+        const double2 v0 = __ldg(a.pq64 + 2 * e), v1 = __ldg(a.pq64 + 2 * e + 1);
+        rs = v0.x; rho = v0.y; qi = v1.x; pi = v1.y;
+    }
+};
+template <> struct PqLoad<df64> {
+    static __device__ __forceinline__ void get(const EriArgs &a, int e, df64 &rs, df64 &rho, df64 &qi, df64 &pi) {
+        const float4 v0 = __ldg(a.pqdf + 2 * e), v1 = __ldg(a.pqdf + 2 * e + 1);
+        rs = df64(v0.x, v0.y); rho = df64(v0.z, v0.w); qi = df64(v1.x, v1.y); pi = df64(v1.z, v1.w);
+    }
+};
+template <typename R>
+__device__ __forceinline__ void pq_factors(const EriArgs &a, int ib, int ik, R p, R q, R &rs, R &ipq, R &rho, R &qi,
+                                           R &pi) {
+    if constexpr (!std::is_same<R, float>::value) {
+        if (a.npq) {  // launch-uniform
+            PqLoad<R>::get(a, __ldg(a.prim_eid + ib) * a.npq + __ldg(a.prim_eid + ik), rs, rho, qi, pi);
+            ipq = rs * rs;
+            return;
+        }
+    }
+    rs = rchem_rsqrt(p + q);
+    ipq = rs * rs;
+    qi = q * ipq;
+    pi = p * ipq;
+    rho = p * qi;
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int EPI>
@@ -172,29 +208,40 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 
     const R *btab = Tabs<R>::boys(a);
     // one primitive quartet: Boys function, then the VRR into acc
-    auto prim = [&](const R p, const R ohp, const R *P, const R *PA, const R Kab, const R q, const R ohq,
-                    const R *Q, const R *QC, const R Kcd) {
-        const R pq = p + q;
-        const R rs = rchem_rsqrt(pq);
-        const R ipq = rs * rs;
+    auto prim = [&](const R ohp, const R *P, const R *PA, const R Kab, const R ohq, const R *Q, const R *QC,
+                    const R Kcd, const R rs, const R ipq, const R rho, const R qi_, const R pi_) {
         const R PQx = P[0] - Q[0], PQy = P[1] - Q[1], PQz = P[2] - Q[2];
-        const R qi_ = q * ipq, pi_ = p * ipq;
-        const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
+        const R T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
         const R pref = Kab * Kcd * rs;
         R F[L + 1];
-        eri_boys<L, R>(a, T, pref, btab, F);
-        C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi_ * PQx, -qi_ * PQy, -qi_ * PQz, QC[0], QC[1], QC[2],
-                           pi_ * PQx, pi_ * PQy, pi_ * PQz, ohp, ohq, R(0.5) * ipq, qi_, pi_);
+        if constexpr (L == 0) {
+            // (ss|ss): the integral is pref F_0; the prefactor goes into the accumulating FMA
+            eri_boys<0, R, false>(a, T, pref, btab, F);
+            acc[0] = rchem_fma(F[0], pref, acc[0]);
+        } else if constexpr (LA == 1 && LB == 0 && LC == 0 && LD == 0) {
+            // (ps|ss): (PA_i F_0 + WP_i F_1) pref with WP = -q/(p+q) PQ, as
+            // PA_i (pref F_0) + PQ_i (-pref q/(p+q) F_1)
+            eri_boys<1, R, false>(a, T, pref, btab, F);
+            const R f0 = F[0] * pref, f1 = F[1] * (pref * -qi_);
+            acc[0] = rchem_fma(PQx, f1, rchem_fma(PA[0], f0, acc[0]));
+            acc[1] = rchem_fma(PQy, f1, rchem_fma(PA[1], f0, acc[1]));
+            acc[2] = rchem_fma(PQz, f1, rchem_fma(PA[2], f0, acc[2]));
+        } else {
+            eri_boys<L, R>(a, T, pref, btab, F);
+            C::template vrr<R>(acc, F, PA[0], PA[1], PA[2], -qi_ * PQx, -qi_ * PQy, -qi_ * PQz, QC[0], QC[1], QC[2],
+                               pi_ * PQx, pi_ * PQy, pi_ * PQz, ohp, ohq, R(0.5) * ipq, qi_, pi_);
+        }
     };
     // the G lanes of a quartet split its npp_bra x npp_ket primitive quartets
     // (one flat loop: a single inlined copy of the VRR), then reduce
     const int nk = kp.npp, ntot = bp.npp * nk;
     for (int tq = r; tq < ntot; tq += G) {
         const int ia = tq / nk, ic = tq - ia * nk;
-        R p, ohp, P[3], PA[3], Kab, q, ohq, Q[3], QC[3], Kcd;
+        R p, ohp, P[3], PA[3], Kab, q, ohq, Q[3], QC[3], Kcd, rs, ipq, rho, qi_, pi_;
         PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, P, PA, Kab);
         PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Q, QC, Kcd);
-        prim(p, ohp, P, PA, Kab, q, ohq, Q, QC, Kcd);
+        pq_factors<R>(a, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi_, pi_);
+        prim(ohp, P, PA, Kab, ohq, Q, QC, Kcd, rs, ipq, rho, qi_, pi_);
     }
     for (int o = G >> 1; o > 0; o >>= 1)
 #pragma unroll
@@ -459,12 +506,10 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         R p, ohp, Pc[3], PA[3], Kab, q, ohq, Qc[3], QC[3], Kcd;
         PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, Pc, PA, Kab);
         PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Qc, QC, Kcd);
-        const R pq = p + q;
-        const R rs = rchem_rsqrt(pq);
-        const R ipq = rs * rs;
+        R rs, ipq, rho, qi_, pi_;
+        pq_factors<R>(a, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi_, pi_);
         const R PQx = Pc[0] - Qc[0], PQy = Pc[1] - Qc[1], PQz = Pc[2] - Qc[2];
-        const R qi_ = q * ipq, pi_ = p * ipq;
-        const R T = p * qi_ * (PQx * PQx + PQy * PQy + PQz * PQz);
+        const R T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
         R F[L + 1];
         eri_boys<L, R>(a, T, Kab * Kcd * rs, btab, F);
         const R WP[3] = {-qi_ * PQx, -qi_ * PQy, -qi_ * PQz}, WQ[3] = {pi_ * PQx, pi_ * PQy, pi_ * PQz};

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <tuple>
 #include <mutex>
 #include <string>
@@ -361,6 +362,11 @@ struct rchem_basis_s {
     PairPrim *d_prims = nullptr;
     PairPrim32 *d_prims32 = nullptr;
     PairPrimDF *d_primsdf = nullptr;
+    // factors of (p, q) by primitive-pair exponent number (EriArgs::pq64)
+    int npq = 0;
+    int *d_prim_eid = nullptr;
+    double2 *d_pq64 = nullptr;
+    float4 *d_pqdf = nullptr;
     float2 *d_Ddf = nullptr;
     AODev *d_ao = nullptr;
     ShellDev *d_sh = nullptr;
@@ -417,7 +423,7 @@ static void free_basis(rchem_basis b) {
     void *ptrs[] = {b->d_pairs, b->d_prims, b->d_prims32, b->d_primsdf, b->d_Ddf, b->d_ao, b->d_sh, b->d_pexp, b->d_pcoef, b->d_Z,
                     b->d_R, b->d_tasks, b->d_segs, b->d_D, b->d_Jh, b->d_Kh, b->d_Jo, b->d_Ko, b->d_D32,
                     b->d_shell_atom, b->d_shell_l, b->d_gtasks, b->d_gsegs, b->d_W, b->d_grad, b->d_geom,
-                    b->d_opairs};
+                    b->d_opairs, b->d_prim_eid, b->d_pq64, b->d_pqdf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < rchem_basis_s::NAUX; ++i) {
@@ -458,6 +464,10 @@ static EriArgs base_args(rchem_basis b) {
     a.boysdf = b->tabs->boysdf;
     a.primsdf = b->d_primsdf;
     a.Ddf = b->d_Ddf;
+    a.npq = b->npq;
+    a.prim_eid = b->d_prim_eid;
+    a.pq64 = b->d_pq64;
+    a.pqdf = b->d_pqdf;
     return a;
 }
 
@@ -533,6 +543,56 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
     Q.assign(np, 0.0);
     CK(cudaMemcpyAsync(Q.data(), d_Q, (size_t)np * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    return RCHEM_OK;
+}
+
+// The primitive pairs' distinct exponents p (numbered by first appearance)
+// and, for every ordered couple (p, q) of them, 1/sqrt(p+q), pq/(p+q),
+// q/(p+q), p/(p+q) in FP64 and as double-float pairs.  A basis has few
+// distinct exponents (the exponent sums of its shells), so the table is small
+// and cache-resident; past kPqMax exponents the kernels compute the factors.
+static const int kPqMax = 512;
+static int build_pq_table(rchem_basis b, const std::vector<PairPrim> &prims) {
+    std::unordered_map<unsigned long long, int> num;
+    std::vector<double> pv;
+    std::vector<int> eid(prims.size());
+    for (size_t i = 0; i < prims.size(); ++i) {
+        unsigned long long bits;
+        memcpy(&bits, &prims[i].p, sizeof(bits));
+        auto it = num.find(bits);
+        if (it == num.end()) {
+            it = num.emplace(bits, (int)pv.size()).first;
+            pv.push_back(prims[i].p);
+        }
+        eid[i] = it->second;
+    }
+    const int n = (int)pv.size();
+    if (n == 0 || n > kPqMax) {
+        b->npq = 0;
+        return RCHEM_OK;
+    }
+    std::vector<double2> t64((size_t)2 * n * n);
+    std::vector<float4> tdf((size_t)2 * n * n);
+    auto split = [](double v, float &hi, float &lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const double p = pv[i], q = pv[j], s = p + q;
+            const double v[4] = {1.0 / std::sqrt(s), p * q / s, q / s, p / s};
+            const size_t e = (size_t)2 * (i * n + j);
+            t64[e] = make_double2(v[0], v[1]);
+            t64[e + 1] = make_double2(v[2], v[3]);
+            float h[8];
+            for (int k = 0; k < 4; ++k) split(v[k], h[2 * k], h[2 * k + 1]);
+            tdf[e] = make_float4(h[0], h[1], h[2], h[3]);
+            tdf[e + 1] = make_float4(h[4], h[5], h[6], h[7]);
+        }
+    CKR(upload(&b->d_prim_eid, eid, b->stream));
+    CKR(upload(&b->d_pq64, t64, b->stream));
+    CKR(upload(&b->d_pqdf, tdf, b->stream));
+    b->npq = n;
     return RCHEM_OK;
 }
 
@@ -675,6 +735,7 @@ static int build_pairs(rchem_basis b) {
     CKR(upload(&b->d_prims, prims, b->stream));
     CKR(upload(&b->d_prims32, p32, b->stream));
     CKR(upload(&b->d_primsdf, pdf, b->stream));
+    CKR(build_pq_table(b, prims));
     CKR(upload(&b->d_pairs, b->pairs, b->stream));
     // Schwarz bounds, then sort each group by Q descending
     std::vector<double> Q;
@@ -699,6 +760,13 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
 // default tile shape: lanes share a quartet only while each keeps at least
 // this many primitive quartets
 static const int kMinPrimPerLane = 16;
+
+// Algorithmic FLOPs of one primitive quartet of class kernel k: the generated
+// count, less p+q, 1/sqrt(p+q) (counted as 4), q/(p+q) and p/(p+q) where the
+// FP64 and double-float lists (prec 0) read them from the exponent table
+static double prim_flops(rchem_basis b, int k, int prec) {
+    return rchem_class_flops[k][0] - ((prec == 0 && b->npq > 0) ? 7.0 : 0.0);
+}
 
 // Split the bra shell pairs of a build into nparts shares of about equal cost:
 // each bra pair's cost is the algorithmic FLOPs of its surviving quartets
@@ -786,7 +854,7 @@ static int plan_tasks(rchem_basis b, double tau, double tau32, int part = 0, int
                 while (lg < 5 && nprimq >= ppl << (lg + 1)) ++lg;
                 if (b->wc[k][prec] || rchem_class_wc_only[k]) lg = 5;  // warp-cooperative: one quartet per warp
                 pack_tasks(sv, s0, total, lg, (nprimq + (1 << lg) - 1) >> lg, lists[k][prec]);
-                const double fl = rchem_class_flops[k][0] * nprimq * total + rchem_class_flops[k][1] * total;
+                const double fl = prim_flops(b, k, prec) * nprimq * total + rchem_class_flops[k][1] * total;
                 b->list_flops[k][prec] += fl;
                 b->class_quartets[k][prec] += total;
                 b->class_prims[k][prec] += total * nprimq;

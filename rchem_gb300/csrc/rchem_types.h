@@ -15,6 +15,8 @@
 
 #ifndef __CUDACC__
 struct float2;  // host-only compiles see the device argument block by pointer only
+struct double2;
+struct float4;
 #endif
 
 #define RCHEM_LMAX 2          // s, p, d shells (Cartesian)
@@ -100,6 +102,12 @@ struct EriArgs {
     int eri_packed;        // 1: one value per unique integral at the 8-fold index (rchem_eri_pack8)
     int wc;                // J/K epilogue of a large class: 1 = warp-cooperative kernel, 0 = one lane group per quartet
     int f32_boys64;        // FP32 quartets: Boys function and downward recursion in FP64
+    // per (bra, ket) primitive-pair exponent: 1/sqrt(p+q), pq/(p+q), q/(p+q),
+    // p/(p+q) from a table (FP64 and double-float kernels); npq = 0: computed
+    int npq;               // distinct primitive-pair exponents p (table side)
+    const int *prim_eid;   // per primitive pair: index of its p among them
+    const double2 *pq64;   // entry (i, j) at 2 (i npq + j): {rs, rho}, {q/(p+q), p/(p+q)}
+    const float4 *pqdf;    // the same as (hi, lo) float pairs
 };
 
 // Shell as the planner sees it.
