@@ -268,6 +268,17 @@ int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen);
  */
 int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl);
 
+/*
+ * The factors of a primitive quartet that depend only on its two exponent sums
+ * p and q (1/sqrt(p+q), pq/(p+q), q/(p+q), p/(p+q)) come from a table built at
+ * rchem_basis_create over the basis's distinct p (up to 1024 of them), or, with
+ * on = 0, are computed in every primitive quartet (no counterpart in the
+ * reference; the same integrals to rounding).  Default on; on = 1 for a basis
+ * without a table gives RCHEM_ERR_UNSUPPORTED.  The FP64 and emulated-FP64
+ * kernels of the Fock build and the gradient read it; the FP32 ones compute.
+ */
+int rchem_set_exponent_table(rchem_basis b, int on);
+
 /* build_I (src/basis.rs:430-460): the dense n^4 ERI tensor I[m][n][l][s]. */
 int rchem_build_I(rchem_basis b, double *I, int where);
 /* JK_inmem (src/basis.rs:462-484): J and K from a dense tensor. */

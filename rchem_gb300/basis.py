@@ -143,6 +143,12 @@ class Basis:
         primitive quartets per lane, 0 = the warp-cooperative kernel."""
         _lib.check(_lib.lib().rchem_set_tile_shape(self.handle, cls, prec, ppl))
 
+    def set_exponent_table(self, on: bool):
+        """Read the primitive quartets' (p, q) factors from the exponent table
+        (default) or compute them in every primitive quartet
+        (rchem_set_exponent_table)."""
+        _lib.check(_lib.lib().rchem_set_exponent_table(self.handle, 1 if on else 0))
+
     def class_stats(self) -> list:
         """Per integral class of the current work plan: (l_a,l_b,l_c,l_d) with the
         FP64 / FP32 shell quartets, primitive quartets and algorithmic FLOPs."""

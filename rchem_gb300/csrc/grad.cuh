@@ -19,6 +19,7 @@
 #include "boys.cuh"
 #include "df64.cuh"
 #include "md.cuh"
+#include "pq_table.cuh"
 #include "rchem_types.h"
 
 #define GR_NI 4    // powers 0..3 per centre and direction (l <= 2, shifted by one)
@@ -41,6 +42,10 @@ struct GradArgs {
     const double *boys64;
     const double *D;
     double *grad;  // 3 * natoms
+    int npq;       // exponent-pair factor table (EriArgs::npq and the three after it)
+    const int *prim_eid;
+    const double2 *pq64;
+    const float4 *pqdf;
 };
 
 // E[i][j][t] of x_A^i x_B^j for i <= imax, j <= jmax (no exponential factor)
@@ -286,7 +291,8 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
             a2 = aa + aa;
             b2 = (p - aa) + (p - aa);
             c2 = ac + ac;
-            const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+            R rs, ipq, rho, qi, pi;
+            pq_factors<R>(g, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi, pi);
             const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
             const R T = rho * (X * X + Y * Y + Zc * Zc);
             boys_eval_rt<R>(L1, T, Kab * Kcd * rs, btab, F);
@@ -515,7 +521,8 @@ __global__ void __launch_bounds__(32 * GW_WARPS) k_grad2e_wc(GradArgs g) {
         GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
         GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
         const R a2 = aa + aa, b2 = (p - aa) + (p - aa), c2 = ac + ac;
-        const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+        R rs, ipq, rho, qi, pi;
+        pq_factors<R>(g, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi, pi);
         const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zq = Pc[2] - Qc[2];
         R F[GR_LMAX + 1];
         boys_eval_rt<R>(L1, rho * (X * X + Y * Y + Zq * Zq), Kab * Kcd * rs, btab, F);

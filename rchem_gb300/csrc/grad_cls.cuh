@@ -241,7 +241,10 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
         GradPrim<R>::get(g, bp.prim0 + ia, p, ohp, Pc, PA, Kab, aa);
         GradPrim<R>::get(g, kp.prim0 + ic, q, ohq, Qc, QC, Kcd, ac);
         const R ab = p - aa;
-        const R pq = p + q, rs = rchem_rsqrt(pq), ipq = rs * rs, rho = p * q * ipq;
+        R rs, ipq, rho, qi, pi;
+        // (pp|ps) and (pp|pp) compute the factors: with the table's loads in
+        // flight they spill several KB more per thread
+        pq_factors<R, !(LA == 1 && LB == 1 && LC == 1)>(g, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi, pi);
         const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
         const R T = rho * (X * X + Y * Y + Zc * Zc);
         R F[L1 + 1], Rt[nr(L1)];

@@ -363,7 +363,8 @@ struct rchem_basis_s {
     PairPrim32 *d_prims32 = nullptr;
     PairPrimDF *d_primsdf = nullptr;
     // factors of (p, q) by primitive-pair exponent number (EriArgs::pq64)
-    int npq = 0;
+    int npq = 0;          // 0: no table (more than kPqMax exponents)
+    bool pq_on = true;    // rchem_set_exponent_table
     int *d_prim_eid = nullptr;
     double2 *d_pq64 = nullptr;
     float4 *d_pqdf = nullptr;
@@ -452,6 +453,9 @@ static const double kPrimCut = 1e-22;  // drop primitive pairs with exp(-ab/p |A
 // below about kPrimRel times its angular factors, far under the 1e-12 targets)
 static const double kPrimRel = 1e-16;
 
+// distinct exponents of the table the kernels read (0: they compute the factors)
+static int pq_active(rchem_basis b) { return b->pq_on ? b->npq : 0; }
+
 static EriArgs base_args(rchem_basis b) {
     EriArgs a;
     memset(&a, 0, sizeof(a));
@@ -464,7 +468,7 @@ static EriArgs base_args(rchem_basis b) {
     a.boysdf = b->tabs->boysdf;
     a.primsdf = b->d_primsdf;
     a.Ddf = b->d_Ddf;
-    a.npq = b->npq;
+    a.npq = pq_active(b);
     a.prim_eid = b->d_prim_eid;
     a.pq64 = b->d_pq64;
     a.pqdf = b->d_pqdf;
@@ -551,7 +555,7 @@ static int compute_schwarz(rchem_basis b, std::vector<double> &Q) {
 // q/(p+q), p/(p+q) in FP64 and as double-float pairs.  A basis has few
 // distinct exponents (the exponent sums of its shells), so the table is small
 // and cache-resident; past kPqMax exponents the kernels compute the factors.
-static const int kPqMax = 512;
+static const int kPqMax = 1024;  // at most 64 MB of tables
 static int build_pq_table(rchem_basis b, const std::vector<PairPrim> &prims) {
     std::unordered_map<unsigned long long, int> num;
     std::vector<double> pv;
@@ -765,7 +769,7 @@ static const int kMinPrimPerLane = 16;
 // count, less p+q, 1/sqrt(p+q) (counted as 4), q/(p+q) and p/(p+q) where the
 // FP64 and double-float lists (prec 0) read them from the exponent table
 static double prim_flops(rchem_basis b, int k, int prec) {
-    return rchem_class_flops[k][0] - ((prec == 0 && b->npq > 0) ? 7.0 : 0.0);
+    return rchem_class_flops[k][0] - ((prec == 0 && pq_active(b) > 0) ? 7.0 : 0.0);
 }
 
 // Split the bra shell pairs of a build into nparts shares of about equal cost:
@@ -1571,6 +1575,10 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         g.boysdf = b->tabs->boysdf;
         g.D = b->d_D;
         g.grad = b->d_grad;
+        g.npq = pq_active(b);
+        g.prim_eid = b->d_prim_eid;
+        g.pq64 = b->d_pq64;
+        g.pqdf = b->d_pqdf;
         // classes run concurrently: longest first, each onto the least-loaded stream
         std::vector<int> ks;
         for (int k = 0; k < GRAD_NLIST; ++k)
@@ -1651,6 +1659,15 @@ extern "C" int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl) {
     b->wc[cls][prec] = ppl == 0;
     b->ppl[cls][prec] = ppl == 0 ? kMinPrimPerLane : ppl;
     b->planned = false;  // the next build replans with this shape
+    return RCHEM_OK;
+}
+
+extern "C" int rchem_set_exponent_table(rchem_basis b, int on) {
+    if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
+    if (on && b->npq == 0)
+        return set_err(RCHEM_ERR_UNSUPPORTED, "the basis has more than %d primitive-pair exponents: no table", kPqMax);
+    b->pq_on = on != 0;
+    b->planned = false;  // the next build replans and recaptures with the new setting
     return RCHEM_OK;
 }
 

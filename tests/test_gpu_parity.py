@@ -433,6 +433,48 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
             b.set_tile_shape(0, 0, 0)  # (ss|ss) has no warp-cooperative kernel
 
 
+def test_exponent_table_on_and_off_vs_oracle(gpu, oracle_mod):
+    """The (p, q) factors from the exponent table (default) and computed in
+    every primitive quartet: FP64 and emulated J/K, one-lane-group and
+    warp-cooperative kernels, both against the 8-fold oracle at 1e-12 and
+    against each other at 1e-13; the FP64 gradient both ways to 1e-11."""
+    import rchem_gb300 as rc
+
+    O = oracle_mod
+    name = "6-31gss-fit"
+    Z, R = rc.geometry.water_cluster(2, 4.5, seed=11)
+    ob = O.expand_basis(Z, R, rc.load_bse(name))
+    D = _sym_density(np.random.default_rng(2), ob.n)
+    W = _sym_density(np.random.default_rng(3), ob.n)
+    Jr, Kr = O.JK_sym(ob, D)
+    with rc.Basis(Z, R, name) as b:
+        n = b.nbf
+        out = {}
+        for wc in (False, True):
+            if wc:
+                for k, c in enumerate(b.class_stats()):
+                    if sum(c["class"]) >= 4:
+                        b.set_tile_shape(k, 0, 0)
+            for emulated in (False, True):
+                for on in (True, False):
+                    b.set_exponent_table(on)
+                    J, K = np.zeros((n, n)), np.zeros((n, n))
+                    rc.JK_direct(J, K, b, D, schwarz_tau=0.0, emulated=emulated)
+                    assert np.abs(J - Jr).max() < 1e-12 and np.abs(K - Kr).max() < 1e-12, (wc, emulated, on)
+                    out[on] = (J, K)
+                assert np.abs(out[True][0] - out[False][0]).max() < 1e-13
+                assert np.abs(out[True][1] - out[False][1]).max() < 1e-13
+        import torch
+
+        res = {"D": torch.from_numpy(D).cuda(), "W": torch.from_numpy(W).cuda()}
+        grads = []
+        for on in (True, False):
+            b.set_exponent_table(on)
+            grads.append(rc.scf.gradient(b, res).cpu().numpy())
+        assert np.abs(grads[0] - grads[1]).max() < 1e-11
+        b.set_exponent_table(True)
+
+
 @pytest.mark.parametrize("name", ["6-31gs-fit", "6-31gss-fit"])
 def test_build_I_and_jk_inmem_d_shells_vs_oracle(gpu, oracle_mod, name):
     """The dense ERI tensor (ERI-store epilogue of all 21 classes, d on O and p
