@@ -88,6 +88,23 @@ __device__ __forceinline__ double widen(float x) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// v 2^k for the degeneracy weights of the J/K scatter (k = -3..1): the
+// exponent field is adjusted with integer operations, so the weights cost no
+// FP64 instruction.  Exact for normal v; zero, subnormals (below 2.2e-308,
+// never a J/K contribution), infinities and NaN are returned unchanged, and a
+// result below the normal range is flushed to zero.
+__device__ __forceinline__ double scale_pow2(double v, int k) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((u >> 52) & 0x7ff), f = e + k;
+    if (e == 0 || e == 0x7ff) return v;
+    if (f <= 0) return 0.0;
+    return __longlong_as_double((long long)((u & ~(0x7ffULL << 52)) | ((unsigned long long)f << 52)));
+}
+// one weighted J/K contribution s 2^k as the FP64 atomic's operand: FP32 scales
+// on its own (wide) pipe, FP64 and double-float by the exponent field
+__device__ __forceinline__ double jk_term(double s, int k) { return scale_pow2(s, k); }
+__device__ __forceinline__ double jk_term(float s, int k) { return widen(s * __int_as_float((127 + k) << 23)); }
+
 template <> struct PrimLoad<df64> {
     static __device__ __forceinline__ void get(const EriArgs &a, int idx, df64 &p, df64 &ohp, df64 *P, df64 *PA,
                                                df64 &K) {
@@ -102,6 +119,7 @@ template <> struct PrimLoad<df64> {
 
 // double-float to double: both words widened exactly, one FP64 add per atomic
 __device__ __forceinline__ double widen(df64 x) { return widen(x.hi) + widen(x.lo); }
+__device__ __forceinline__ double jk_term(df64 s, int k) { return scale_pow2(widen(s), k); }
 
 template <typename R> struct Tabs;
 template <> struct Tabs<double> {
@@ -255,11 +273,8 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
     }
 
     // ---- EPI_JK: degeneracy-weighted 8-fold scatter -------------------------
-    R deg = R(1);
-    if (bp.diag) deg *= R(0.5);
-    if (kp.diag) deg *= R(0.5);
-    if (bidx == kidx) deg *= R(0.5);
-    const R deg2 = deg + deg;  // J carries the factor 2
+    // weight 2^kK (1/2 per diagonal pair and for bra = ket); J carries a factor 2
+    const int kK = -(bp.diag + kp.diag + (bidx == kidx ? 1 : 0)), kJ = kK + 1;
 
     if (!lead) return;
     // J-hat bra block: 2 (ab|cd) D_cd
@@ -278,7 +293,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dcd[ic * ND + id];
-                atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, widen(s * deg2));
+                atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, jk_term(s, kJ));
             }
     }
     // J-hat ket block: 2 (ab|cd) D_ab
@@ -297,7 +312,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ib = 0; ib < NB; ++ib) s += out[IDX(ia, ib, ic, id)] * Dab[ia * NB + ib];
-                atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, widen(s * deg2));
+                atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, jk_term(s, kJ));
             }
     }
     // K-hat[a][c] += (ab|cd) D_bd
@@ -316,7 +331,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dbd[ib * ND + id];
-                atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, widen(s * deg));
+                atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, jk_term(s, kK));
             }
     }
     // K-hat[b][c] += (ab|cd) D_ad
@@ -335,7 +350,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int id = 0; id < ND; ++id) s += out[IDX(ia, ib, ic, id)] * Dad[ia * ND + id];
-                atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, widen(s * deg));
+                atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, jk_term(s, kK));
             }
     }
     // K-hat[a][d] += (ab|cd) D_bc
@@ -354,7 +369,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dbc[ib * NC + ic];
-                atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, widen(s * deg));
+                atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, jk_term(s, kK));
             }
     }
     // K-hat[b][d] += (ab|cd) D_ac
@@ -373,7 +388,7 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
                 for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                     for (int ic = 0; ic < NC; ++ic) s += out[IDX(ia, ib, ic, id)] * Dac[ia * NC + ic];
-                atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, widen(s * deg));
+                atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, jk_term(s, kK));
             }
     }
 #undef IDX
@@ -590,11 +605,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
     }
 
     // degeneracy-weighted 8-fold scatter, the lanes splitting each contraction
-    R deg = R(1);
-    if (bp.diag) deg *= R(0.5);
-    if (kp.diag) deg *= R(0.5);
-    if (bidx == kidx) deg *= R(0.5);
-    const R deg2 = deg + deg;
+    const int kK = -(bp.diag + kp.diag + (bidx == kidx ? 1 : 0)), kJ = kK + 1;
     const int n = bp.mn, mo = bp.moff;
     const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
 #define WIDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
@@ -604,7 +615,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ic = 0; ic < NC; ++ic)
             for (int id = 0; id < ND; ++id)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id), sum);
-        atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, widen(sum * deg2));
+        atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, jk_term(sum, kJ));
     }
     for (int t = lane; t < NC * ND; t += 32) {  // J-hat ket: 2 (ab|cd) D_ab
         const int ic = t / ND, id = t - ic * ND;
@@ -612,7 +623,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ia = 0; ia < NA; ++ia)
             for (int ib = 0; ib < NB; ++ib)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib), sum);
-        atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, widen(sum * deg2));
+        atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, jk_term(sum, kJ));
     }
     for (int t = lane; t < NA * NC; t += 32) {  // K-hat[a][c] += (ab|cd) D_bd
         const int ia = t / NC, ic = t - ia * NC;
@@ -620,7 +631,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ib = 0; ib < NB; ++ib)
             for (int id = 0; id < ND; ++id)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id), sum);
-        atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, widen(sum * deg));
+        atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, jk_term(sum, kK));
     }
     for (int t = lane; t < NB * NC; t += 32) {  // K-hat[b][c] += (ab|cd) D_ad
         const int ib = t / NC, ic = t - ib * NC;
@@ -628,7 +639,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ia = 0; ia < NA; ++ia)
             for (int id = 0; id < ND; ++id)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id), sum);
-        atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, widen(sum * deg));
+        atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, jk_term(sum, kK));
     }
     for (int t = lane; t < NA * ND; t += 32) {  // K-hat[a][d] += (ab|cd) D_bc
         const int ia = t / ND, id = t - ia * ND;
@@ -636,7 +647,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ib = 0; ib < NB; ++ib)
             for (int ic = 0; ic < NC; ++ic)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic), sum);
-        atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, widen(sum * deg));
+        atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, jk_term(sum, kK));
     }
     for (int t = lane; t < NB * ND; t += 32) {  // K-hat[b][d] += (ab|cd) D_ac
         const int ib = t / ND, id = t - ib * ND;
@@ -644,7 +655,7 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         for (int ia = 0; ia < NA; ++ia)
             for (int ic = 0; ic < NC; ++ic)
                 sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic), sum);
-        atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, widen(sum * deg));
+        atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, jk_term(sum, kK));
     }
 #undef WIDX
 }
