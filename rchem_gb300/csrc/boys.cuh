@@ -2,12 +2,16 @@
 //
 // The reference evaluates F_m with a Numerical-Recipes incomplete gamma
 // function (libpyquante2/cints.c:302-373, relative error ~1e-7).  Here:
-//   T < BOYS_TMAX: Taylor expansion about the nearest grid point T_i = i*h,
-//     F_m(T_i + d) = sum_k F_{m+k}(T_i) (-d)^k / k!,  |d| <= h/2,
-//     with NTAY terms (6 in FP64: remainder < 3e-16 F; 4 in FP32: < 2e-10 F).
-//     The tables hold the coefficients already divided by k!, one sub-table per
-//     m (and one for e^{-T} = e^{-T_i} e^{-d}), so an evaluation is a pure
-//     Horner chain in x = -d: NTAY-1 fused multiply-adds.  Small L evaluates
+//   T < BOYS_TMAX: a polynomial in x = T_i - T about the nearest grid point
+//     T_i = i*h, from the Taylor expansion
+//     F_m(T_i + d) = sum_k F_{m+k}(T_i) (-d)^k / k!,  |d| <= h/2:
+//     FP64 (h = 1/128): the 7-term expansion economized to 5 coefficients on
+//     |x| <= h/2 (Chebyshev economization: x^6 and x^5 replaced by their
+//     best lower-degree approximations, error <= (a_5 + a_6 h/2) (h/2)^5 / 16
+//     ~ 5e-16 F); FP32 (h = 1/64): 4 Taylor terms (< 2e-10 F).
+//     The tables hold the coefficients, one sub-table per m (and one for
+//     e^{-T} = e^{-T_i} e^{-d}), so an evaluation is a pure Horner chain in x:
+//     NTAY-1 fused multiply-adds.  Small L evaluates
 //     every F_m that way ("direct"); larger L evaluates F_L and e^{-T} and runs
 //     the downward recursion F_m = (2T F_{m+1} + e^{-T}) / (2m+1).
 //   T >= BOYS_TMAX: F_0 = sqrt(pi/T)/2 (erfc(sqrt T) < 4e-19 there) and the
@@ -21,21 +25,26 @@
 
 #include "rchem_types.h"
 
-// h = 1/64 is exact in binary, so T_i = i*h and d = T - T_i are exact in both
-// precisions and the host tables are built at exactly the device's grid points.
-// With |d| <= h/2 the Taylor remainder after NT terms is below
-// F_m (h/2)^NT / NT!: 3e-16 relative for the 6 FP64 terms, 2e-10 for the 4 FP32 ones.
-#define BOYS_NGRID 2561  // rows i = 0..2560 (nearest-point rounding reaches 2560 just below T = 40)
+// h = 1/128 (FP64) and 1/64 (FP32) are exact in binary, so T_i = i*h and
+// T_i - T are exact and the host tables are built at exactly the device's grid
+// points.  Rows i = 0..TMAX/h (nearest-point rounding reaches the last one just
+// below T = 40).
 #define BOYS_MMAX 16     // F_0 .. F_16
 #define BOYS_NSUB (BOYS_MMAX + 2)  // sub-table 0 = e^{-T}, sub-table m+1 = F_m
 #define BOYS_TMAX 40.0
-#define BOYS_INVH 64.0
-#define BOYS_H 0.015625
-#define BOYS_NT64 6
+#define BOYS_NGRID64 5121
+#define BOYS_INVH64 128.0
+#define BOYS_H64 0.0078125
+#define BOYS_NT64 5
+#define BOYS_NGRID32 2561
+#define BOYS_INVH32 64.0
+#define BOYS_H32 0.015625
 #define BOYS_NT32 4
 
-template <typename R> struct BoysPrec { static constexpr int NTAY = BOYS_NT64; };  // double, double-float
-template <> struct BoysPrec<float> { static constexpr int NTAY = BOYS_NT32; };
+template <typename R> struct BoysPrec {  // double, double-float
+    static constexpr int NTAY = BOYS_NT64, NGRID = BOYS_NGRID64;
+};
+template <> struct BoysPrec<float> { static constexpr int NTAY = BOYS_NT32, NGRID = BOYS_NGRID32; };
 
 // 1/k for a small integer k, as a compile-time constant of type R
 template <typename R> RCHEM_HD constexpr R rchem_recip(int k) { return R(1.0 / (double)k); }
@@ -56,8 +65,8 @@ RCHEM_HD inline bool rchem_lt(float a, float b) { return a < b; }
 RCHEM_HD inline float rchem_tofloat(double a) { return (float)a; }
 RCHEM_HD inline float rchem_tofloat(float a) { return a; }
 
-// table element (sub-table s, grid row i, Taylor order k)
-RCHEM_HD inline int boys_idx(int s, int i, int k, int nt) { return (s * BOYS_NGRID + i) * nt + k; }
+// table element (sub-table s, grid row i, coefficient k) of a table of ngrid rows
+RCHEM_HD inline int boys_idx(int s, int i, int k, int nt, int ngrid) { return (s * ngrid + i) * nt + k; }
 
 RCHEM_HD inline double rchem_rsqrt(double x) {
 #ifdef __CUDA_ARCH__
@@ -90,37 +99,37 @@ RCHEM_HD inline R rchem_ldg(const R *p) {
 #endif
 }
 
-// nearest grid row i and x = T_i - T, for 0 <= T < BOYS_TMAX.  On the device
-// the row comes from T's bits with integer operations (T = m 2^(e-52), so
-// T/h = m 2^(e-46), rounded half up) and T_i = i h is assembled as a double
+// nearest FP64 grid row i and x = T_i - T, for 0 <= T < BOYS_TMAX.  On the
+// device the row comes from T's bits with integer operations (T = m 2^(e-52),
+// so T/h = m 2^(e-45), rounded half up) and T_i = i h is assembled as a double
 // from i's bits, leaving one FP64 subtraction; the host rounds with the
 // 2^52 + 2^51 addition.  Either rounding keeps |x| <= h/2.
 RCHEM_HD inline void boys_grid(double T, int &i, double &x) {
 #ifdef __CUDA_ARCH__
     const long long bits = __double_as_longlong(T);
     const int e = (int)((bits >> 52) & 0x7ff) - 1023;  // T < 40: e <= 5
-    const int sh = 46 - e;                              // >= 41
+    const int sh = 45 - e;                              // >= 40
     const long long m = (bits & 0xfffffffffffffLL) | 0x10000000000000LL;
     i = (e < -1022 || sh >= 63) ? 0 : (int)((m + (1LL << (sh - 1))) >> sh);
     double Ti = 0.0;
     if (i > 0) {
-        const int msb = 31 - __clz(i);  // i h = i 2^-6: exponent msb - 6, mantissa i's lower bits
-        Ti = __longlong_as_double(((long long)(msb - 6 + 1023) << 52) |
+        const int msb = 31 - __clz(i);  // i h = i 2^-7: exponent msb - 7, mantissa i's lower bits
+        Ti = __longlong_as_double(((long long)(msb - 7 + 1023) << 52) |
                                   (((long long)i << (52 - msb)) & 0xfffffffffffffLL));
     }
     x = Ti - T;
 #else
     const double magic = 6755399441055744.0;  // 2^52 + 2^51
-    const double t = fma(T, BOYS_INVH, magic);
+    const double t = fma(T, BOYS_INVH64, magic);
     long long bits;
     memcpy(&bits, &t, sizeof(bits));
     i = (int)(bits & 0xffffffffLL);
-    x = fma(t - magic, BOYS_H, -T);
+    x = fma(t - magic, BOYS_H64, -T);
 #endif
 }
 RCHEM_HD inline void boys_grid(float T, int &i, float &x) {
     const float magic = 12582912.0f;  // 2^23 + 2^22
-    const float t = fmaf(T, (float)BOYS_INVH, magic);
+    const float t = fmaf(T, (float)BOYS_INVH32, magic);
 #ifdef __CUDA_ARCH__
     i = __float_as_int(t) - __float_as_int(magic);
 #else
@@ -129,13 +138,13 @@ RCHEM_HD inline void boys_grid(float T, int &i, float &x) {
     memcpy(&mb, &magic, sizeof(mb));
     i = bits - mb;
 #endif
-    x = fmaf(t - magic, (float)BOYS_H, -T);
+    x = fmaf(t - magic, (float)BOYS_H32, -T);
 }
 
 template <typename R>
 RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
     constexpr int NT = BoysPrec<R>::NTAY;
-    const R *c = tab + boys_idx(s, i, 0, NT);
+    const R *c = tab + boys_idx(s, i, 0, NT, BoysPrec<R>::NGRID);
     R acc = rchem_ldg(c + NT - 1);
 #pragma unroll
     for (int k = NT - 2; k >= 0; --k) acc = rchem_fma(acc, x, rchem_ldg(c + k));
@@ -197,34 +206,66 @@ RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab,
     }
 }
 
-// Host: fill the FP64 and FP32 tables (sizes boys_table_size(nt)).
-inline size_t boys_table_size(int nt) { return (size_t)BOYS_NSUB * BOYS_NGRID * nt; }
+// Host: fill the FP64 and FP32 tables (sizes boys_table_size(nt, ngrid)).
+inline size_t boys_table_size(int nt, int ngrid) { return (size_t)BOYS_NSUB * ngrid * nt; }
 
-inline double boys_series_host(int m, double x) {
-    // F_m(x) = e^{-x} sum_k (2x)^k / prod_{i=0..k} (2m+2i+1): every term positive
-    double term = 1.0 / (2 * m + 1), sum = term;
-    for (int k = 1; k < 2000; ++k) {
-        term *= 2.0 * x / (2 * m + 2 * k + 1);
+// F_0..F_mtop at x (host, long double: a 64- or 113-bit significand, so the
+// tables carry each F_m rounded once to double): F_mtop from its series
+// e^{-x} sum_k (2x)^k / prod_{i=0..k} (2m+2i+1) (every term positive), the
+// rest by the stable downward recursion F_m = (2x F_{m+1} + e^{-x}) / (2m+1).
+inline void boys_row_host(double x, int mtop, double *F) {
+    long double term = 1.0L / (2 * mtop + 1), sum = term;
+    const long double x2 = 2.0L * x, ex = expl(-(long double)x);
+    for (int k = 1; k < 4000; ++k) {
+        term *= x2 / (2 * mtop + 2 * k + 1);
         sum += term;
-        if (term < sum * 1e-18) break;
+        if (term < sum * 1e-24L) break;
     }
-    return exp(-x) * sum;
+    long double f = ex * sum;
+    F[mtop] = (double)f;
+    for (int m = mtop - 1; m >= 0; --m) {
+        f = (x2 * f + ex) / (2 * m + 1);
+        F[m] = (double)f;
+    }
 }
-
+// FP64: a_k = F_{m+k}(T_i) / k! for k = 0..6 economized on |x| <= d = h/2
+// (u = x/d; u^5 -> (20 u^3 - 5 u)/16, u^6 -> (48 u^4 - 18 u^2 + 1)/32, the
+// Chebyshev polynomials T_5 and T_6 dropped); FP32: a_0..a_3.
+inline void boys_econ5(const double *a, double *b) {
+    const double d2 = 0.25 * BOYS_H64 * BOYS_H64, d4 = d2 * d2, d6 = d4 * d2;
+    b[0] = a[0] + d6 / 32.0 * a[6];
+    b[1] = a[1] - 5.0 / 16.0 * d4 * a[5];
+    b[2] = a[2] - 9.0 / 16.0 * d4 * a[6];
+    b[3] = a[3] + 5.0 / 4.0 * d2 * a[5];
+    b[4] = a[4] + 3.0 / 2.0 * d2 * a[6];
+}
 inline void boys_fill_tables(double *t64, float *t32) {
     double fk[32];
     fk[0] = 1.0;
     for (int k = 1; k < 32; ++k) fk[k] = fk[k - 1] * k;
-    for (int i = 0; i < BOYS_NGRID; ++i) {
-        const double T = (double)i * BOYS_H;  // exact: h = 1/64
-        double F[BOYS_MMAX + BOYS_NT64 + 1];
-        for (int m = 0; m <= BOYS_MMAX + BOYS_NT64; ++m) F[m] = boys_series_host(m, T);
-        const double e = exp(-T);
-        for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(0, i, k, BOYS_NT64)] = e / fk[k];
-        for (int k = 0; k < BOYS_NT32; ++k) t32[boys_idx(0, i, k, BOYS_NT32)] = (float)(e / fk[k]);
+    constexpr int NA = 7;  // Taylor terms before the economization
+    for (int i = 0; i < BOYS_NGRID64; ++i) {
+        const double T = (double)i * BOYS_H64;  // exact
+        double F[BOYS_MMAX + NA + 1], a[NA], b[BOYS_NT64];
+        boys_row_host(T, BOYS_MMAX + NA, F);
+        const double e = (double)expl(-(long double)T);
+        for (int k = 0; k < NA; ++k) a[k] = e / fk[k];
+        boys_econ5(a, b);
+        for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(0, i, k, BOYS_NT64, BOYS_NGRID64)] = b[k];
         for (int m = 0; m <= BOYS_MMAX; ++m) {
-            for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(m + 1, i, k, BOYS_NT64)] = F[m + k] / fk[k];
-            for (int k = 0; k < BOYS_NT32; ++k) t32[boys_idx(m + 1, i, k, BOYS_NT32)] = (float)(F[m + k] / fk[k]);
+            for (int k = 0; k < NA; ++k) a[k] = F[m + k] / fk[k];
+            boys_econ5(a, b);
+            for (int k = 0; k < BOYS_NT64; ++k) t64[boys_idx(m + 1, i, k, BOYS_NT64, BOYS_NGRID64)] = b[k];
         }
+    }
+    for (int i = 0; i < BOYS_NGRID32; ++i) {
+        const double T = (double)i * BOYS_H32;
+        double F[BOYS_MMAX + BOYS_NT32 + 1];
+        boys_row_host(T, BOYS_MMAX + BOYS_NT32, F);
+        const double e = exp(-T);
+        for (int k = 0; k < BOYS_NT32; ++k) t32[boys_idx(0, i, k, BOYS_NT32, BOYS_NGRID32)] = (float)(e / fk[k]);
+        for (int m = 0; m <= BOYS_MMAX; ++m)
+            for (int k = 0; k < BOYS_NT32; ++k)
+                t32[boys_idx(m + 1, i, k, BOYS_NT32, BOYS_NGRID32)] = (float)(F[m + k] / fk[k]);
     }
 }

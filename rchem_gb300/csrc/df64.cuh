@@ -90,9 +90,9 @@ __device__ __forceinline__ df64 rchem_ldg(const df64 *p) {
 // than an ulp of T, far inside the Taylor radius); x = T_i - T exactly in df64
 __device__ __forceinline__ void boys_grid(df64 T, int &i, df64 &x) {
     const float magic = 12582912.0f;  // 2^23 + 2^22
-    const float t = fmaf(T.hi, (float)BOYS_INVH, magic);
+    const float t = fmaf(T.hi, (float)BOYS_INVH64, magic);
     i = __float_as_int(t) - __float_as_int(magic);
-    x = df64((t - magic) * (float)BOYS_H, 0.f) - T;
+    x = df64((t - magic) * (float)BOYS_H64, 0.f) - T;
 }
 __device__ __forceinline__ df64 __shfl_xor_sync(unsigned mask, df64 v, int lane) {
     return df64(__shfl_xor_sync(mask, v.hi, lane), __shfl_xor_sync(mask, v.lo, lane));

@@ -113,8 +113,8 @@ static int get_tables(const DevTables **out) {
     std::lock_guard<std::mutex> lk(g_tab_mu);
     DevTables &t = g_tabs[dev];
     if (!t.boys64) {
-        std::vector<double> b64(boys_table_size(BOYS_NT64));
-        std::vector<float> b32(boys_table_size(BOYS_NT32));
+        std::vector<double> b64(boys_table_size(BOYS_NT64, BOYS_NGRID64));
+        std::vector<float> b32(boys_table_size(BOYS_NT32, BOYS_NGRID32));
         boys_fill_tables(b64.data(), b32.data());
         std::vector<float2> bdf(b64.size());
         for (size_t i = 0; i < b64.size(); ++i) {

@@ -31,8 +31,8 @@ static std::vector<float> g_b32;
 
 static void init_tables() {
     if (!g_b64.empty()) return;
-    g_b64.resize(boys_table_size(BOYS_NT64));
-    g_b32.resize(boys_table_size(BOYS_NT32));
+    g_b64.resize(boys_table_size(BOYS_NT64, BOYS_NGRID64));
+    g_b32.resize(boys_table_size(BOYS_NT32, BOYS_NGRID32));
     boys_fill_tables(g_b64.data(), g_b32.data());
 }
 
