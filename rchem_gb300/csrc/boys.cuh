@@ -32,10 +32,22 @@
 #define BOYS_MMAX 16     // F_0 .. F_16
 #define BOYS_NSUB (BOYS_MMAX + 2)  // sub-table 0 = e^{-T}, sub-table m+1 = F_m
 #define BOYS_TMAX 40.0
-#define BOYS_NGRID64 5121
+#define BOYS_NGRID64 10241  // T < 80: the branch-free evaluation (boys_eval_u) uses rows past T = 40
 #define BOYS_INVH64 128.0
 #define BOYS_H64 0.0078125
 #define BOYS_NT64 5
+// Power-law table of boys_eval_u for T beyond the Taylor range: F_m(T) =
+// Gamma(m+1/2)/2 T^-(m+1/2) (the e^{-T} terms are below 1e-17 of F_m for m <= 1
+// at T >= 40 and for m <= 8 at T >= 80).  T = 2^(2k+par) v with v in [1, 2];
+// sub-table (par, m) holds, at v_j = 1 + j/BOYS_FAR_R, 5 coefficients of
+// Gamma(m+1/2)/2 2^-(par (m+1/2)) v^-(m+1/2) in x = v_j - v (7 Taylor terms
+// economized on |x| <= 1/(2 BOYS_FAR_R)); the factor 2^-(k (2m+1)) goes on
+// by the exponent field.  A row of zeros (the far e^{-T}) follows the rows.
+#define BOYS_FAR_R 2048
+#define BOYS_FAR_ROWS (BOYS_FAR_R + 1)
+#define BOYS_FAR_M 9  // m = 0..8 (the class kernels' L <= 8)
+#define BOYS_FAR_ZERO (2 * BOYS_FAR_M * BOYS_FAR_ROWS * BOYS_NT64)
+#define BOYS_FAR_SIZE (BOYS_FAR_ZERO + BOYS_NT64)
 #define BOYS_NGRID32 2561
 #define BOYS_INVH32 64.0
 #define BOYS_H32 0.015625
@@ -189,6 +201,76 @@ RCHEM_HD inline void boys_eval(R T, R pref, const R *__restrict__ tab, R *F) {
     }
 }
 
+#ifdef __CUDACC__
+// v 2^k by the exponent field (integer operations; k = 0 leaves v as it is):
+// zero, subnormals, infinities and NaN unchanged, results below the normal
+// range flushed to zero.
+__device__ __forceinline__ double boys_ldexp(double v, int k) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((u >> 52) & 0x7ff), f = e + k;
+    if (e == 0 || e == 0x7ff) return v;
+    if (f <= 0) return 0.0;
+    return __longlong_as_double((long long)((u & ~(0x7ffULL << 52)) | ((unsigned long long)f << 52)));
+}
+
+template <int NT>
+__device__ __forceinline__ double boys_horner_at(const double *__restrict__ c, double x) {
+    double acc = __ldg(c + NT - 1);
+#pragma unroll
+    for (int k = NT - 2; k >= 0; --k) acc = fma(acc, x, __ldg(c + k));
+    return acc;
+}
+
+// F[0..L] (times pref with SCALE) in FP64 for the class kernels, with one FP64
+// instruction stream for every T: below the switch point (40 for L <= 1, 80
+// above) a row of the Taylor table at T_i = i/128, above it a row of the
+// power-law table at v_j, T = 2^(2k+par) v; the row, its grid point and the
+// argument are chosen with integer operations, so the lanes of a warp with T
+// on either side run the same x = grid - argument, the same Horner chains and,
+// for L >= 2, the same downward recursion (e^{-T} from the zero row above the
+// switch), instead of both branches of boys_eval.
+template <int L, bool SCALE>
+__device__ __forceinline__ void boys_eval_u(double T, double pref, const double *__restrict__ tab,
+                                            const double *__restrict__ far, double *F) {
+    constexpr int NT = BOYS_NT64, NG = BOYS_NGRID64;
+    const long long bits = __double_as_longlong(T);
+    const bool nr = bits < (L <= 1 ? 0x4044000000000000LL : 0x4054000000000000LL);  // T < 40 / T < 80
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    const long long man = bits & 0xfffffffffffffLL;
+    // Taylor row: i = T 128 rounded half up (clamped, so far lanes hold an unused valid row)
+    int sh = 45 - e;
+    sh = sh < 1 ? 1 : sh;
+    int i = (e < -1022 || sh >= 63) ? 0 : (int)min((long long)(NG - 1), ((man | (1LL << 52)) + (1LL << (sh - 1))) >> sh);
+    long long gb_near = 0;
+    if (i > 0) {
+        const int msb = 31 - __clz(i);  // i/128: exponent msb - 7, mantissa i's lower bits
+        gb_near = ((long long)(msb - 7 + 1023) << 52) | (((long long)i << (52 - msb)) & 0xfffffffffffffLL);
+    }
+    // power-law row: v = T 2^-e in [1, 2), j = (v - 1) BOYS_FAR_R rounded, v_j = 1 + j/BOYS_FAR_R
+    // (j = BOYS_FAR_R carries into the exponent: v_j = 2)
+    const int par = e & 1, k = e >> 1;
+    const int j = (int)((man + (1LL << 40)) >> 41);
+    const long long gb_far = (1023LL << 52) + ((long long)j << 41);
+    const long long ab_far = man | (1023LL << 52);
+    const double x = __longlong_as_double(nr ? gb_near : gb_far) - __longlong_as_double(nr ? bits : ab_far);
+    auto row = [&](int m) {  // F_m's row (m <= L)
+        return nr ? tab + boys_idx(m + 1, i, 0, NT, NG) : far + ((par * BOYS_FAR_M + m) * BOYS_FAR_ROWS + j) * NT;
+    };
+    auto sc = [&](double v) { return SCALE ? v * pref : v; };
+    if (L <= BOYS_DIRECT_MAXL) {
+#pragma unroll
+        for (int m = 0; m <= L; ++m) F[m] = sc(boys_ldexp(boys_horner_at<NT>(row(m), x), nr ? 0 : -k * (2 * m + 1)));
+    } else {
+        const double *pex = nr ? tab + boys_idx(0, i, 0, NT, NG) : far + BOYS_FAR_ZERO;
+        const double ex = sc(boys_horner_at<NT>(pex, x));
+        F[L] = sc(boys_ldexp(boys_horner_at<NT>(row(L), x), nr ? 0 : -k * (2 * L + 1)));
+        const double T2 = T + T;
+#pragma unroll
+        for (int m = L - 1; m >= 0; --m) F[m] = fma(T2, F[m + 1], ex) * rchem_recip<double>(2 * m + 1);
+    }
+}
+#endif
+
 // Runtime-L variant for the generic (non-class) kernels; L <= BOYS_MMAX.
 template <typename R>
 RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab, R *F) {
@@ -239,6 +321,34 @@ inline void boys_econ5(const double *a, double *b) {
     b[3] = a[3] + 5.0 / 4.0 * d2 * a[5];
     b[4] = a[4] + 3.0 / 2.0 * d2 * a[6];
 }
+// The power-law table (BOYS_FAR_SIZE doubles), coefficients in long double.
+inline void boys_fill_far(double *far) {
+    const long double d = 0.5L / BOYS_FAR_R, d2 = d * d, d4 = d2 * d2, d6 = d4 * d2;
+    long double g_half = sqrtl(3.14159265358979323846264338327950288L);  // Gamma(1/2)
+    for (int m = 0; m < BOYS_FAR_M; ++m) {
+        const long double al = m + 0.5L, C0 = g_half / 2;  // Gamma(m+1/2)/2
+        for (int par = 0; par < 2; ++par) {
+            const long double C = par ? C0 * powl(2.0L, -al) : C0;
+            for (int j = 0; j < BOYS_FAR_ROWS; ++j) {
+                const long double g = 1.0L + (long double)j / BOYS_FAR_R;
+                long double a[7], rf = 1.0L, fk = 1.0L;
+                for (int q = 0; q < 7; ++q) {
+                    a[q] = C * rf * powl(g, -al - q) / fk;  // C (al)_q g^-(al+q) / q!
+                    rf *= al + q;
+                    fk *= q + 1;
+                }
+                const long double b[5] = {a[0] + d6 / 32 * a[6], a[1] - 5.0L / 16 * d4 * a[5],
+                                          a[2] - 9.0L / 16 * d4 * a[6], a[3] + 5.0L / 4 * d2 * a[5],
+                                          a[4] + 3.0L / 2 * d2 * a[6]};
+                for (int q = 0; q < BOYS_NT64; ++q)
+                    far[((par * BOYS_FAR_M + m) * BOYS_FAR_ROWS + j) * BOYS_NT64 + q] = (double)b[q];
+            }
+        }
+        g_half *= al;  // Gamma(m+3/2) = (m+1/2) Gamma(m+1/2)
+    }
+    for (int q = 0; q < BOYS_NT64; ++q) far[BOYS_FAR_ZERO + q] = 0.0;
+}
+
 inline void boys_fill_tables(double *t64, float *t32) {
     double fk[32];
     fk[0] = 1.0;

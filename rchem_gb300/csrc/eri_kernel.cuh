@@ -159,7 +159,11 @@ __device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R 
             return;
         }
     }
-    boys_eval<L, R, SCALE>(T, pref, btab, F);
+    if constexpr (std::is_same<R, double>::value && L <= BOYS_FAR_M - 1) {
+        boys_eval_u<L, SCALE>(T, pref, btab, a.boysfar, F);  // one FP64 instruction stream for every T
+    } else {
+        boys_eval<L, R, SCALE>(T, pref, btab, F);
+    }
 }
 
 

@@ -100,6 +100,7 @@ extern "C" int rchem_abi_version(void) { return 1; }
 // ---------------------------------------------------------------------------
 struct DevTables {
     double *boys64 = nullptr;
+    double *boysfar = nullptr;  // power-law table of the branch-free FP64 evaluation
     float *boys32 = nullptr;
     float2 *boysdf = nullptr;  // the FP64 table split into (hi, lo) float pairs
 };
@@ -116,6 +117,8 @@ static int get_tables(const DevTables **out) {
         std::vector<double> b64(boys_table_size(BOYS_NT64, BOYS_NGRID64));
         std::vector<float> b32(boys_table_size(BOYS_NT32, BOYS_NGRID32));
         boys_fill_tables(b64.data(), b32.data());
+        std::vector<double> bfar(BOYS_FAR_SIZE);
+        boys_fill_far(bfar.data());
         std::vector<float2> bdf(b64.size());
         for (size_t i = 0; i < b64.size(); ++i) {
             const float hi = (float)b64[i];
@@ -129,10 +132,13 @@ static int get_tables(const DevTables **out) {
         CudaFreeGuard g32(n.boys32);
         CK(cudaMalloc(&n.boysdf, bdf.size() * sizeof(float2)));
         CudaFreeGuard gdf(n.boysdf);
+        CK(cudaMalloc(&n.boysfar, bfar.size() * sizeof(double)));
+        CudaFreeGuard gfar(n.boysfar);
         CK(cudaMemcpy(n.boys64, b64.data(), b64.size() * sizeof(double), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boys32, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(n.boysdf, bdf.data(), bdf.size() * sizeof(float2), cudaMemcpyHostToDevice));
-        g64.p = g32.p = gdf.p = nullptr;  // kept for the life of the process
+        CK(cudaMemcpy(n.boysfar, bfar.data(), bfar.size() * sizeof(double), cudaMemcpyHostToDevice));
+        g64.p = g32.p = gdf.p = gfar.p = nullptr;  // kept for the life of the process
         t = n;
     }
     *out = &t;
@@ -464,6 +470,7 @@ static EriArgs base_args(rchem_basis b) {
     a.prims = b->d_prims;
     a.prims32 = b->d_prims32;
     a.boys64 = b->tabs->boys64;
+    a.boysfar = b->tabs->boysfar;
     a.boys32 = b->tabs->boys32;
     a.boysdf = b->tabs->boysdf;
     a.primsdf = b->d_primsdf;

@@ -90,6 +90,7 @@ struct EriArgs {
     const PairPrim *prims;
     const PairPrim32 *prims32;
     const double *boys64;  // Boys Taylor tables (boys.cuh layout)
+    const double *boysfar; // and the FP64 power-law table beyond them (boys_eval_u)
     const float *boys32;
     const double *D;       // density, nbf x nbf row-major
     const float *D32;      // the same in single precision (mixed form)
