@@ -317,15 +317,99 @@ def best_hrr(la, lb, lc, ld, targets):
 # chain of NTAY-1 FMAs per evaluated function; every F_m for L <= 1, else F_L
 # and e^{-T} followed by the downward recursion (one FMA + one multiply per m);
 # the prefactor multiplies (L+1 or 2); the grid index (one FMA + one add + one FMA).
-NTAY64 = 6
+NTAY64 = 5  # FP64 Boys table coefficients per row (boys.cuh)
 NTAY32 = 4
 
 
 def boys_ops(L, ntay=NTAY64):
-    """(fma, other) FP64 operations of one Boys evaluation."""
+    """(fma, other) FP64 operations of one Boys evaluation (boys_eval_u): x =
+    grid - argument, one Horner chain per F_m (L <= 1) or for F_L and e^{-T}
+    with the downward recursion (fma and a product per step, 2T once), and
+    the products by the prefactor."""
     if L <= 1:
-        return (ntay - 1) * (L + 1) + 2, (L + 1) + 1
-    return 2 * (ntay - 1) + L + 2, L + 2 + 1
+        return (ntay - 1) * (L + 1), 1 + (L + 1)
+    return 2 * (ntay - 1) + L, 1 + 2 + 1 + L
+
+
+def _split_args(s):
+    """Top-level comma-separated arguments of s."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    out.append(cur.strip())
+    return out
+
+
+def _count_expr(e, seen):
+    """(fma, other) of an emitted expression, each distinct subexpression once
+    (the compiler evaluates a repeated one once)."""
+    e = e.strip()
+    while e.startswith("(") and e.endswith(")") and _split_args(e[1:-1]) == [e[1:-1].strip()]:
+        e = e[1:-1].strip()
+    if e.startswith("-") and "*" not in e and "rchem_fma" not in e:
+        return 0, 0  # a negated operand: a sign modifier
+    if e.startswith("rchem_fma("):
+        f, o = (0, 0) if e in seen else (1, 0)
+        seen.add(e)
+        for a in _split_args(e[len("rchem_fma("):-1]):
+            df, do = _count_expr(a, seen)
+            f += df
+            o += do
+        return f, o
+    depth = 0
+    for i, ch in enumerate(e):
+        if ch in "([":
+            depth += 1
+        elif ch in ")]":
+            depth -= 1
+        elif ch == "*" and depth == 0:
+            if e[:i].strip().startswith("R(") and e in seen:
+                return 0, 0
+            f, o = (0, 0) if e in seen else (0, 1)
+            seen.add(e)
+            for part in (e[:i], e[i + 1:]):
+                df, do = _count_expr(part, seen)
+                f += df
+                o += do
+            return f, o
+    return 0, 0  # a leaf
+
+
+def count_ops(lines):
+    """(fma, other) FP64 operations of emitted statement lines (`lhs = expr;`)."""
+    seen, f, o = set(), 0, 0
+    for ln in lines:
+        ln = ln.strip()
+        if "=" not in ln or not ln.endswith(";"):
+            continue
+        rhs = ln.split("=", 1)[1].rstrip(";")
+        if rhs.strip().startswith("R(") and "*" not in rhs:
+            continue
+        df, do = _count_expr(rhs, seen)
+        f += df
+        o += do
+    return f, o
+
+
+def setup_ops(la, lb, lc, ld):
+    """(fma, other) FP64 operations of a primitive quartet before the Boys
+    function, with 1/sqrt(p+q), pq/(p+q), q/(p+q), p/(p+q) from the exponent
+    table: P - Q (3), |P - Q|^2 (a product and 2 FMA), T (1), the prefactor
+    K_ab K_cd rs (2), W - P when the bra has angular momentum (3), W - Q when
+    the ket has (3), 1/(2(p+q)) when both have (2).  (ss|ss) and (ps|ss) fold
+    the prefactor and the W - P factor into their own products (their cases in
+    eri_class_kernel)."""
+    bra, ket = la + lb > 0, lc + ld > 0
+    other = 3 + 1 + 1 + 2 + (3 if bra else 0) + (3 if ket else 0) + (2 if bra and ket else 0)
+    return 2, other
 
 
 # ---------------------------------------------------------------------------
@@ -572,14 +656,20 @@ def main(outdir):
         NE = len(comps_range(la, la + lb))
         NF = len(comps_range(lc, lc + ld))
         NA, NB, NC, ND = ncart(la), ncart(lb), ncart(lc), ncart(ld)
+        # algorithmic FP64 operations of one primitive quartet, as the kernel
+        # evaluates it: set-up, Boys function, the emitted VRR (each distinct
+        # subexpression once); the two smallest classes by their own forms
         bf, bo = boys_ops(L)
-        # per primitive quartet set-up: p+q, rsqrt (library: ~4 FP64 ops), 1/(p+q),
-        # P-Q, q/(p+q), p/(p+q), T (3 FMA-type), prefactor (2), W-P and W-Q (6),
-        # 1/(2(p+q)): 12 multiply/add + 3 FMA + rsqrt
-        setup_fma, setup_other = 3, 16
-        prim_flops = 2 * (vem.nfma + bf + setup_fma) + (vem.nmul + bo + setup_other)
+        sf, so = setup_ops(la, lb, lc, ld)
+        vf, vo = count_ops(vem.lines)
+        if (la, lb, lc, ld) == (0, 0, 0, 0):  # pref F_0 into the accumulating FMA
+            bo, vf, vo = bo - 1, 1, 0
+        elif (la, lb, lc, ld) == (1, 0, 0, 0):  # PA_i (pref F_0) + PQ_i (-pref q/(p+q) F_1)
+            so, bo, vf, vo = so - 3, bo + 1, 6, 0
+        prim_flops = 2 * (vf + bf + sf) + (vo + bo + so)
         # per contracted quartet: HRR + scatter (6 FMA per integral)
-        contr_flops = 2 * hem.nfma + hem.nmul + 2 * 6 * NA * NB * NC * ND
+        hf, ho = count_ops(hem.lines)
+        contr_flops = 2 * hf + ho + 2 * 6 * NA * NB * NC * ND
         lines = []
         lines.append("// class (%d%d|%d%d): VRR %s-choice %d ops, HRR %s-choice %d ops" % (la, lb, lc, ld, chv, cost_v, chh, cost_h))
         lines.append("template <> struct EriClass<%d,%d,%d,%d> {" % (la, lb, lc, ld))

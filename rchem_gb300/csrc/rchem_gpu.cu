@@ -773,10 +773,12 @@ static int count_ge(const std::vector<ShellPair> &p, const PairGroup &g, double 
 static const int kMinPrimPerLane = 16;
 
 // Algorithmic FLOPs of one primitive quartet of class kernel k: the generated
-// count, less p+q, 1/sqrt(p+q) (counted as 4), q/(p+q) and p/(p+q) where the
-// FP64 and double-float lists (prec 0) read them from the exponent table
+// count (the operations the FP64 kernel evaluates, its (p, q) factors read
+// from the exponent table), plus p+q, 1/sqrt(p+q) (counted as 4), 1/(p+q),
+// q/(p+q), p/(p+q) and pq/(p+q) where the kernel computes them (the FP32
+// lists, and every list of a basis without the table)
 static double prim_flops(rchem_basis b, int k, int prec) {
-    return rchem_class_flops[k][0] - ((prec == 0 && pq_active(b) > 0) ? 7.0 : 0.0);
+    return rchem_class_flops[k][0] + ((prec == 0 && pq_active(b) > 0) ? 0.0 : 9.0);
 }
 
 // Split the bra shell pairs of a build into nparts shares of about equal cost:
