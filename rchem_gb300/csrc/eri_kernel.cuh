@@ -148,19 +148,28 @@ template <> struct Tabs<float> {
 // Scaled Boys values F[0..L] of one primitive quartet.  With a.f32_boys64 the
 // FP32 kernels evaluate the function and its downward recursion in FP64 from
 // the FP32 argument and prefactor, and round the results to FP32.
+// The Boys function.  FP64 (and the FP64 Boys function of the FP32 quartets
+// with f32_boys64) runs boys_eval_u, one instruction stream for T on either
+// side of the Taylor range: those kernels are bound by the narrow FP64 pipe,
+// where a diverged warp issuing both branches cost 12 % of the build.  The
+// FP32 and double-float kernels keep boys_eval's two branches: they are bound
+// by instruction issue, and the branch-free form's extra integer selects and
+// loads cost them more than the divergence (measured: mixed 21.2 -> 22.3 ms,
+// emulated 24.1 -> 27.2 ms on the (H2O)32 build).
 template <int L, typename R, bool SCALE = true>
 __device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R *btab, R *F) {
+    static_assert(L <= BOYS_FAR_M - 1, "the power-law table holds m <= 8");
     if constexpr (std::is_same<R, float>::value) {
         if (a.f32_boys64) {
             double Fd[L + 1];
-            boys_eval<L, double, SCALE>((double)T, (double)pref, a.boys64, Fd);
+            boys_eval_u<L, SCALE>((double)T, (double)pref, a.boys64, a.boysfar, Fd);
 #pragma unroll
             for (int m = 0; m <= L; ++m) F[m] = (float)Fd[m];
             return;
         }
-    }
-    if constexpr (std::is_same<R, double>::value && L <= BOYS_FAR_M - 1) {
-        boys_eval_u<L, SCALE>(T, pref, btab, a.boysfar, F);  // one FP64 instruction stream for every T
+        boys_eval<L, R, SCALE>(T, pref, btab, F);
+    } else if constexpr (std::is_same<R, double>::value) {
+        boys_eval_u<L, SCALE>(T, pref, btab, a.boysfar, F);
     } else {
         boys_eval<L, R, SCALE>(T, pref, btab, F);
     }

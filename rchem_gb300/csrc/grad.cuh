@@ -40,6 +40,7 @@ struct GradArgs {
     const int *shell_atom;
     const int *shell_l;
     const double *boys64;
+    const double *boysfar;  // the FP64 power-law table of boys_eval_u
     const double *D;
     double *grad;  // 3 * natoms
     int npq;       // exponent-pair factor table (EriArgs::npq and the three after it)

@@ -248,7 +248,11 @@ __global__ void __launch_bounds__(64) k_grad2e_cls(GradArgs g) {
         const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
         const R T = rho * (X * X + Y * Y + Zc * Zc);
         R F[L1 + 1], Rt[nr(L1)];
-        boys_eval<L1, R>(T, Kab * Kcd * rs, btab, F);
+        // FP64: one instruction stream for every T (not (pp|ps), (pp|pp): register-bound)
+        if constexpr (std::is_same<R, double>::value && L1 <= BOYS_FAR_M - 1 && !(LA == 1 && LB == 1 && LC == 1))
+            boys_eval_u<L1, true>(T, Kab * Kcd * rs, btab, g.boysfar, F);
+        else
+            boys_eval<L1, R>(T, Kab * Kcd * rs, btab, F);
         coulomb<L1, R>(rho, X, Y, Zc, F, Rt);
         Herm<LA + 1, LB + 1, R> Eb[3];
         Herm<LC + 1, LD, R> Ek[3];

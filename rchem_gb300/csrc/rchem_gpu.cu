@@ -1580,6 +1580,7 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
         g.shell_atom = b->d_shell_atom;
         g.shell_l = b->d_shell_l;
         g.boys64 = b->tabs->boys64;
+        g.boysfar = b->tabs->boysfar;
         g.boys32 = b->tabs->boys32;
         g.boysdf = b->tabs->boysdf;
         g.D = b->d_D;
