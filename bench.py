@@ -621,7 +621,7 @@ def main():
     roof["nominal_fp64"] = NOMINAL_FP64_TFLOPS
     roof["build"] = {"achieved": build_tflops, "frac": build_tflops / peak64 if peak64 else None,
                      "flops_per_build": st64["flops_fp64"], "ms": ms, "traffic": traffic.get("build")}
-    roof["lists"] = rows[:8]
+    roof["lists"] = rows
 
     # ---- precision forms (same timing), SCF against the FP64 SCF ----------
     forms = {}

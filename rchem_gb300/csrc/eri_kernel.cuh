@@ -469,7 +469,7 @@ __device__ __forceinline__ R wc_sel4(int n, const R *v) {  // v[0..3] = 1..4 tim
 }
 
 template <int LA, int LB, int LC, int LD, typename R, int EPI = EPI_JK>
-__global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
+__global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 registers
     using C = EriClass<LA, LB, LC, LD>;
     using P = EriProg<LA, LB, LC, LD>;
     using W = WcShape<LA, LB, LC, LD, R>;
@@ -526,33 +526,43 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
             if (n2) v = rchem_fma(wc_sel4(n2, cpq), tg, v);
             return v;
         };
+        // one pass: NS <= WC_U independent terms per lane, every program word,
+        // then every operand, loaded before any result is stored (latency overlap)
+        auto vpass = [&](const int t, const int e, auto nsc) {
+            constexpr int NS = decltype(nsc)::value;
+            uint4 o[NS];
+            R ta[NS], tb[NS], tc[NS], td[NS], tg[NS];
+#pragma unroll
+            for (int u = 0; u < NS; ++u) o[u] = t + 32 * u < e ? __ldg(vprog + t + 32 * u) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (int u = 0; u < NS; ++u) {
+                const unsigned n1 = (o[u].w >> 3) & 7, n2 = (o[u].w >> 6) & 7;
+                ta[u] = S[o[u].x >> 16];
+                tb[u] = S[o[u].y & 0xffff];
+                tc[u] = n1 ? S[o[u].y >> 16] : R(0);
+                td[u] = n1 ? S[o[u].z & 0xffff] : R(0);
+                tg[u] = n2 ? S[o[u].z >> 16] : R(0);
+            }
+#pragma unroll
+            for (int u = 0; u < NS; ++u) {
+                const R v = term(o[u].w, ta[u], tb[u], tc[u], td[u], tg[u]);
+                if (t + 32 * u < e) {
+                    const unsigned dest = o[u].x & 0xffff, tg1 = o[u].w >> 9;
+                    if (dest != 0xffffu) S[dest] = v;
+                    if (tg1) S[tg1 - 1] += v;  // a target: into its contraction accumulator
+                }
+            }
+        };
         for (int lv = 0; lv < P::NVL; ++lv) {
             const int e = __ldg(vlev + lv + 1);
-            // WC_U independent terms per lane and pass: every program word, then
-            // every operand, is loaded before any result is stored (latency overlap)
-            for (int t = __ldg(vlev + lv) + lane; t < e; t += 32 * WC_U) {
-                uint4 o[WC_U];
-                R ta[WC_U], tb[WC_U], tc[WC_U], td[WC_U], tg[WC_U];
-#pragma unroll
-                for (int u = 0; u < WC_U; ++u) o[u] = t + 32 * u < e ? __ldg(vprog + t + 32 * u) : make_uint4(0, 0, 0, 0);
-#pragma unroll
-                for (int u = 0; u < WC_U; ++u) {
-                    const unsigned n1 = (o[u].w >> 3) & 7, n2 = (o[u].w >> 6) & 7;
-                    ta[u] = S[o[u].x >> 16];
-                    tb[u] = S[o[u].y & 0xffff];
-                    tc[u] = n1 ? S[o[u].y >> 16] : R(0);
-                    td[u] = n1 ? S[o[u].z & 0xffff] : R(0);
-                    tg[u] = n2 ? S[o[u].z >> 16] : R(0);
-                }
-#pragma unroll
-                for (int u = 0; u < WC_U; ++u) {
-                    const R v = term(o[u].w, ta[u], tb[u], tc[u], td[u], tg[u]);
-                    if (t + 32 * u < e) {
-                        const unsigned dest = o[u].x & 0xffff, tg1 = o[u].w >> 9;
-                        if (dest != 0xffffu) S[dest] = v;
-                        if (tg1) S[tg1 - 1] += v;  // a target: into its contraction accumulator
-                    }
-                }
+            // passes over the level (warp-uniform): each takes only the term slots
+            // that hold a term for some lane, so a small level's empty slots cost nothing
+            for (int b = __ldg(vlev + lv); b < e; b += 32 * WC_U) {
+                const int ns = min(WC_U, (e - b + 31) >> 5);
+                if (ns == 4) vpass(b + lane, e, std::integral_constant<int, 4>{});
+                else if (ns == 3) vpass(b + lane, e, std::integral_constant<int, 3>{});
+                else if (ns == 2) vpass(b + lane, e, std::integral_constant<int, 2>{});
+                else vpass(b + lane, e, std::integral_constant<int, 1>{});
             }
             __syncwarp();
         }
@@ -567,23 +577,31 @@ __global__ void __launch_bounds__(256) eri_wc_kernel(EriArgs a) {
         const int dir = (op.y >> 16) & 255, side = op.y >> 24;
         return side ? wc_sel3(dir, CD[0], CD[1], CD[2]) : wc_sel3(dir, AB[0], AB[1], AB[2]);
     };
+    auto hpass = [&](const int t, const int e, auto nsc) {
+        constexpr int NS = decltype(nsc)::value;
+        uint2 o[NS];
+        R tx[NS], ty[NS];
+#pragma unroll
+        for (int u = 0; u < NS; ++u) o[u] = t + 32 * u < e ? __ldg(hprog + t + 32 * u) : make_uint2(0, 0);
+#pragma unroll
+        for (int u = 0; u < NS; ++u) {
+            tx[u] = S[o[u].x >> 16];
+            ty[u] = S[o[u].y & 0xffff];
+        }
+#pragma unroll
+        for (int u = 0; u < NS; ++u) {
+            const R v = rchem_fma(hcoef(o[u]), ty[u], tx[u]);
+            if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
+        }
+    };
     for (int lv = 0; lv < P::NHL; ++lv) {
         const int e = __ldg(hlev + lv + 1);
-        for (int t = __ldg(hlev + lv) + lane; t < e; t += 32 * WC_U) {
-            uint2 o[WC_U];
-            R tx[WC_U], ty[WC_U];
-#pragma unroll
-            for (int u = 0; u < WC_U; ++u) o[u] = t + 32 * u < e ? __ldg(hprog + t + 32 * u) : make_uint2(0, 0);
-#pragma unroll
-            for (int u = 0; u < WC_U; ++u) {
-                tx[u] = S[o[u].x >> 16];
-                ty[u] = S[o[u].y & 0xffff];
-            }
-#pragma unroll
-            for (int u = 0; u < WC_U; ++u) {
-                const R v = rchem_fma(hcoef(o[u]), ty[u], tx[u]);
-                if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
-            }
+        for (int b = __ldg(hlev + lv); b < e; b += 32 * WC_U) {
+            const int ns = min(WC_U, (e - b + 31) >> 5);
+            if (ns == 4) hpass(b + lane, e, std::integral_constant<int, 4>{});
+            else if (ns == 3) hpass(b + lane, e, std::integral_constant<int, 3>{});
+            else if (ns == 2) hpass(b + lane, e, std::integral_constant<int, 2>{});
+            else hpass(b + lane, e, std::integral_constant<int, 1>{});
         }
         __syncwarp();
     }
