@@ -461,6 +461,13 @@ struct WcShape {
     static_assert(BYTES <= RCHEM_BLOCK_SMEM, "a warp's recurrence values exceed a block's shared memory");
 };
 
+// lanes per target of a warp-cooperative contraction of ntg sums of nl terms
+constexpr int wc_split(int ntg, int nl) {
+    int p = 1;
+    while (2 * p * ntg <= 32 && 2 * p <= nl) p *= 2;
+    return p;
+}
+
 template <typename R>
 __device__ __forceinline__ R wc_sel3(int i, R a, R b, R c) { return i == 0 ? a : (i == 1 ? b : c); }
 template <typename R>
@@ -635,59 +642,82 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
         return;
     }
 
-    // degeneracy-weighted 8-fold scatter, the lanes splitting each contraction
+    // degeneracy-weighted 8-fold scatter: each of the six contractions is a
+    // set of NTG target sums of NL terms; SPL lanes share a target (each a
+    // strided part of its sum, then a shuffle reduction), SPL the largest power
+    // of two with NTG SPL <= 32 and SPL <= NL, so a contraction with few
+    // targets still keeps the lanes busy
     const int kK = -(bp.diag + kp.diag + (bidx == kidx ? 1 : 0)), kJ = kK + 1;
     const int n = bp.mn, mo = bp.moff;
     const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
 #define WIDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
-    for (int t = lane; t < NA * NB; t += 32) {  // J-hat bra: 2 (ab|cd) D_cd
-        const int ia = t / NB, ib = t - ia * NB;
-        R sum = R(0);
-        for (int ic = 0; ic < NC; ++ic)
-            for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (l0 + ic) * n + s0 + id), sum);
-        atomicAdd(a.J + mo + (m0 + ia) * n + n0 + ib, jk_term(sum, kJ));
-    }
-    for (int t = lane; t < NC * ND; t += 32) {  // J-hat ket: 2 (ab|cd) D_ab
-        const int ic = t / ND, id = t - ic * ND;
-        R sum = R(0);
-        for (int ia = 0; ia < NA; ++ia)
-            for (int ib = 0; ib < NB; ++ib)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + n0 + ib), sum);
-        atomicAdd(a.J + mo + (l0 + ic) * n + s0 + id, jk_term(sum, kJ));
-    }
-    for (int t = lane; t < NA * NC; t += 32) {  // K-hat[a][c] += (ab|cd) D_bd
-        const int ia = t / NC, ic = t - ia * NC;
-        R sum = R(0);
-        for (int ib = 0; ib < NB; ++ib)
-            for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + s0 + id), sum);
-        atomicAdd(a.K + mo + (m0 + ia) * n + l0 + ic, jk_term(sum, kK));
-    }
-    for (int t = lane; t < NB * NC; t += 32) {  // K-hat[b][c] += (ab|cd) D_ad
-        const int ib = t / NC, ic = t - ib * NC;
-        R sum = R(0);
-        for (int ia = 0; ia < NA; ++ia)
-            for (int id = 0; id < ND; ++id)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + s0 + id), sum);
-        atomicAdd(a.K + mo + (n0 + ib) * n + l0 + ic, jk_term(sum, kK));
-    }
-    for (int t = lane; t < NA * ND; t += 32) {  // K-hat[a][d] += (ab|cd) D_bc
-        const int ia = t / ND, id = t - ia * ND;
-        R sum = R(0);
-        for (int ib = 0; ib < NB; ++ib)
-            for (int ic = 0; ic < NC; ++ic)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (n0 + ib) * n + l0 + ic), sum);
-        atomicAdd(a.K + mo + (m0 + ia) * n + s0 + id, jk_term(sum, kK));
-    }
-    for (int t = lane; t < NB * ND; t += 32) {  // K-hat[b][d] += (ab|cd) D_ac
-        const int ib = t / ND, id = t - ib * ND;
-        R sum = R(0);
-        for (int ia = 0; ia < NA; ++ia)
-            for (int ic = 0; ic < NC; ++ic)
-                sum = rchem_fma(A(WIDX(ia, ib, ic, id)), Tabs<R>::dens(a, mo + (m0 + ia) * n + l0 + ic), sum);
-        atomicAdd(a.K + mo + (n0 + ib) * n + s0 + id, jk_term(sum, kK));
-    }
+    auto contract = [&](auto ntg_c, auto nl_c, double *M, int kw, auto tgt, auto term) {
+        constexpr int NTG = decltype(ntg_c)::value, NL = decltype(nl_c)::value;
+        constexpr int SPL = wc_split(NTG, NL), PER = 32 / SPL;
+        const int sl = lane & (SPL - 1);
+        for (int t0 = 0; t0 < NTG; t0 += PER) {
+            const int t = t0 + lane / SPL;
+            R sum = R(0);
+            if (t < NTG)
+                for (int i = sl; i < NL; i += SPL) {
+                    int ai, di;
+                    term(t, i, ai, di);
+                    sum = rchem_fma(A(ai), Tabs<R>::dens(a, di), sum);
+                }
+#pragma unroll
+            for (int o = SPL >> 1; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            if (t < NTG && sl == 0) atomicAdd(M + tgt(t), jk_term(sum, kw));
+        }
+    };
+    using std::integral_constant;
+    // J-hat bra: 2 (ab|cd) D_cd
+    contract(integral_constant<int, NA * NB>{}, integral_constant<int, NC * ND>{}, a.J, kJ,
+             [&](int t) { return mo + (m0 + t / NB) * n + n0 + t % NB; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ic = i / ND, id = i % ND;
+                 ai = WIDX(t / NB, t % NB, ic, id);
+                 di = mo + (l0 + ic) * n + s0 + id;
+             });
+    // J-hat ket: 2 (ab|cd) D_ab
+    contract(integral_constant<int, NC * ND>{}, integral_constant<int, NA * NB>{}, a.J, kJ,
+             [&](int t) { return mo + (l0 + t / ND) * n + s0 + t % ND; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ia = i / NB, ib = i % NB;
+                 ai = WIDX(ia, ib, t / ND, t % ND);
+                 di = mo + (m0 + ia) * n + n0 + ib;
+             });
+    // K-hat[a][c] += (ab|cd) D_bd
+    contract(integral_constant<int, NA * NC>{}, integral_constant<int, NB * ND>{}, a.K, kK,
+             [&](int t) { return mo + (m0 + t / NC) * n + l0 + t % NC; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ib = i / ND, id = i % ND;
+                 ai = WIDX(t / NC, ib, t % NC, id);
+                 di = mo + (n0 + ib) * n + s0 + id;
+             });
+    // K-hat[b][c] += (ab|cd) D_ad
+    contract(integral_constant<int, NB * NC>{}, integral_constant<int, NA * ND>{}, a.K, kK,
+             [&](int t) { return mo + (n0 + t / NC) * n + l0 + t % NC; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ia = i / ND, id = i % ND;
+                 ai = WIDX(ia, t / NC, t % NC, id);
+                 di = mo + (m0 + ia) * n + s0 + id;
+             });
+    // K-hat[a][d] += (ab|cd) D_bc
+    contract(integral_constant<int, NA * ND>{}, integral_constant<int, NB * NC>{}, a.K, kK,
+             [&](int t) { return mo + (m0 + t / ND) * n + s0 + t % ND; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ib = i / NC, ic = i % NC;
+                 ai = WIDX(t / ND, ib, ic, t % ND);
+                 di = mo + (n0 + ib) * n + l0 + ic;
+             });
+    // K-hat[b][d] += (ab|cd) D_ac
+    contract(integral_constant<int, NB * ND>{}, integral_constant<int, NA * NC>{}, a.K, kK,
+             [&](int t) { return mo + (n0 + t / ND) * n + s0 + t % ND; },
+             [&](int t, int i, int &ai, int &di) {
+                 const int ia = i / NC, ic = i % NC;
+                 ai = WIDX(ia, t / ND, ic, t % ND);
+                 di = mo + (m0 + ia) * n + l0 + ic;
+             });
 #undef WIDX
 }
 
