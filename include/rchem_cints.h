@@ -68,7 +68,10 @@ int rchem_eri_prim_batch(int count, const rchem_prim *prims, double *out, int wh
  * 2 = nuclear_attraction (with norms and sign; centre i = centers[3i..3i+2]). */
 int rchem_onee_prim_batch(int kind, int count, const rchem_prim *prims, const double *centers, double *out,
                           int where);
-/* out[i] = F_m[i](x[i]); precision 64 or 32 (the kernels' FP32 Boys, widened). */
+/* out[i] = F_m[i](x[i]); precision 64 (0 <= m <= 16; the run-time-m evaluation
+ * of the gradient kernels), 65 (0 <= m <= 8; the branch-free FP64 evaluation of
+ * the ERI kernels, through its L = 8 downward recursion) or 32 (the kernels' FP32
+ * Boys, widened).  A device-resident m outside the range gives NaN. */
 int rchem_boys_batch(int count, const int *m, const double *x, double *out, int precision, int where);
 
 #ifdef __cplusplus

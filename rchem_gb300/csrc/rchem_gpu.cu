@@ -230,11 +230,19 @@ __global__ void k_onee_prim_batch(int kind, int count, const rchem_prim *pr, con
 }
 
 __global__ void k_boys_batch(int count, const int *m, const double *x, const double *b64, const float *b32,
-                             int prec, double *out) {
+                             const double *bfar, int prec, double *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
     const int mm = m[i];
-    if (prec == 32) {
+    if (mm < 0 || mm > (prec == 65 ? BOYS_FAR_M - 1 : BOYS_MMAX)) {  // device input unchecked on the host
+        out[i] = nan("");
+        return;
+    }
+    if (prec == 65) {  // the ERI kernels' branch-free evaluation, through the L = 8 recursion
+        double F[BOYS_FAR_M];
+        boys_eval_u<BOYS_FAR_M - 1, false>(x[i], 1.0, b64, bfar, F);
+        out[i] = F[mm];
+    } else if (prec == 32) {
         float F[BOYS_MMAX + 1];
         boys_eval_rt<float>(mm, (float)x[i], 1.0f, b32, F);
         out[i] = F[mm];
@@ -2066,12 +2074,14 @@ extern "C" int rchem_onee_prim_batch(int kind, int count, const rchem_prim *prim
 
 extern "C" int rchem_boys_batch(int count, const int *m, const double *x, double *out, int precision, int where) {
     if (count < 0 || (count > 0 && (!m || !x || !out))) return set_err(RCHEM_ERR_INVALID, "bad argument");
-    if (precision != 64 && precision != 32) return set_err(RCHEM_ERR_INVALID, "precision=%d", precision);
+    if (precision != 64 && precision != 32 && precision != 65)
+        return set_err(RCHEM_ERR_INVALID, "precision=%d", precision);
     if (count == 0) return RCHEM_OK;
+    const int mmax = precision == 65 ? BOYS_FAR_M - 1 : BOYS_MMAX;
     if (where == RCHEM_HOST)
         for (int i = 0; i < count; ++i)
-            if (m[i] < 0 || m[i] > BOYS_MMAX || !(x[i] >= 0.0))
-                return set_err(RCHEM_ERR_INVALID, "m=%d x=%g (0 <= m <= %d, x >= 0)", m[i], x[i], BOYS_MMAX);
+            if (m[i] < 0 || m[i] > mmax || !(x[i] >= 0.0))
+                return set_err(RCHEM_ERR_INVALID, "m=%d x=%g (0 <= m <= %d, x >= 0)", m[i], x[i], mmax);
     const DevTables *t;
     CKR(get_tables(&t));
     std::vector<void *> tmp;
@@ -2085,7 +2095,7 @@ extern "C" int rchem_boys_batch(int count, const int *m, const double *x, double
         if (cudaMalloc(&dout, count * sizeof(double)) != cudaSuccess) { free_all(tmp); return set_err(RCHEM_ERR_NOMEM, "out"); }
         tmp.push_back(dout);
     }
-    k_boys_batch<<<(count + 127) / 128, 128>>>(count, dm, dx, t->boys64, t->boys32, precision, dout);
+    k_boys_batch<<<(count + 127) / 128, 128>>>(count, dm, dx, t->boys64, t->boys32, t->boysfar, precision, dout);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && where == RCHEM_HOST) e = cudaMemcpy(out, dout, count * sizeof(double), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && where == RCHEM_DEVICE) e = cudaDeviceSynchronize();

@@ -72,6 +72,14 @@ def test_boys_batch(gpu, port):
     v64 = cints.boys_batch(ms, xs, 64)
     v32 = cints.boys_batch(ms, xs, 32)
     assert np.all(np.abs(v64 - ex) <= 4e-15 * ex)
+    # the ERI kernels' branch-free evaluation (m <= 8): Taylor rows, the power
+    # law past T = 80 (both sides of the switch in the sample), L = 8 recursion
+    lo = np.array(ms) <= 8
+    xs_u = list(np.array(xs)[lo]) + [79.99, 80.0, 80.01, 1e4, 3.7e7]
+    ms_u = list(np.array(ms)[lo]) + [8, 8, 0, 3, 1]
+    ex_u = np.array([port.boys_exact(m, x) for m, x in zip(ms_u, xs_u)])
+    vu = cints.boys_batch(ms_u, xs_u, 65)
+    assert np.all(np.abs(vu - ex_u) <= 2e-15 * ex_u), np.max(np.abs(vu - ex_u) / ex_u)
     normal32 = ex > 1e-30  # below that the single-precision values are subnormal
     # the FP32 form (screened-weak quartets only) loses ~m ulps in the upward recursion
     assert np.all(np.abs(v32 - ex)[normal32] <= 1e-5 * ex[normal32])
