@@ -23,6 +23,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "rchem_types.h"
 
 // h = 1/128 (FP64) and 1/64 (FP32) are exact in binary, so T_i = i*h and
@@ -157,6 +159,14 @@ template <typename R>
 RCHEM_HD inline R boys_horner(const R *__restrict__ tab, int s, int i, R x) {
     constexpr int NT = BoysPrec<R>::NTAY;
     const R *c = tab + boys_idx(s, i, 0, NT, BoysPrec<R>::NGRID);
+#ifdef __CUDA_ARCH__
+    if constexpr (std::is_same<R, float>::value && NT == 4) {
+        // an FP32 row is 16 aligned bytes: one vector load (the FP32 kernels
+        // are bound by their global-load instructions, not their arithmetic)
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(c));
+        return fmaf(fmaf(fmaf(v.w, x, v.z), x, v.y), x, v.x);
+    }
+#endif
     R acc = rchem_ldg(c + NT - 1);
 #pragma unroll
     for (int k = NT - 2; k >= 0; --k) acc = rchem_fma(acc, x, rchem_ldg(c + k));
