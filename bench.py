@@ -336,30 +336,34 @@ def fock_forms(rc, torch, b, J, K, Dh, J64, K64, run, steps, warmup, scf_ref):
     """The precision forms on the same workload: time, J/K at the timed
     density against FP64, and the converged SCF against the FP64 SCF."""
     out = {}
-    forms = (("mixed_1e-6_boys64", 1e-6, False, True,
-              "FP32 for quartets with Q_ab Q_cd < 1e-6 with the Boys function and its downward recursion in FP64, "
-              "native FP64 above, FP64 accumulation: the stated mixed form, literally"),
-             ("mixed_1e-6", 1e-6, False, False,
-              "as mixed_1e-6_boys64 with the Boys function in FP32 too (its error, <= 2e-6 relative, is that of "
-              "the FP32 argument)"),
-             ("mixed_1e-4", 1e-4, False, False, "as mixed_1e-6 with the FP32 threshold at 1e-4"),
-             ("emulated", 0.0, True, False,
+    # (tag, fp32_tau, emulated, FP32 quartets' Boys function: "fp32" | "rec64" | "boys64", description)
+    forms = (("mixed_1e-6_rec64", 1e-6, False, "rec64",
+              "FP32 for quartets with Q_ab Q_cd < 1e-6, their Boys-function downward recursion in FP64 (table "
+              "values in FP32), native FP64 above, FP64 accumulation: the stated mixed form, literally"),
+             ("mixed_1e-6_boys64", 1e-6, False, "boys64",
+              "as mixed_1e-6_rec64 with the FP32 quartets' whole Boys function (table values too) in FP64"),
+             ("mixed_1e-6", 1e-6, False, "fp32",
+              "as mixed_1e-6_rec64 with the recursion in FP32 too (the Boys function's error, <= 2e-6 relative, "
+              "is that of the FP32 argument)"),
+             ("mixed_1e-4", 1e-4, False, "fp32", "as mixed_1e-6 with the FP32 threshold at 1e-4"),
+             ("emulated", 0.0, True, "fp32",
               "double-float (hi+lo float pairs, ~48-bit significand) on the FP32 pipe for every quartet of the "
               "classes that have it, native FP64 for the rest: an addition beyond the stated form"),
-             ("emulated_mixed_1e-6", 1e-6, True, False,
+             ("emulated_mixed_1e-6", 1e-6, True, "fp32",
               "FP32 below 1e-6, double-float above: an addition beyond the stated form"))
     ms64 = scf_ref["ms"]
-    for tag, tau32, emul, b64, what in forms:
-        b.autotune(SCHWARZ_TAU, tau32, emulated=emul, fp32_boys64=b64)
-        ms = float(np.mean(run(tau32, steps, warmup, emulated=emul, fp32_boys64=b64)))
+    for tag, tau32, emul, bmode, what in forms:
+        fl = {"fp32_boys64": bmode == "boys64", "fp32_rec64": bmode == "rec64"}
+        b.autotune(SCHWARZ_TAU, tau32, emulated=emul, **fl)
+        ms = float(np.mean(run(tau32, steps, warmup, emulated=emul, **fl)))
         st = b.stats()
         Jf, Kf = J.cpu().numpy(), K.cpu().numpy()
         t0 = time.perf_counter()
-        r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=emul, fp32_boys64=b64)
+        r = rc.scf.rhf(b, thresh_e=1e-10, fp32_tau=tau32, emulated=emul, **fl)
         torch.cuda.synchronize()
         t_scf = time.perf_counter() - t0
         out[tag] = {
-            "arithmetic": what, "fp32_tau": tau32, "emulated": emul, "fp32_boys64": b64, "ms": ms,
+            "arithmetic": what, "fp32_tau": tau32, "emulated": emul, "fp32_boys": bmode, "ms": ms,
             "builds_per_s": 1000.0 / ms,
             "speedup_vs_fp64": ms64 / ms,
             "fp32_quartet_fraction": st["quartets_fp32"] / max(1, st["quartets_fp32"] + st["quartets_fp64"]),
@@ -549,17 +553,19 @@ def main():
     K = torch.empty_like(D)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def run(tau32, steps, warmup, emulated=False, fp32_boys64=False):
+    def run(tau32, steps, warmup, emulated=False, fp32_boys64=False, fp32_rec64=False):
         # device time of each build from the library's own CUDA events on the
         # stream its kernels run on (bracketing the copy of D in, the class
         # kernels and the copies of J and K out); the L2 flush runs before.
         for _ in range(warmup):
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64,
+                         fp32_rec64=fp32_rec64)
         ms = []
         for _ in range(steps):
             with torch.cuda.stream(stream):
                 flush.fill_(1)
-            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64)
+            rc.JK_direct(J, K, b, D, fp32_tau=tau32, emulated=emulated, fp32_boys64=fp32_boys64,
+                         fp32_rec64=fp32_rec64)
             ms.append(b.stats()["gpu_ms"])
         torch.cuda.synchronize()
         return ms

@@ -94,6 +94,9 @@ int rchem_moment(rchem_basis b, const double *center, int ox, int oy, int oz, do
 #define RCHEM_JK_EMULATED 1    /* the FP64 quartets in double-float arithmetic on the FP32 pipe */
 #define RCHEM_JK_FP32_BOYS64 2 /* the FP32 quartets (below fp32_tau) evaluate the Boys function and its
                                   downward recursion in FP64, from their FP32 argument and prefactor */
+#define RCHEM_JK_FP32_REC64 4  /* the FP32 quartets evaluate the Boys function's table (or asymptotic)
+                                  values in FP32 and its recursion in FP64; with RCHEM_JK_FP32_BOYS64:
+                                  RCHEM_ERR_INVALID */
 
 /* Fock-build options.  Zero-initialised options mean: FP64 everywhere,
  * Schwarz threshold 1e-12, host arrays. */
@@ -106,7 +109,8 @@ typedef struct {
                            (~48-bit significand): every class with l_a+l_b+l_c+l_d <= 4, and
                            the larger classes whose list runs the warp-cooperative kernel
                            (rchem_autotune's choice); the others stay FP64.
-                           RCHEM_JK_FP32_BOYS64: see above.  Other bits: RCHEM_ERR_INVALID */
+                           RCHEM_JK_FP32_BOYS64, RCHEM_JK_FP32_REC64: see above.  Other bits:
+                           RCHEM_ERR_INVALID */
 } rchem_jk_opts;
 
 /* Work done by the last Fock build of a handle. */

@@ -127,14 +127,14 @@ class Basis:
         _lib.check(_lib.lib().rchem_basis_set_stream(self.handle, C.c_void_p(stream_ptr)))
         self._stream = stream_ptr
 
-    def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False, fp32_boys64=False):
+    def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False, fp32_boys64=False, fp32_rec64=False):
         """Pick the Fock build's tile shape per integral class for this basis
         (rchem_autotune); returns {(class, precision): min primitive quartets per lane}."""
         import numpy as _np
 
         chosen = _np.zeros(2 * 21, dtype=_np.int32)
         o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
-                        emulated=jk_flags(emulated, fp32_boys64))
+                        emulated=jk_flags(emulated, fp32_boys64, fp32_rec64))
         _lib.check(_lib.lib().rchem_autotune(self.handle, C.byref(o), chosen.ctypes.data))
         return {(k, p): int(chosen[2 * k + p]) for k in range(21) for p in range(2)}
 
@@ -229,17 +229,19 @@ def moment(basis: Basis, center, order, device=False):
     return out
 
 
-def jk_flags(emulated=False, fp32_boys64=False) -> int:
-    """rchem_jk_opts.emulated: RCHEM_JK_EMULATED (1) | RCHEM_JK_FP32_BOYS64 (2)."""
-    return (1 if emulated else 0) | (2 if fp32_boys64 else 0)
+def jk_flags(emulated=False, fp32_boys64=False, fp32_rec64=False) -> int:
+    """rchem_jk_opts.emulated: RCHEM_JK_EMULATED (1) | RCHEM_JK_FP32_BOYS64 (2) or
+    RCHEM_JK_FP32_REC64 (4)."""
+    return (1 if emulated else 0) | (2 if fp32_boys64 else 0) | (4 if fp32_rec64 else 0)
 
 
 def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False, part=0, nparts=1,
-              fp32_boys64=False):
+              fp32_boys64=False, fp32_rec64=False):
     """Fill J and K (in place, like the reference) from the density D.
     ``fp32_tau`` > 0 selects the mixed form; ``emulated`` computes the FP64
     quartets in double-float arithmetic on the FP32 pipe; ``fp32_boys64`` the
-    FP32 quartets' Boys function and downward recursion in FP64.  ``nparts`` > 1
+    FP32 quartets' Boys function and downward recursion in FP64, ``fp32_rec64``
+    only their recursion.  ``nparts`` > 1
     computes only share ``part`` of the bra shell pairs (rchem_jk_direct_part):
     the sum over the nparts shares is the whole build."""
     if not (0 <= part < nparts):
@@ -250,7 +252,7 @@ def JK_direct(J, K, basis: Basis, D, schwarz_tau=1e-12, fp32_tau=0.0, emulated=F
     for X, name in ((D, "D"), (J, "J"), (K, "K")):
         _check_f64(X, name, shape=(n, n))
     o = _lib.JKOpts(schwarz_tau=schwarz_tau if schwarz_tau > 0 else -1.0, fp32_tau=fp32_tau,
-                    where=_lib.DEVICE if dev else _lib.HOST, emulated=jk_flags(emulated, fp32_boys64))
+                    where=_lib.DEVICE if dev else _lib.HOST, emulated=jk_flags(emulated, fp32_boys64, fp32_rec64))
     _after_torch(basis, D, J, K)
     if nparts == 1:
         _lib.check(_lib.lib().rchem_jk_direct(basis.handle, C.c_void_p(_ptr(D)), C.c_void_p(_ptr(J)),

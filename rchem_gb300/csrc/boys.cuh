@@ -281,6 +281,35 @@ __device__ __forceinline__ void boys_eval_u(double T, double pref, const double 
 }
 #endif
 
+#ifdef __CUDACC__
+// FP32 quartets with the recursion in FP64 (RCHEM_JK_FP32_REC64): the Taylor
+// values F_L and e^{-T} (T < 40) or F_0 and e^{-T} (above) in FP32 as in
+// boys_eval, the downward (upward) recursion over m in FP64, the results
+// rounded to FP32 (times pref with SCALE).
+template <int L, bool SCALE>
+__device__ __forceinline__ void boys_eval_rec64(float T, float pref, const float *__restrict__ tab, float *F) {
+    double Fd[L + 1];
+    if (boys_small(T)) {
+        int i;
+        float x;
+        boys_grid(T, i, x);
+        const double ex = (double)boys_horner<float>(tab, 0, i, x);
+        Fd[L] = (double)boys_horner<float>(tab, L + 1, i, x);
+        const double T2 = 2.0 * (double)T;
+#pragma unroll
+        for (int m = L - 1; m >= 0; --m) Fd[m] = fma(T2, Fd[m + 1], ex) * rchem_recip<double>(2 * m + 1);
+    } else {
+        const float rs = rsqrtf(T);
+        const double inv2T = (double)(0.5f * rs * rs), ex = (double)expf(-T);
+        Fd[0] = (double)(0.88622692545275801365f * rs);
+#pragma unroll
+        for (int m = 1; m <= L; ++m) Fd[m] = (double(2 * m - 1) * Fd[m - 1] - ex) * inv2T;
+    }
+#pragma unroll
+    for (int m = 0; m <= L; ++m) F[m] = SCALE ? (float)Fd[m] * pref : (float)Fd[m];
+}
+#endif
+
 // Runtime-L variant for the generic (non-class) kernels; L <= BOYS_MMAX.
 template <typename R>
 RCHEM_HD inline void boys_eval_rt(int L, R T, R pref, const R *__restrict__ tab, R *F) {

@@ -149,7 +149,7 @@ template <> struct Tabs<float> {
 // FP32 kernels evaluate the function and its downward recursion in FP64 from
 // the FP32 argument and prefactor, and round the results to FP32.
 // The Boys function.  FP64 (and the FP64 Boys function of the FP32 quartets
-// with f32_boys64) runs boys_eval_u, one instruction stream for T on either
+// with f32_boys64 = 1) runs boys_eval_u, one instruction stream for T on either
 // side of the Taylor range: those kernels are bound by the narrow FP64 pipe,
 // where a diverged warp issuing both branches cost 12 % of the build.  The
 // FP32 and double-float kernels keep boys_eval's two branches: they are bound
@@ -160,12 +160,18 @@ template <int L, typename R, bool SCALE = true>
 __device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R *btab, R *F) {
     static_assert(L <= BOYS_FAR_M - 1, "the power-law table holds m <= 8");
     if constexpr (std::is_same<R, float>::value) {
-        if (a.f32_boys64) {
+        if (a.f32_boys64 == 1) {  // values and recursion in FP64
             double Fd[L + 1];
             boys_eval_u<L, SCALE>((double)T, (double)pref, a.boys64, a.boysfar, Fd);
 #pragma unroll
             for (int m = 0; m <= L; ++m) F[m] = (float)Fd[m];
             return;
+        }
+        if constexpr (L >= 2) {  // the recursion in FP64 (L <= 1 evaluates every F_m directly)
+            if (a.f32_boys64 == 2) {
+                boys_eval_rec64<L, SCALE>(T, pref, btab, F);
+                return;
+            }
         }
         boys_eval<L, R, SCALE>(T, pref, btab, F);
     } else if constexpr (std::is_same<R, double>::value) {

@@ -1360,7 +1360,16 @@ extern "C" int rchem_moment(rchem_basis b, const double *center, int ox, int oy,
 // ---------------------------------------------------------------------------
 // The device part of a Fock build on the handle's internal buffers:
 // d_D -> (d_D32) -> class kernels -> J-hat, K-hat -> d_Jo, d_Ko.
-static int record_build(rchem_basis b, bool any32, bool emul, bool boys64 = false) {
+// The FP32 quartets' Boys function from the arithmetic flags: 0 = FP32, 1 = FP64
+// (RCHEM_JK_FP32_BOYS64), 2 = FP32 values with the recursion in FP64
+// (RCHEM_JK_FP32_REC64); -1 = an invalid combination of flags.
+static int f32_boys_mode(int flags) {
+    if (flags & ~(RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64 | RCHEM_JK_FP32_REC64)) return -1;
+    if ((flags & RCHEM_JK_FP32_BOYS64) && (flags & RCHEM_JK_FP32_REC64)) return -1;
+    return (flags & RCHEM_JK_FP32_BOYS64) ? 1 : ((flags & RCHEM_JK_FP32_REC64) ? 2 : 0);
+}
+
+static int record_build(rchem_basis b, bool any32, bool emul, int boys64 = 0) {
     const size_t nn = (size_t)b->packed;
     const int th = 256;
     if (any32) {
@@ -1378,7 +1387,7 @@ static int record_build(rchem_basis b, bool any32, bool emul, bool boys64 = fals
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
-    a.f32_boys64 = boys64 ? 1 : 0;
+    a.f32_boys64 = boys64;
     CKR(launch_lists(b, a, EPI_JK, any32, emul));
     k_symmetrize<<<(unsigned)((nn + th - 1) / th), th, 0, b->stream>>>((long long)nn, b->ngeom, b->d_geom, b->d_Jh,
                                                                         b->d_Kh, b->d_Jo, b->d_Ko);
@@ -1393,8 +1402,10 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
     memset(&o, 0, sizeof(o));
     if (opts) o = *opts;
     if (o.where != RCHEM_HOST && o.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.where);
-    if (o.emulated & ~(RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64))
-        return set_err(RCHEM_ERR_INVALID, "emulated=%d (flags RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64)", o.emulated);
+    if (f32_boys_mode(o.emulated) < 0)
+        return set_err(RCHEM_ERR_INVALID,
+                       "emulated=%d (flags RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64 or RCHEM_JK_FP32_REC64)",
+                       o.emulated);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     CKR(plan_tasks(b, tau, tau32, part, nparts));
@@ -1406,7 +1417,8 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
     // replay the captured build; capture it again when the plan has changed.
     // The legacy default stream cannot be captured: run the launches directly there.
-    const bool emul = (o.emulated & RCHEM_JK_EMULATED) != 0, boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) != 0;
+    const bool emul = (o.emulated & RCHEM_JK_EMULATED) != 0;
+    const int boys64 = f32_boys_mode(o.emulated);
     const bool capturable = b->stream != nullptr && b->stream != cudaStreamLegacy;
     if (!capturable) {
         CKR(record_build(b, any32, emul, boys64));
@@ -1709,6 +1721,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
     if (opts) o = *opts;
+    if (f32_boys_mode(o.emulated) < 0) return set_err(RCHEM_ERR_INVALID, "emulated=%d", o.emulated);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     static const int cand[] = {4, 8, 16, 32, 64, 1 << 30};
@@ -1742,7 +1755,7 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
         a.Ddf = b->d_Ddf;
         a.J = b->d_Jh;
         a.K = b->d_Kh;
-        a.f32_boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) ? 1 : 0;
+        a.f32_boys64 = f32_boys_mode(o.emulated);
         for (int k = 0; k < RCHEM_NCLASS; ++k)
             for (int p = 0; p < 2; ++p) {
                 if (b->task_cnt[k][p] == 0 || (wc && !rchem_class_wc[k])) continue;
@@ -1775,6 +1788,7 @@ extern "C" int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, flo
     rchem_jk_opts o;
     memset(&o, 0, sizeof(o));
     if (opts) o = *opts;
+    if (f32_boys_mode(o.emulated) < 0) return set_err(RCHEM_ERR_INVALID, "emulated=%d", o.emulated);
     const double tau = (o.schwarz_tau == 0.0) ? 1e-12 : (o.schwarz_tau < 0.0 ? 0.0 : o.schwarz_tau);
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     CKR(plan_tasks(b, tau, tau32));
@@ -1790,7 +1804,7 @@ extern "C" int rchem_jk_list_times(rchem_basis b, const rchem_jk_opts *opts, flo
     a.D32 = b->d_D32;
     a.J = b->d_Jh;
     a.K = b->d_Kh;
-    a.f32_boys64 = (o.emulated & RCHEM_JK_FP32_BOYS64) ? 1 : 0;
+    a.f32_boys64 = f32_boys_mode(o.emulated);
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
             ms[2 * k + p] = 0.f;
@@ -2319,7 +2333,7 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     if (o.diis < 0 || o.diis > RCHEM_DIIS_MAX) return set_err(RCHEM_ERR_INVALID, "diis = %d (0..%d)", o.diis, RCHEM_DIIS_MAX);
     if (o.max_iter < 1) return set_err(RCHEM_ERR_INVALID, "max_iter = %d", o.max_iter);
     if (o.jk.where != RCHEM_HOST && o.jk.where != RCHEM_DEVICE) return set_err(RCHEM_ERR_INVALID, "where=%d", o.jk.where);
-    if (o.jk.emulated & ~(RCHEM_JK_EMULATED | RCHEM_JK_FP32_BOYS64))
+    if (f32_boys_mode(o.jk.emulated) < 0)
         return set_err(RCHEM_ERR_INVALID, "jk.emulated=%d", o.jk.emulated);
     const int ng = b->ngeom;
     const long long packed = b->packed;
@@ -2416,7 +2430,8 @@ extern "C" int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *n
     CKR(plan_tasks(b, tau, tau32));
     bool any32 = false;
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
-    const bool emul = (jo.emulated & RCHEM_JK_EMULATED) != 0, boys64 = (jo.emulated & RCHEM_JK_FP32_BOYS64) != 0;
+    const bool emul = (jo.emulated & RCHEM_JK_EMULATED) != 0;
+    const int boys64 = f32_boys_mode(jo.emulated);
     // One iteration, every argument fixed (state-driven), so the same launches
     // can be captured once and replayed:  J, K of D (the Fock build on the
     // handle's buffers), F = H + 2J - K, the energies, the DIIS step, the

@@ -31,7 +31,7 @@ def nuclear_repulsion(atomnos, coords) -> float:
 
 def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thresh_d: float = 1e-7,
         max_iter: int = 128, diis: int = 8, fp32_tau: float = 0.0, schwarz_tau: float = 1e-12, emulated=False,
-        verbose=False, fp32_boys64=False):
+        verbose=False, fp32_boys64=False, fp32_rec64=False):
     """Converge RHF for ``basis``; returns a dict with energies, D, C, eps, W."""
     import torch
 
@@ -60,7 +60,7 @@ def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thres
     it = 0
     for it in range(1, max_iter + 1):
         _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau, emulated=emulated,
-                    fp32_boys64=fp32_boys64)
+                    fp32_boys64=fp32_boys64, fp32_rec64=fp32_rec64)
         F = H + 2.0 * J - K
         e_old, e_new = e_new, float(torch.sum((H + F) * D))
         # DIIS on the orthogonalised commutator FDS - SDF
@@ -100,7 +100,7 @@ def rhf(basis: _b.Basis, nocc: int | None = None, thresh_e: float = 1e-10, thres
             break
     # energy at the final density with its own Fock matrix
     _b.JK_direct(J, K, basis, D, schwarz_tau=schwarz_tau, fp32_tau=fp32_tau, emulated=emulated,
-                    fp32_boys64=fp32_boys64)
+                    fp32_boys64=fp32_boys64, fp32_rec64=fp32_rec64)
     F = H + 2.0 * J - K
     e_elec = float(torch.sum((H + F) * D))
     eps, Cp = torch.linalg.eigh(X.T @ F @ X)

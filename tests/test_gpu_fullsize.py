@@ -120,13 +120,15 @@ def test_h2o32_elements_cover_every_class(h2o32_oracle):
     assert (np.abs(h2o32_oracle["K"]) > 1e-4).sum() >= 50
 
 
-@pytest.mark.parametrize("emulated,fp32_tau,b64,tol", [(False, 0.0, False, 1e-11), (True, 0.0, False, 1e-11),
-                                                       (False, 1e-6, False, 1e-7), (False, 1e-6, True, 1e-7)])
-def test_h2o32_sampled_elements_vs_oracle(gpu, h2o32_oracle, emulated, fp32_tau, b64, tol):
+@pytest.mark.parametrize("emulated,fp32_tau,bmode,tol", [(False, 0.0, "fp32", 1e-11), (True, 0.0, "fp32", 1e-11),
+                                                         (False, 1e-6, "fp32", 1e-7), (False, 1e-6, "boys64", 1e-7),
+                                                         (False, 1e-6, "rec64", 1e-7)])
+def test_h2o32_sampled_elements_vs_oracle(gpu, h2o32_oracle, emulated, fp32_tau, bmode, tol):
     """(H2O)32 in the 6-31G*-shaped basis with the autotuned plan the bench
     times (warp-cooperative kernels for the large classes): 216 J/K elements
     against the oracle, FP64 and emulated FP64 at 1e-11; the mixed form
-    (FP32 below 1e-6, its Boys function in FP32 or FP64) at 1e-7."""
+    (FP32 below 1e-6, its Boys function in FP32, in FP64, or FP32 with the
+    recursion in FP64) at 1e-7."""
     import torch
 
     import rchem_gb300 as rc
@@ -135,12 +137,13 @@ def test_h2o32_sampled_elements_vs_oracle(gpu, h2o32_oracle, emulated, fp32_tau,
     with rc.Basis(o["Z"], o["R"], o["bname"]) as b:
         n = b.nbf
         assert n == 608
-        chosen = b.autotune(1e-12, fp32_tau, emulated=emulated, fp32_boys64=b64)
+        fl = {"fp32_boys64": bmode == "boys64", "fp32_rec64": bmode == "rec64"}
+        chosen = b.autotune(1e-12, fp32_tau, emulated=emulated, **fl)
         if not emulated and fp32_tau == 0.0:
             assert any(v == 0 for (k, p), v in chosen.items() if p == 0)  # some list runs warp-cooperatively
         D = torch.from_numpy(o["D"]).cuda()
         J, K = torch.empty_like(D), torch.empty_like(D)
-        rc.JK_direct(J, K, b, D, fp32_tau=fp32_tau, emulated=emulated, fp32_boys64=b64)
+        rc.JK_direct(J, K, b, D, fp32_tau=fp32_tau, emulated=emulated, **fl)
         J, K = J.cpu().numpy(), K.cpu().numpy()
     dJ = np.abs(J[o["mus"], o["nus"]] - o["J"]).max()
     dK = np.abs(K[o["mus"], o["nus"]] - o["K"]).max()
@@ -159,9 +162,9 @@ def _oracle_scf(O, ob, Z, R, nocc):
 
 def test_h2o4_scf_energy_vs_oracle(gpu, oracle_mod):
     """(H2O)4 in the 6-31G**-shaped basis: the converged RHF energy of the GPU
-    driver (FP64) against the oracle's SCF at 1e-10 Eh; the mixed form (FP32
-    Boys function or FP64 Boys function below 1e-6) and emulated+mixed within
-    1e-9 Eh of the oracle."""
+    driver (FP64) against the oracle's SCF at 1e-10 Eh; the mixed form (below
+    1e-6 the Boys function in FP32, in FP64, or FP32 with its recursion in
+    FP64) and emulated+mixed within 1e-9 Eh of the oracle."""
     import rchem_gb300 as rc
 
     O = oracle_mod
@@ -174,9 +177,11 @@ def test_h2o4_scf_energy_vs_oracle(gpu, oracle_mod):
         assert r["converged"]
         assert abs(r["e_total"] - e_ref) < 1e-10, (r["e_total"], e_ref)
         assert float(np.abs(r["D"].cpu().numpy() - D_ref).max()) < 1e-6
-        for tau32, emul, b64 in ((1e-6, False, False), (1e-6, True, False), (1e-6, False, True)):
-            r2 = rc.scf.rhf(b, thresh_e=1e-11, thresh_d=1e-8, fp32_tau=tau32, emulated=emul, fp32_boys64=b64)
-            assert abs(r2["e_total"] - e_ref) < 1e-9, (tau32, emul, b64, r2["e_total"] - e_ref)
+        for tau32, emul, b64, r64 in ((1e-6, False, False, False), (1e-6, True, False, False),
+                                      (1e-6, False, True, False), (1e-6, False, False, True)):
+            r2 = rc.scf.rhf(b, thresh_e=1e-11, thresh_d=1e-8, fp32_tau=tau32, emulated=emul, fp32_boys64=b64,
+                            fp32_rec64=r64)
+            assert abs(r2["e_total"] - e_ref) < 1e-9, (tau32, emul, b64, r64, r2["e_total"] - e_ref)
 
 
 def test_batch_sample_energies_vs_oracle(gpu, oracle_mod):

@@ -241,14 +241,21 @@ def test_mixed_precision_close_to_fp64(gpu):
         assert b.stats()["quartets_fp32"] == st["quartets_fp32"]
         assert np.abs(Jb - J).max() < 1e-8 and np.abs(Kb - K).max() < 1e-8
         assert np.abs(Jb - Jm).max() > 0.0  # a different evaluation did run
-        # an unknown flag is refused before any work
+        # ... with only the Boys function's recursion in FP64 (the stated form)
+        Jr, Kr = np.zeros((n, n)), np.zeros((n, n))
+        rc.JK_direct(Jr, Kr, b, D, fp32_tau=1e-6, fp32_rec64=True)
+        assert b.stats()["quartets_fp32"] == st["quartets_fp32"]
+        assert np.abs(Jr - J).max() < 1e-8 and np.abs(Kr - K).max() < 1e-8
+        assert np.abs(Jr - Jm).max() > 0.0
+        # an unknown flag, or both FP64 Boys forms at once, is refused before any work
         from rchem_gb300 import _lib
 
         import ctypes as C
 
-        o = _lib.JKOpts(schwarz_tau=1e-12, fp32_tau=1e-6, where=_lib.HOST, emulated=4)
-        assert _lib.lib().rchem_jk_direct(b.handle, D.ctypes.data, Jb.ctypes.data, Kb.ctypes.data,
-                                          C.byref(o)) == _lib.RCHEM_ERR_INVALID
+        for bad in (8, 6):
+            o = _lib.JKOpts(schwarz_tau=1e-12, fp32_tau=1e-6, where=_lib.HOST, emulated=bad)
+            assert _lib.lib().rchem_jk_direct(b.handle, D.ctypes.data, Jb.ctypes.data, Kb.ctypes.data,
+                                              C.byref(o)) == _lib.RCHEM_ERR_INVALID
 
 
 def test_scf_energy_with_gpu_fock(gpu, oracle_mod):
