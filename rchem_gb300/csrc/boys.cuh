@@ -19,6 +19,11 @@
 // All F values come out multiplied by the caller's prefactor.
 // The FP64 grid index and the T < TMAX test use integer operations on T's bits,
 // so only the Taylor chains and one subtraction run on the (narrow) FP64 pipe.
+// boys_eval_u, the FP64 ERI kernels' form, removes the branch: below a switch
+// point (40 for L <= 1, 80 above, the FP64 table extended to T < 80) a lane
+// takes a Taylor row, above it a row of a power-law table, both chosen with
+// integer operations, so a warp whose lanes straddle the switch issues one
+// instruction stream.
 #pragma once
 #include <math.h>
 #include <string.h>
@@ -29,8 +34,8 @@
 
 // h = 1/128 (FP64) and 1/64 (FP32) are exact in binary, so T_i = i*h and
 // T_i - T are exact and the host tables are built at exactly the device's grid
-// points.  Rows i = 0..TMAX/h (nearest-point rounding reaches the last one just
-// below T = 40).
+// points.  Rows i = 0..T_end/h (nearest-point rounding reaches the last one
+// just below T_end: 80 for the FP64 table, 40 for the FP32 one).
 #define BOYS_MMAX 16     // F_0 .. F_16
 #define BOYS_NSUB (BOYS_MMAX + 2)  // sub-table 0 = e^{-T}, sub-table m+1 = F_m
 #define BOYS_TMAX 40.0
