@@ -463,9 +463,12 @@ static int upload(T **dst, const std::vector<T> &src, cudaStream_t s) {
 
 static const double kPrimCut = 1e-22;  // drop primitive pairs with exp(-ab/p |AB|^2) below this
 // ... and those whose prefactor bounds every primitive integral they enter below
-// 1e-16: |K_ab| max|K_cd| < kPrimRel (an integral of such a pair with any ket is
-// below about kPrimRel times its angular factors, far under the 1e-12 targets)
-static const double kPrimRel = 1e-16;
+// 1e-14: |K_ab| max|K_cd| < kPrimRel (an integral of such a pair with any ket is
+// below about kPrimRel times its angular factors, two orders under the 1e-12
+// Schwarz screen of whole quartets; against the oracle's unscreened primitives
+// the full (H2O)8 J and K are unchanged at 6.6e-13 from 1e-16, with 4.7 % fewer
+// primitive quartets in the (H2O)32 build)
+static const double kPrimRel = 1e-14;
 
 // distinct exponents of the table the kernels read (0: they compute the factors)
 static int pq_active(rchem_basis b) { return b->pq_on ? b->npq : 0; }
