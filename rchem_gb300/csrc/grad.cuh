@@ -50,12 +50,12 @@ struct GradArgs {
 };
 
 // E[i][j][t] of x_A^i x_B^j for i <= imax, j <= jmax (no exponential factor)
-template <typename R>
-__device__ __forceinline__ void gr_herm(int imax, int jmax, R PA, R AB, R ohp, R (*E)[GR_NI][GR_NT]) {
+template <typename R, int NJ = GR_NI, int NT = GR_NT>
+__device__ __forceinline__ void gr_herm(int imax, int jmax, R PA, R AB, R ohp, R (*E)[NJ][NT]) {
     const R PB = PA + AB;  // P - B = (P - A) + (A - B)
     for (int i = 0; i <= imax; ++i)
         for (int j = 0; j <= jmax; ++j)
-            for (int t = 0; t < GR_NT; ++t) E[i][j][t] = R(0);
+            for (int t = 0; t < NT; ++t) E[i][j][t] = R(0);
     E[0][0][0] = R(1);
     for (int i = 0; i <= imax; ++i) {
         if (i > 0)
@@ -75,10 +75,13 @@ __device__ __forceinline__ void gr_herm(int imax, int jmax, R PA, R AB, R ohp, R
     }
 }
 
-template <typename R>
+// R^0_tuv for t+u+v <= L (md_tuv order) into out, NR >= (L+1)(L+2)(L+3)/6
+// values; the recursion alternates between out and one scratch table, starting
+// in the one that makes the last pass land in out
+template <typename R, int NR = GR_NR>
 __device__ __forceinline__ void gr_R(int L, R a, R X, R Y, R Z, const R *F, R *out) {
-    R buf[2][GR_NR];
-    R *cur = buf[0], *nxt = buf[1];
+    R buf[NR];
+    R *cur = (L & 1) ? buf : out, *nxt = (L & 1) ? out : buf;
     const R m2a = R(-2) * a;
     R pw[GR_LMAX + 1];
     pw[0] = R(1);
@@ -101,8 +104,6 @@ __device__ __forceinline__ void gr_R(int L, R a, R X, R Y, R Z, const R *F, R *o
         cur = nxt;
         nxt = tmp;
     }
-    const int cnt = (L + 1) * (L + 2) * (L + 3) / 6;
-    for (int i = 0; i < cnt; ++i) out[i] = cur[i];
 }
 
 __device__ __forceinline__ void gr_comp(int l, int k, int *lmn) {
@@ -168,8 +169,8 @@ __device__ __forceinline__ df64 gt_narrow(double x, df64 *) { return df64(x); }
 // Hermite index with t+u+v <= bmax (stored compactly in md_tuv order): the ket of one component
 // contracted with the Coulomb integrals once, reused by every bra component.  The sum is
 // nested one direction at a time (one FMA per term instead of a product and an FMA).
-template <typename T>
-__device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], const int *c, const int *d, const T *R,
+template <typename T, int NJ = GR_NI, int NT = GR_NT>
+__device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][NJ][NT], const int *c, const int *d, const T *R,
                                         int bmax, T *Z) {
     const T *ex = Ek[0][c[0]][d[0]], *ey = Ek[1][c[1]][d[1]], *ez = Ek[2][c[2]][d[2]];
     const int nx = c[0] + d[0], ny = c[1] + d[1], nz = c[2] + d[2];
@@ -191,6 +192,14 @@ __device__ __forceinline__ void gr_zvec(const T (*Ek)[GR_NI][GR_NI][GR_NT], cons
 }
 
 #define GR_ZN 56  // (t,u,v) with t+u+v <= la+lb+1 <= 5
+#define GR_ZB 35  // (t,u,v) with t+u+v <= la+lb <= 4
+// the per-lane kernel's classes: total L + 1 <= 7 (the two largest classes run
+// the warp-cooperative kernel), so its R table holds t+u+v <= 7
+#define GR_RT_MAXL1 7
+#define GR_RT_NR 120
+// ... and its ket pairs have l_d <= 1: ket Hermite tables [i <= 3][j <= 1][t <= 4]
+#define GR_RT_NJ 2
+#define GR_RT_NTK 5
 
 #define GR_MAXC4 1296  // components of a (dd|dd) quartet
 
@@ -270,8 +279,8 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
     const R *btab = GradPrim<R>::boys(g);
     R gA[3] = {R(0), R(0), R(0)}, gB[3] = {R(0), R(0), R(0)}, gC[3] = {R(0), R(0), R(0)};
     const int L1 = la + lb + lc + ld + 1;
-    R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_NI][GR_NT], Rt[GR_NR], F[GR_LMAX + 1];
-    R Z0[GR_ZN], Zp[3][GR_ZN], Zm[3][GR_ZN], H0[GR_ZN];
+    R Eb[3][GR_NI][GR_NI][GR_NT], Ek[3][GR_NI][GR_RT_NJ][GR_RT_NTK], Rt[GR_RT_NR], F[GR_RT_MAXL1 + 1];
+    R Z0[GR_ZN], Zp[3][GR_ZB], Zm[3][GR_ZB], H0[GR_ZB];
     // work units: (primitive quartet, ket component pair); the G lanes split them
     // (a d-shell quartet's few primitive quartets alone would leave lanes idle)
     const int nk = kp.npp, ntot = bp.npp * nk, ncd = nc * nd;
@@ -297,13 +306,13 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
             const R X = Pc[0] - Qc[0], Y = Pc[1] - Qc[1], Zc = Pc[2] - Qc[2];
             const R T = rho * (X * X + Y * Y + Zc * Zc);
             boys_eval_rt<R>(L1, T, Kab * Kcd * rs, btab, F);
-            gr_R<R>(L1, rho, X, Y, Zc, F, Rt);
+            gr_R<R, GR_RT_NR>(L1, rho, X, Y, Zc, F, Rt);
             for (int dd = 0; dd < 3; ++dd) {
                 gr_herm<R>(la + 1, lb + 1, PA[dd], AB[dd], ohp, Eb[dd]);
-                gr_herm<R>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
+                gr_herm<R, GR_RT_NJ, GR_RT_NTK>(lc + 1, ld, QC[dd], CD[dd], ohq, Ek[dd]);
                 for (int i = 0; i <= lc + 1; ++i)  // ket sign (-1)^t folded in
                     for (int j = 0; j <= ld; ++j)
-                        for (int t = 1; t < GR_NT; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
+                        for (int t = 1; t < GR_RT_NTK; t += 2) Ek[dd][i][j][t] = -Ek[dd][i][j][t];
             }
         }
         const int kc = kcd / nd, kd = kcd - kc * nd;
@@ -312,14 +321,14 @@ __global__ void __launch_bounds__(64) k_grad2e_rt(GradArgs g) {
         const int l_ = kp.aoA + kc, s_ = kp.aoB + kd;
         const double Dls = Dg[l_ * n + s_], wcd = deg * nC[kc] * nD[kd];
         // ket contracted with R: unshifted (the bra may be shifted by one) and C-shifted
-        gr_zvec<R>(Ek, Cc, cD[kd], Rt, la + lb + 1, Z0);
+        gr_zvec<R, GR_RT_NJ, GR_RT_NTK>(Ek, Cc, cD[kd], Rt, la + lb + 1, Z0);
         for (int x = 0; x < 3; ++x) {
             int s[3] = {Cc[0], Cc[1], Cc[2]};
             s[x] += 1;
-            gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
+            gr_zvec<R, GR_RT_NJ, GR_RT_NTK>(Ek, s, cD[kd], Rt, la + lb, Zp[x]);
             if (Cc[x] > 0) {
                 s[x] -= 2;
-                gr_zvec<R>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
+                gr_zvec<R, GR_RT_NJ, GR_RT_NTK>(Ek, s, cD[kd], Rt, la + lb, Zm[x]);
             }
         }
         // centre C through the bra Hermite density H0_tuv = sum_ab Gamma_ab E^{ab}_tuv

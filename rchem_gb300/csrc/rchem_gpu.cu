@@ -1515,8 +1515,9 @@ static int plan_gradient(rchem_basis b, double tau, double tau32) {
             // warp-cooperative kernel, one quartet per warp; the smaller ones keep
             // whole quartets per lane group, whose lanes the cooperative kernel
             // could not fill
-            const bool wc = !sp && (long long)ncart(gb.la) * ncart(gb.lb) * ncart(gk.la) * ncart(gk.lb) >=
-                                       grad_wc_min();
+            const bool wc = !sp && ((long long)ncart(gb.la) * ncart(gb.lb) * ncart(gk.la) * ncart(gk.lb) >=
+                                        grad_wc_min() ||
+                                    L + 1 > GR_RT_MAXL1 || gk.lb >= GR_RT_NJ);  // the per-lane kernel's table sizes
             if (wc) lg = 5;
             const long long work = (long long)(L + 2) * (L + 2) * (L + 2);  // ~ Hermite work per primitive quartet
             for (int prec = 0; prec < 2; ++prec) {
