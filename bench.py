@@ -632,6 +632,10 @@ def main():
     # ---- precision forms (same timing), SCF against the FP64 SCF ----------
     forms = {}
     if rank == 0:
+        # the first FP64 eigensolve of a process creates cuSOLVER's handle and
+        # workspaces (about a second): do it before the SCF timings
+        torch.linalg.eigh(torch.eye(n, dtype=torch.float64, device="cuda"))
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         r64 = rc.scf.rhf(b, thresh_e=1e-10)
         torch.cuda.synchronize()
