@@ -145,10 +145,11 @@ template <> struct Tabs<float> {
     static __device__ __forceinline__ void ab(const ShellPair &s, float *v) { v[0] = s.AB32[0]; v[1] = s.AB32[1]; v[2] = s.AB32[2]; }
 };
 
-// Scaled Boys values F[0..L] of one primitive quartet.  With a.f32_boys64 the
-// FP32 kernels evaluate the function and its downward recursion in FP64 from
-// the FP32 argument and prefactor, and round the results to FP32.
-// The Boys function.  FP64 (and the FP64 Boys function of the FP32 quartets
+// Scaled Boys values F[0..L] of one primitive quartet.  The FP32 kernels take
+// them in FP32 (a.f32_boys64 = 0), entirely in FP64 from the FP32 argument and
+// prefactor (1), or with FP32 table values and the recursion over m in FP64
+// (2), rounding the results to FP32.
+// FP64 (and the FP64 Boys function of the FP32 quartets
 // with f32_boys64 = 1) runs boys_eval_u, one instruction stream for T on either
 // side of the Taylor range: those kernels are bound by the narrow FP64 pipe,
 // where a diverged warp issuing both branches cost 12 % of the build.  The
@@ -180,7 +181,6 @@ __device__ __forceinline__ void eri_boys(const EriArgs &a, R T, R pref, const R 
         boys_eval<L, R, SCALE>(T, pref, btab, F);
     }
 }
-
 
 template <int LA, int LB, int LC, int LD, typename R, int EPI>
 __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
