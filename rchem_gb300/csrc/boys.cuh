@@ -374,12 +374,13 @@ inline void boys_fill_far(double *far) {
         for (int par = 0; par < 2; ++par) {
             const long double C = par ? C0 * powl(2.0L, -al) : C0;
             for (int j = 0; j < BOYS_FAR_ROWS; ++j) {
-                const long double g = 1.0L + (long double)j / BOYS_FAR_R;
-                long double a[7], rf = 1.0L, fk = 1.0L;
+                const long double g = 1.0L + (long double)j / BOYS_FAR_R, ig = 1.0L / g;
+                long double a[7], rf = 1.0L, fk = 1.0L, gp = powl(g, -al);
                 for (int q = 0; q < 7; ++q) {
-                    a[q] = C * rf * powl(g, -al - q) / fk;  // C (al)_q g^-(al+q) / q!
+                    a[q] = C * rf * gp / fk;  // C (al)_q g^-(al+q) / q!
                     rf *= al + q;
                     fk *= q + 1;
+                    gp *= ig;
                 }
                 const long double b[5] = {a[0] + d6 / 32 * a[6], a[1] - 5.0L / 16 * d4 * a[5],
                                           a[2] - 9.0L / 16 * d4 * a[6], a[3] + 5.0L / 4 * d2 * a[5],
