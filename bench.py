@@ -669,8 +669,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "config": cfg,
-        "tuning": "rchem_autotune per class list before timing (lanes per quartet; warp-cooperative kernel for "
-                  "the classes of total angular momentum >= 4)",
+        "tuning": "rchem_autotune per class list before timing (lanes per quartet; warp-cooperative kernel with "
+                  "32, 16 or 8 lanes per quartet for the classes of total angular momentum >= 4: tile shape 0, -16, "
+                  "-8)",
         "eris_per_s": st64["eris_fp64"] / (ms * 1e-3),
         "forms": forms,
         "e2e": {"value": e2e, "unit": "builds/s", "h2d_bytes_per_step": n * n * 8,

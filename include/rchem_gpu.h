@@ -255,10 +255,14 @@ int rchem_rhf(rchem_basis b, const rchem_scf_opts *opts, const int *nocc, double
  * (no counterpart in the reference): for every integral class list (21
  * classes x {FP64, FP32}) time the list alone under each candidate number of
  * lanes per shell quartet, and for the classes with l_a+l_b+l_c+l_d >= 4 also
- * the warp-cooperative kernel (one quartet per warp, intermediates in shared
- * memory), and keep the fastest.  chosen (may be NULL) receives 2*21 ints: the
- * minimum primitive quartets per lane picked for each list (2^30 = never split,
- * 0 = the warp-cooperative kernel).  Later rchem_jk_direct calls use the choices.
+ * the warp-cooperative kernel (32, 16 or 8 lanes per quartet, so 1, 2 or 4
+ * quartets per warp, intermediates in shared memory), and keep the fastest;
+ * then, since the lists run concurrently in a build, settle each list of those
+ * classes (longest first) on the shape that gives the fastest whole build.
+ * chosen (may be NULL) receives 2*21 ints: the minimum primitive quartets per
+ * lane picked for each list (2^30 = never split), or 0, -16, -8 for the
+ * warp-cooperative kernel with 32, 16, 8 lanes per quartet.  Later
+ * rchem_jk_direct calls use the choices.
  */
 int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen);
 
@@ -267,8 +271,9 @@ int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen);
  * overrides rchem_autotune for that list): class index cls 0..20 in the order
  * of the generated class table (s,p,d pairs with l_a >= l_b), prec 0 = FP64 /
  * emulated list, 1 = FP32 list; ppl = minimum primitive quartets per lane, or
- * 0 for the warp-cooperative kernel (classes with l_a+l_b+l_c+l_d >= 4 only,
- * else RCHEM_ERR_UNSUPPORTED).  The next Fock build replans.
+ * 0, -16, -8 for the warp-cooperative kernel with 32, 16, 8 lanes per quartet
+ * (classes with l_a+l_b+l_c+l_d >= 4 only, else RCHEM_ERR_UNSUPPORTED; other
+ * negative values RCHEM_ERR_INVALID).  The next Fock build replans.
  */
 int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl);
 

@@ -129,7 +129,8 @@ class Basis:
 
     def autotune(self, schwarz_tau=1e-12, fp32_tau=0.0, emulated=False, fp32_boys64=False, fp32_rec64=False):
         """Pick the Fock build's tile shape per integral class for this basis
-        (rchem_autotune); returns {(class, precision): min primitive quartets per lane}."""
+        (rchem_autotune); returns {(class, precision): min primitive quartets per lane,
+        or 0 / -16 / -8 for the warp-cooperative kernel with 32 / 16 / 8 lanes per quartet}."""
         import numpy as _np
 
         chosen = _np.zeros(2 * 21, dtype=_np.int32)
@@ -140,7 +141,8 @@ class Basis:
 
     def set_tile_shape(self, cls: int, prec: int, ppl: int):
         """Fix one class list's tile shape (rchem_set_tile_shape): ppl = minimum
-        primitive quartets per lane, 0 = the warp-cooperative kernel."""
+        primitive quartets per lane; 0, -16, -8 = the warp-cooperative kernel with
+        32, 16, 8 lanes per quartet."""
         _lib.check(_lib.lib().rchem_set_tile_shape(self.handle, cls, prec, ppl))
 
     def set_exponent_table(self, on: bool):

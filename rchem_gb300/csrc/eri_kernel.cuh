@@ -429,6 +429,12 @@ __global__ void __launch_bounds__(128) eri_class_kernel(EriArgs a) {
 // reused from one level to the next, so a warp's array holds the live values
 // of a level, not the whole DAG; terms are sorted by branch shape inside a
 // level so lanes mostly agree on it.
+// With QL = 16 or 8 lanes per quartet a warp runs 2 or 4 quartets of the list
+// side by side, each in its own array: the per-primitive-quartet set-up and
+// Boys function, which every lane of a quartet evaluates, then cost a warp
+// instruction per 2 or 4 quartets, and levels and contractions smaller than 32
+// terms leave fewer lanes idle (the classes whose shell quartets have one or
+// two primitive quartets).
 template <int LA, int LB, int LC, int LD> struct EriProg;
 
 #define WC_U 4  // independent recurrence terms per lane and pass
@@ -440,10 +446,15 @@ template <int LA, int LB, int LC, int LD> struct EriProg;
 #define RCHEM_BLOCK_SMEM (227 * 1024)
 #define RCHEM_WC_MAX_WARPS 16
 
-template <int LA, int LB, int LC, int LD, typename R>
+template <int LA, int LB, int LC, int LD, typename R, int QL = 32>
 struct WcShape {
     using P = EriProg<LA, LB, LC, LD>;
-    static constexpr int PER_WARP = P::SCR;  // elements of R
+    static_assert(QL == 32 || QL == 16 || QL == 8, "8, 16 or 32 lanes per quartet");
+    static constexpr int QW = 32 / QL;  // quartets per warp
+    // one quartet's array (elements of R); with several quartets per warp the
+    // stride is 4 mod 16 elements, so the arrays start on different banks
+    static constexpr int STRIDE = QW == 1 ? P::SCR : P::SCR + (20 - P::SCR % 16) % 16;
+    static constexpr int PER_WARP = QW * STRIDE;
     static constexpr size_t BYTES = (size_t)PER_WARP * sizeof(R);
     // warps per block that keep the most warps resident on an SM (ties: the
     // larger block, so a block's warps spread over the SM's four schedulers)
@@ -468,9 +479,10 @@ struct WcShape {
 };
 
 // lanes per target of a warp-cooperative contraction of ntg sums of nl terms
-constexpr int wc_split(int ntg, int nl) {
+// over the ql lanes of a quartet
+constexpr int wc_split(int ntg, int nl, int ql) {
     int p = 1;
-    while (2 * p * ntg <= 32 && 2 * p <= nl) p *= 2;
+    while (2 * p * ntg <= ql && 2 * p <= nl) p *= 2;
     return p;
 }
 
@@ -481,20 +493,25 @@ __device__ __forceinline__ R wc_sel4(int n, const R *v) {  // v[0..3] = 1..4 tim
     return n == 1 ? v[0] : (n == 2 ? v[1] : (n == 3 ? v[2] : v[3]));
 }
 
-template <int LA, int LB, int LC, int LD, typename R, int EPI = EPI_JK>
+template <int LA, int LB, int LC, int LD, typename R, int EPI = EPI_JK, int QL = 32>
 __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 registers
     using C = EriClass<LA, LB, LC, LD>;
     using P = EriProg<LA, LB, LC, LD>;
-    using W = WcShape<LA, LB, LC, LD, R>;
-    constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, L = C::L;
+    using W = WcShape<LA, LB, LC, LD, R, QL>;
+    static_assert(QL == 32 || EPI == EPI_JK, "the ERI-store and Schwarz epilogues run one quartet per warp");
+    constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, L = C::L, QW = W::QW;
     extern __shared__ __align__(16) unsigned char wc_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    // the warp's array: accumulators [0, NT), Boys values and VRR terms above
-    // them; after the HRR the integrals (ab|cd) at [OUTB, OUTB + NOUT)
-    R *S = reinterpret_cast<R *>(wc_smem) + wib * W::PER_WARP;
+    const int sub = lane & (QL - 1), qs = lane / QL;  // lane within the quartet, quartet within the warp
+    // the quartet's array: accumulators [0, NT), Boys values and VRR terms
+    // above them; after the HRR the integrals (ab|cd) in their own slots
+    R *S = reinterpret_cast<R *>(wc_smem) + wib * W::PER_WARP + qs * W::STRIDE;
     const int w = blockIdx.x * W::WARPS + wib;
-    if (w >= a.ntasks) return;  // warp-uniform
-    const EriTask tk = a.tasks[w];
+    if (w * QW >= a.ntasks) return;  // warp-uniform
+    // quartets past the end of the list (the last warp's) run on the list's
+    // last task with no primitive quartets and no stores
+    const bool valid = w * QW + qs < a.ntasks;
+    const EriTask tk = a.tasks[valid ? w * QW + qs : a.ntasks - 1];
     int sg = tk.seg, off = tk.off;
     EriSeg seg = a.segs[sg];
     while (off >= seg.count) {
@@ -503,18 +520,25 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
     }
     const int bidx = seg.bra, kidx = seg.ket0 + off;
     const ShellPair bp = a.pairs[bidx], kp = a.pairs[kidx];
-    for (int k = lane; k < P::NT; k += 32) S[k] = R(0);
+    for (int k = sub; k < P::NT; k += QL) S[k] = R(0);
     const R *btab = Tabs<R>::boys(a);
     const uint4 *vprog = P::vrr();
     const int *vlev = P::vrrlv();
-    const int nk = kp.npp, ntot = bp.npp * nk;
-    for (int tq = 0; tq < ntot; ++tq) {
-        const int ia = tq / nk, ic = tq - ia * nk;
-        R p, ohp, Pc[3], PA[3], Kab, q, ohq, Qc[3], QC[3], Kcd;
-        PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, Pc, PA, Kab);
-        PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Qc, QC, Kcd);
-        R rs, ipq, rho, qi_, pi_;
-        pq_factors<R>(a, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi_, pi_);
+    const int nk = kp.npp, ntot = valid ? bp.npp * nk : 0;
+    int nmax = ntot;  // the warp runs its quartets' primitive loops side by side
+    if constexpr (QW > 1) nmax = __reduce_max_sync(0xffffffffu, ntot);
+    for (int tq = 0; tq < nmax; ++tq) {
+        // a quartet past its last primitive quartet computes on zeros and stores nothing
+        const bool live = tq < ntot;
+        R p = R(0), ohp = R(0), Pc[3] = {R(0), R(0), R(0)}, PA[3] = {R(0), R(0), R(0)}, Kab = R(0);
+        R q = R(0), ohq = R(0), Qc[3] = {R(0), R(0), R(0)}, QC[3] = {R(0), R(0), R(0)}, Kcd = R(0);
+        R rs = R(0), ipq = R(0), rho = R(0), qi_ = R(0), pi_ = R(0);
+        if (QW == 1 || live) {
+            const int ia = tq / nk, ic = tq - ia * nk;
+            PrimLoad<R>::get(a, bp.prim0 + ia, p, ohp, Pc, PA, Kab);
+            PrimLoad<R>::get(a, kp.prim0 + ic, q, ohq, Qc, QC, Kcd);
+            pq_factors<R>(a, bp.prim0 + ia, kp.prim0 + ic, p, q, rs, ipq, rho, qi_, pi_);
+        }
         const R PQx = Pc[0] - Qc[0], PQy = Pc[1] - Qc[1], PQz = Pc[2] - Qc[2];
         const R T = rho * (PQx * PQx + PQy * PQy + PQz * PQz);
         R F[L + 1];
@@ -527,7 +551,7 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
         __syncwarp();  // the previous primitive quartet's terms have been read
 #pragma unroll
         for (int m = 0; m <= L; ++m)
-            if (lane == m) S[P::NT + m] = F[m];
+            if ((m & (QL - 1)) == sub) S[P::NT + m] = F[m];
         __syncwarp();
         // one term: X a + Y b [+ n1 c (c_ - rho d)] [+ n2 ohpq g]
         auto term = [&](const unsigned wd, R ta, R tb, R tc, R td, R tg) {
@@ -546,7 +570,7 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
             uint4 o[NS];
             R ta[NS], tb[NS], tc[NS], td[NS], tg[NS];
 #pragma unroll
-            for (int u = 0; u < NS; ++u) o[u] = t + 32 * u < e ? __ldg(vprog + t + 32 * u) : make_uint4(0, 0, 0, 0);
+            for (int u = 0; u < NS; ++u) o[u] = t + QL * u < e ? __ldg(vprog + t + QL * u) : make_uint4(0, 0, 0, 0);
 #pragma unroll
             for (int u = 0; u < NS; ++u) {
                 const unsigned n1 = (o[u].w >> 3) & 7, n2 = (o[u].w >> 6) & 7;
@@ -559,7 +583,7 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
 #pragma unroll
             for (int u = 0; u < NS; ++u) {
                 const R v = term(o[u].w, ta[u], tb[u], tc[u], td[u], tg[u]);
-                if (t + 32 * u < e) {
+                if (t + QL * u < e && (QW == 1 || live)) {
                     const unsigned dest = o[u].x & 0xffff, tg1 = o[u].w >> 9;
                     if (dest != 0xffffu) S[dest] = v;
                     if (tg1) S[tg1 - 1] += v;  // a target: into its contraction accumulator
@@ -570,12 +594,12 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
             const int e = __ldg(vlev + lv + 1);
             // passes over the level (warp-uniform): each takes only the term slots
             // that hold a term for some lane, so a small level's empty slots cost nothing
-            for (int b = __ldg(vlev + lv); b < e; b += 32 * WC_U) {
-                const int ns = min(WC_U, (e - b + 31) >> 5);
-                if (ns == 4) vpass(b + lane, e, std::integral_constant<int, 4>{});
-                else if (ns == 3) vpass(b + lane, e, std::integral_constant<int, 3>{});
-                else if (ns == 2) vpass(b + lane, e, std::integral_constant<int, 2>{});
-                else vpass(b + lane, e, std::integral_constant<int, 1>{});
+            for (int b = __ldg(vlev + lv); b < e; b += QL * WC_U) {
+                const int ns = min(WC_U, (e - b + QL - 1) / QL);
+                if (ns == 4) vpass(b + sub, e, std::integral_constant<int, 4>{});
+                else if (ns == 3) vpass(b + sub, e, std::integral_constant<int, 3>{});
+                else if (ns == 2) vpass(b + sub, e, std::integral_constant<int, 2>{});
+                else vpass(b + sub, e, std::integral_constant<int, 1>{});
             }
             __syncwarp();
         }
@@ -595,7 +619,7 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
         uint2 o[NS];
         R tx[NS], ty[NS];
 #pragma unroll
-        for (int u = 0; u < NS; ++u) o[u] = t + 32 * u < e ? __ldg(hprog + t + 32 * u) : make_uint2(0, 0);
+        for (int u = 0; u < NS; ++u) o[u] = t + QL * u < e ? __ldg(hprog + t + QL * u) : make_uint2(0, 0);
 #pragma unroll
         for (int u = 0; u < NS; ++u) {
             tx[u] = S[o[u].x >> 16];
@@ -604,24 +628,24 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
 #pragma unroll
         for (int u = 0; u < NS; ++u) {
             const R v = rchem_fma(hcoef(o[u]), ty[u], tx[u]);
-            if (t + 32 * u < e) S[o[u].x & 0xffff] = v;
+            if (t + QL * u < e) S[o[u].x & 0xffff] = v;
         }
     };
     for (int lv = 0; lv < P::NHL; ++lv) {
         const int e = __ldg(hlev + lv + 1);
-        for (int b = __ldg(hlev + lv); b < e; b += 32 * WC_U) {
-            const int ns = min(WC_U, (e - b + 31) >> 5);
-            if (ns == 4) hpass(b + lane, e, std::integral_constant<int, 4>{});
-            else if (ns == 3) hpass(b + lane, e, std::integral_constant<int, 3>{});
-            else if (ns == 2) hpass(b + lane, e, std::integral_constant<int, 2>{});
-            else hpass(b + lane, e, std::integral_constant<int, 1>{});
+        for (int b = __ldg(hlev + lv); b < e; b += QL * WC_U) {
+            const int ns = min(WC_U, (e - b + QL - 1) / QL);
+            if (ns == 4) hpass(b + sub, e, std::integral_constant<int, 4>{});
+            else if (ns == 3) hpass(b + sub, e, std::integral_constant<int, 3>{});
+            else if (ns == 2) hpass(b + sub, e, std::integral_constant<int, 2>{});
+            else hpass(b + sub, e, std::integral_constant<int, 1>{});
         }
         __syncwarp();
     }
     // the integrals (ab|cd) scaled by their component norms, in place (every
     // output has a slot of its own); A(k) reads integral k
     const unsigned short *oslot = P::out();
-    for (int k = lane; k < P::NOUT; k += 32) {
+    for (int k = sub; k < P::NOUT; k += QL) {
         const int sk = __ldg(oslot + k);
         S[sk] = R(__ldg(P::onorm() + k)) * S[sk];
     }
@@ -651,18 +675,18 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
     // degeneracy-weighted 8-fold scatter: each of the six contractions is a
     // set of NTG target sums of NL terms; SPL lanes share a target (each a
     // strided part of its sum, then a shuffle reduction), SPL the largest power
-    // of two with NTG SPL <= 32 and SPL <= NL, so a contraction with few
-    // targets still keeps the lanes busy
+    // of two with NTG SPL <= QL and SPL <= NL, so a contraction with few
+    // targets still keeps the quartet's lanes busy
     const int kK = -(bp.diag + kp.diag + (bidx == kidx ? 1 : 0)), kJ = kK + 1;
     const int n = bp.mn, mo = bp.moff;
     const int m0 = bp.aoA, n0 = bp.aoB, l0 = kp.aoA, s0 = kp.aoB;
 #define WIDX(ia, ib, ic, id) ((((ia) * NB + (ib)) * NC + (ic)) * ND + (id))
     auto contract = [&](auto ntg_c, auto nl_c, double *M, int kw, auto tgt, auto term) {
         constexpr int NTG = decltype(ntg_c)::value, NL = decltype(nl_c)::value;
-        constexpr int SPL = wc_split(NTG, NL), PER = 32 / SPL;
-        const int sl = lane & (SPL - 1);
+        constexpr int SPL = wc_split(NTG, NL, QL), PER = QL / SPL;
+        const int sl = sub & (SPL - 1);
         for (int t0 = 0; t0 < NTG; t0 += PER) {
-            const int t = t0 + lane / SPL;
+            const int t = t0 + sub / SPL;
             R sum = R(0);
             if (t < NTG)
                 for (int i = sl; i < NL; i += SPL) {
@@ -672,7 +696,7 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
                 }
 #pragma unroll
             for (int o = SPL >> 1; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-            if (t < NTG && sl == 0) atomicAdd(M + tgt(t), jk_term(sum, kw));
+            if (valid && t < NTG && sl == 0) atomicAdd(M + tgt(t), jk_term(sum, kw));
         }
     };
     using std::integral_constant;
@@ -729,32 +753,48 @@ __global__ void __launch_bounds__(256, 2) eri_wc_kernel(EriArgs a) {  // <= 128 
 
 // Raise the shared-memory limit of the warp-cooperative kernels (once per
 // device, outside any stream capture).
+template <int LA, int LB, int LC, int LD, typename R, int EPI, int QL>
+cudaError_t wc_set_smem() {
+    return cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, R, EPI, QL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)WcShape<LA, LB, LC, LD, R, QL>::SMEM);
+}
+template <int LA, int LB, int LC, int LD, typename R>
+cudaError_t wc_set_smem_jk() {
+    cudaError_t e = wc_set_smem<LA, LB, LC, LD, R, EPI_JK, 32>();
+    if (e == cudaSuccess) e = wc_set_smem<LA, LB, LC, LD, R, EPI_JK, 16>();
+    if (e == cudaSuccess) e = wc_set_smem<LA, LB, LC, LD, R, EPI_JK, 8>();
+    return e;
+}
+
 template <int LA, int LB, int LC, int LD>
 cudaError_t prepare_eri_class() {
     if constexpr (EriClass<LA, LB, LC, LD>::WC) {
-        cudaError_t e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)WcShape<LA, LB, LC, LD, double>::SMEM);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, df64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)WcShape<LA, LB, LC, LD, df64>::SMEM);
+        cudaError_t e = wc_set_smem_jk<LA, LB, LC, LD, double>();
+        if (e == cudaSuccess) e = wc_set_smem_jk<LA, LB, LC, LD, df64>();
+        if (e == cudaSuccess) e = wc_set_smem_jk<LA, LB, LC, LD, float>();
         if (e != cudaSuccess) return e;
         if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
-            e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double, EPI_STORE>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)WcShape<LA, LB, LC, LD, double>::SMEM);
+            e = wc_set_smem<LA, LB, LC, LD, double, EPI_STORE, 32>();
             if (e != cudaSuccess) return e;
-            if constexpr (LA == LC && LB == LD) {
-                e = cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, double, EPI_DIAG>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)WcShape<LA, LB, LC, LD, double>::SMEM);
-                if (e != cudaSuccess) return e;
-            }
+            if constexpr (LA == LC && LB == LD) e = wc_set_smem<LA, LB, LC, LD, double, EPI_DIAG, 32>();
         }
-        return cudaFuncSetAttribute(eri_wc_kernel<LA, LB, LC, LD, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)WcShape<LA, LB, LC, LD, float>::SMEM);
+        return e;
     }
     return cudaSuccess;
+}
+
+// A warp-cooperative list: ceil(ntasks / QW) warps of QW quartets each.
+template <int LA, int LB, int LC, int LD, typename R, int EPI, int QL>
+void launch_wc(const EriArgs &a, cudaStream_t s) {
+    using W = WcShape<LA, LB, LC, LD, R, QL>;
+    const int warps = (a.ntasks + W::QW - 1) / W::QW;
+    eri_wc_kernel<LA, LB, LC, LD, R, EPI, QL><<<(warps + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
+}
+template <int LA, int LB, int LC, int LD, typename R>
+void launch_wc_jk(const EriArgs &a, cudaStream_t s) {
+    if (a.wc == 8) launch_wc<LA, LB, LC, LD, R, EPI_JK, 8>(a, s);
+    else if (a.wc == 16) launch_wc<LA, LB, LC, LD, R, EPI_JK, 16>(a, s);
+    else launch_wc<LA, LB, LC, LD, R, EPI_JK, 32>(a, s);
 }
 
 template <int LA, int LB, int LC, int LD>
@@ -766,33 +806,20 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
     if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
         // the largest classes exist only as warp-cooperative kernels (one quartet per
         // task in every plan); their straight-line code would take minutes to compile
-        using W = WcShape<LA, LB, LC, LD, double>;
-        const int wb = (a.ntasks + W::WARPS - 1) / W::WARPS;
         if (epi == EPI_STORE) {
-            eri_wc_kernel<LA, LB, LC, LD, double, EPI_STORE><<<wb, 32 * W::WARPS, W::SMEM, s>>>(a);
+            launch_wc<LA, LB, LC, LD, double, EPI_STORE, 32>(a, s);
             return;
         }
         if (epi == EPI_DIAG) {
-            if constexpr (LA == LC && LB == LD)
-                eri_wc_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<wb, 32 * W::WARPS, W::SMEM, s>>>(a);
+            if constexpr (LA == LC && LB == LD) launch_wc<LA, LB, LC, LD, double, EPI_DIAG, 32>(a, s);
             return;
         }
     }
     if constexpr (EriClass<LA, LB, LC, LD>::WC) {
         if (epi == EPI_JK && (a.wc || EriClass<LA, LB, LC, LD>::WC_ONLY)) {  // one quartet per task
-            if (prec == 1) {
-                using W = WcShape<LA, LB, LC, LD, float>;
-                eri_wc_kernel<LA, LB, LC, LD, float>
-                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
-            } else if (prec == 2) {
-                using W = WcShape<LA, LB, LC, LD, df64>;
-                eri_wc_kernel<LA, LB, LC, LD, df64>
-                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
-            } else {
-                using W = WcShape<LA, LB, LC, LD, double>;
-                eri_wc_kernel<LA, LB, LC, LD, double>
-                    <<<(a.ntasks + W::WARPS - 1) / W::WARPS, 32 * W::WARPS, W::SMEM, s>>>(a);
-            }
+            if (prec == 1) launch_wc_jk<LA, LB, LC, LD, float>(a, s);
+            else if (prec == 2) launch_wc_jk<LA, LB, LC, LD, df64>(a, s);
+            else launch_wc_jk<LA, LB, LC, LD, double>(a, s);
             return;
         }
     }

@@ -400,7 +400,7 @@ struct rchem_basis_s {
     // tile shape per class list: lanes share a quartet while each keeps at
     // least this many primitive quartets (rchem_autotune chooses them)
     int ppl[RCHEM_NCLASS][2];
-    int wc[RCHEM_NCLASS][2];  // large classes: warp-cooperative J/K kernel (chosen by the autotuner)
+    int wc[RCHEM_NCLASS][2];  // large classes: warp-cooperative J/K kernel, lanes per quartet (0: not; the autotuner)
     // concurrent class kernels: fork/join over auxiliary streams
     static const int NAUX = 16;
     cudaStream_t aux[NAUX] = {};
@@ -1398,6 +1398,32 @@ static int record_build(rchem_basis b, bool any32, bool emul, int boys64 = 0) {
     return RCHEM_OK;
 }
 
+// The captured Fock build of the current plan and arithmetic flags, captured
+// again when either has changed since the last capture.
+static int ensure_graph(rchem_basis b, bool any32, int flags) {
+    if (b->graph_version == b->plan_version && b->graph_emul == flags && b->graph) return RCHEM_OK;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_version = -1;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = record_build(b, any32, (flags & RCHEM_JK_EMULATED) != 0, f32_boys_mode(flags));
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc != RCHEM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "capturing the Fock build: %s", cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "instantiating the Fock build: %s", cudaGetErrorString(ei));
+    b->graph_version = b->plan_version;
+    b->graph_emul = flags;
+    return RCHEM_OK;
+}
+
+static bool stream_capturable(rchem_basis b) { return b->stream != nullptr && b->stream != cudaStreamLegacy; }
+
 static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, const rchem_jk_opts *opts, int part,
                           int nparts) {
     if (!b || !D || !J || !K) return set_err(RCHEM_ERR_INVALID, "null argument");
@@ -1420,30 +1446,9 @@ static int jk_direct_impl(rchem_basis b, const double *D, double *J, double *K, 
     for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
     // replay the captured build; capture it again when the plan has changed.
     // The legacy default stream cannot be captured: run the launches directly there.
-    const bool emul = (o.emulated & RCHEM_JK_EMULATED) != 0;
-    const int boys64 = f32_boys_mode(o.emulated);
-    const bool capturable = b->stream != nullptr && b->stream != cudaStreamLegacy;
-    if (!capturable) {
-        CKR(record_build(b, any32, emul, boys64));
-    } else if (b->graph_version != b->plan_version || b->graph_emul != o.emulated) {
-        if (b->graph) cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
-        b->graph_version = -1;
-        cudaGraph_t g = nullptr;
-        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = record_build(b, any32, emul, boys64);
-        const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-        if (rc != RCHEM_OK) {
-            if (g) cudaGraphDestroy(g);
-            return rc;
-        }
-        if (e != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "capturing the Fock build: %s", cudaGetErrorString(e));
-        const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (ei != cudaSuccess) return set_err(RCHEM_ERR_CUDA, "instantiating the Fock build: %s", cudaGetErrorString(ei));
-        b->graph_version = b->plan_version;
-        b->graph_emul = o.emulated;
-    }
+    const bool capturable = stream_capturable(b);
+    if (!capturable) CKR(record_build(b, any32, (o.emulated & RCHEM_JK_EMULATED) != 0, f32_boys_mode(o.emulated)));
+    else CKR(ensure_graph(b, any32, o.emulated));
     if (capturable) CK(cudaGraphLaunch(b->graph, b->stream));
     const cudaMemcpyKind out = o.where == RCHEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     CK(cudaMemcpyAsync(J, b->d_Jo, nn * sizeof(double), out, b->stream));
@@ -1687,11 +1692,13 @@ extern "C" int rchem_set_tile_shape(rchem_basis b, int cls, int prec, int ppl) {
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
     if (cls < 0 || cls >= RCHEM_NCLASS || prec < 0 || prec > 1)
         return set_err(RCHEM_ERR_INVALID, "class %d / precision %d out of range", cls, prec);
-    if (ppl < 0) return set_err(RCHEM_ERR_INVALID, "primitive quartets per lane %d", ppl);
-    if (ppl == 0 && !rchem_class_wc[cls])
+    // ppl > 0: one lane group per quartet; 0, -16, -8: the warp-cooperative
+    // kernel with 32, 16 or 8 lanes per quartet
+    if (ppl < 0 && ppl != -16 && ppl != -8) return set_err(RCHEM_ERR_INVALID, "primitive quartets per lane %d", ppl);
+    if (ppl <= 0 && !rchem_class_wc[cls])
         return set_err(RCHEM_ERR_UNSUPPORTED, "class %d has no warp-cooperative kernel", cls);
-    b->wc[cls][prec] = ppl == 0;
-    b->ppl[cls][prec] = ppl == 0 ? kMinPrimPerLane : ppl;
+    b->wc[cls][prec] = ppl > 0 ? 0 : (ppl == 0 ? 32 : -ppl);
+    b->ppl[cls][prec] = ppl <= 0 ? kMinPrimPerLane : ppl;
     b->planned = false;  // the next build replans with this shape
     return RCHEM_OK;
 }
@@ -1719,6 +1726,26 @@ static int time_list(rchem_basis b, EriArgs a, int k, int prec, float *ms) {
     return RCHEM_OK;
 }
 
+// One whole Fock build under the current tile shapes, as rchem_jk_direct runs
+// it (the captured build, once to warm up, then timed): its device time in *ms.
+static int time_build(rchem_basis b, double tau, double tau32, int flags, float *ms) {
+    b->planned = false;
+    CKR(plan_tasks(b, tau, tau32));
+    bool any32 = false;
+    for (int k = 0; k < RCHEM_NCLASS; ++k) any32 |= b->task_cnt[k][1] > 0;
+    const bool capturable = stream_capturable(b);
+    if (capturable) CKR(ensure_graph(b, any32, flags));
+    for (int rep = 0; rep < 2; ++rep) {
+        CK(cudaEventRecord(b->ev_t0, b->stream));
+        if (capturable) CK(cudaGraphLaunch(b->graph, b->stream));
+        else CKR(record_build(b, any32, (flags & RCHEM_JK_EMULATED) != 0, f32_boys_mode(flags)));
+        CK(cudaEventRecord(b->ev_t1, b->stream));
+        CK(cudaEventSynchronize(b->ev_t1));
+    }
+    CK(cudaEventElapsedTime(ms, b->ev_t0, b->ev_t1));
+    return RCHEM_OK;
+}
+
 extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *chosen) {
     NvtxRange nv("rchem_autotune");
     if (!b) return set_err(RCHEM_ERR_INVALID, "null handle");
@@ -1730,25 +1757,27 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
     const double tau32 = (o.fp32_tau > 0.0) ? o.fp32_tau : 0.0;
     static const int cand[] = {4, 8, 16, 32, 64, 1 << 30};
     const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
-    float best_ms[RCHEM_NCLASS][2];
-    int best[RCHEM_NCLASS][2], best_wc[RCHEM_NCLASS][2];
+    float best_ms[RCHEM_NCLASS][2], cls_ms[RCHEM_NCLASS][2];
+    int best[RCHEM_NCLASS][2], best_wc[RCHEM_NCLASS][2], cls_ppl[RCHEM_NCLASS][2];
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
-            best_ms[k][p] = 1e30f;
-            best[k][p] = kMinPrimPerLane;
+            best_ms[k][p] = cls_ms[k][p] = 1e30f;
+            best[k][p] = cls_ppl[k][p] = kMinPrimPerLane;
             best_wc[k][p] = 0;
         }
     const size_t nn = (size_t)b->packed;
     CK(cudaMemsetAsync(b->d_D, 0, nn * sizeof(double), b->stream));
     CK(cudaMemsetAsync(b->d_D32, 0, nn * sizeof(float), b->stream));
     CK(cudaMemsetAsync(b->d_Ddf, 0, nn * sizeof(float2), b->stream));
-    // candidates: every lanes-per-quartet shape, then (c == ncand) the
-    // warp-cooperative kernel of the large classes
-    for (int c = 0; c <= ncand; ++c) {
-        const bool wc = c == ncand;
+    // candidates: every lanes-per-quartet shape, then (c >= ncand) the
+    // warp-cooperative kernel of the large classes with 32, 16 and 8 lanes per quartet
+    static const int wc_lanes[] = {32, 16, 8};
+    for (int c = 0; c < ncand + 3; ++c) {
+        const bool wc = c >= ncand;
+        const int ql = wc ? wc_lanes[c - ncand] : 0;
         for (int k = 0; k < RCHEM_NCLASS; ++k) {
             b->ppl[k][0] = b->ppl[k][1] = wc ? kMinPrimPerLane : cand[c];
-            b->wc[k][0] = b->wc[k][1] = wc ? rchem_class_wc[k] : 0;
+            b->wc[k][0] = b->wc[k][1] = rchem_class_wc[k] ? ql : 0;
         }
         b->planned = false;
         CKR(plan_tasks(b, tau, tau32));
@@ -1771,16 +1800,77 @@ extern "C" int rchem_autotune(rchem_basis b, const rchem_jk_opts *opts, int *cho
                 if (ms < best_ms[k][p]) {
                     best_ms[k][p] = ms;
                     best[k][p] = wc ? kMinPrimPerLane : cand[c];
-                    best_wc[k][p] = wc ? 1 : 0;
+                    best_wc[k][p] = ql;
+                }
+                if (!wc && ms < cls_ms[k][p]) {
+                    cls_ms[k][p] = ms;
+                    cls_ppl[k][p] = cand[c];
                 }
             }
     }
     for (int k = 0; k < RCHEM_NCLASS; ++k)
         for (int p = 0; p < 2; ++p) {
+            if (rchem_class_wc_only[k] && best_wc[k][p] == 0) {  // its one-lane-group shapes run 32 lanes per quartet
+                best[k][p] = kMinPrimPerLane;
+                best_wc[k][p] = 32;
+            }
             b->ppl[k][p] = best[k][p];
             b->wc[k][p] = best_wc[k][p];
-            if (chosen) chosen[2 * k + p] = best_wc[k][p] ? 0 : best[k][p];
         }
+    // In a build the class lists run concurrently, and a list's time alone
+    // misjudges its cost there: a warp-cooperative kernel's shared memory takes
+    // L1 from the kernels co-resident on its SMs (the (H2O)32 6-31G*-shaped
+    // build: its (dd|ds) list with 8 lanes per quartet ran 9 % faster alone
+    // than with one lane group per quartet, and made the build 11 % slower).
+    // So each large-class list, the longest first, takes the shape of the
+    // fastest whole build among its candidates (its best one-lane-group shape
+    // and the warp-cooperative kernel with 32, 16, 8 lanes per quartet), the
+    // other lists as chosen so far.
+    struct Ref {
+        int k, p;
+        float ms;
+    };
+    std::vector<Ref> refs;
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p)
+            if (rchem_class_wc[k] && b->task_cnt[k][p] > 0) refs.push_back(Ref{k, p, best_ms[k][p]});
+    std::stable_sort(refs.begin(), refs.end(), [](const Ref &x, const Ref &y) { return x.ms > y.ms; });
+    float cur = 0.f;
+    if (!refs.empty()) CKR(time_build(b, tau, tau32, o.emulated, &cur));
+    for (const Ref &r : refs) {
+        const int k = r.k, p = r.p;
+        int opt_ppl[4], opt_wc[4], nopt = 0;
+        if (!rchem_class_wc_only[k]) {
+            opt_ppl[nopt] = cls_ppl[k][p];
+            opt_wc[nopt++] = 0;
+        }
+        for (int i = 0; i < 3; ++i) {
+            opt_ppl[nopt] = kMinPrimPerLane;
+            opt_wc[nopt++] = wc_lanes[i];
+        }
+        int win_ppl = b->ppl[k][p], win_wc = b->wc[k][p];
+        for (int i = 0; i < nopt; ++i) {
+            if (opt_wc[i] == win_wc && (opt_wc[i] != 0 || opt_ppl[i] == win_ppl)) continue;  // the current shape
+            const int keep_ppl = b->ppl[k][p], keep_wc = b->wc[k][p];
+            b->ppl[k][p] = opt_ppl[i];
+            b->wc[k][p] = opt_wc[i];
+            float ms = 0.f;
+            CKR(time_build(b, tau, tau32, o.emulated, &ms));
+            if (ms < cur) {
+                cur = ms;
+                win_ppl = opt_ppl[i];
+                win_wc = opt_wc[i];
+            } else {
+                b->ppl[k][p] = keep_ppl;
+                b->wc[k][p] = keep_wc;
+            }
+        }
+        b->ppl[k][p] = win_ppl;
+        b->wc[k][p] = win_wc;
+    }
+    for (int k = 0; k < RCHEM_NCLASS; ++k)
+        for (int p = 0; p < 2; ++p)
+            if (chosen) chosen[2 * k + p] = b->wc[k][p] ? (b->wc[k][p] == 32 ? 0 : -b->wc[k][p]) : b->ppl[k][p];
     b->planned = false;
     CKR(plan_tasks(b, tau, tau32));
     return RCHEM_OK;

@@ -101,7 +101,8 @@ struct EriArgs {
     double *K;
     double *eri;           // ERI-tensor epilogue output: dense nbf^4, or packed (eri_packed)
     int eri_packed;        // 1: one value per unique integral at the 8-fold index (rchem_eri_pack8)
-    int wc;                // J/K epilogue of a large class: 1 = warp-cooperative kernel, 0 = one lane group per quartet
+    int wc;                // J/K epilogue of a large class: the warp-cooperative kernel with 32, 16 or 8
+                           // lanes per quartet, 0 = one lane group per quartet
     int f32_boys64;        // FP32 quartets' Boys function: 0 FP32, 1 FP64 (values and recursion),
                            // 2 FP32 table / asymptotic values with the recursion in FP64
     // per (bra, ket) primitive-pair exponent: 1/sqrt(p+q), pq/(p+q), q/(p+q),

@@ -140,7 +140,7 @@ def test_h2o32_sampled_elements_vs_oracle(gpu, h2o32_oracle, emulated, fp32_tau,
         fl = {"fp32_boys64": bmode == "boys64", "fp32_rec64": bmode == "rec64"}
         chosen = b.autotune(1e-12, fp32_tau, emulated=emulated, **fl)
         if not emulated and fp32_tau == 0.0:
-            assert any(v == 0 for (k, p), v in chosen.items() if p == 0)  # some list runs warp-cooperatively
+            assert any(v <= 0 for (k, p), v in chosen.items() if p == 0)  # some list runs warp-cooperatively
         D = torch.from_numpy(o["D"]).cuda()
         J, K = torch.empty_like(D), torch.empty_like(D)
         rc.JK_direct(J, K, b, D, fp32_tau=fp32_tau, emulated=emulated, **fl)

@@ -335,7 +335,7 @@ def test_autotune_keeps_results(gpu):
         J0, K0 = np.zeros((104, 104)), np.zeros((104, 104))
         rc.JK_direct(J0, K0, b, D)
         chosen = b.autotune()
-        assert len(chosen) == 42 and all(v == 0 or v >= 4 for v in chosen.values())
+        assert len(chosen) == 42 and all(v in (0, -16, -8) or v >= 4 for v in chosen.values())
         J1, K1 = np.zeros((104, 104)), np.zeros((104, 104))
         rc.JK_direct(J1, K1, b, D)
         np.testing.assert_allclose(J1, J0, atol=1e-12, rtol=0)
@@ -416,9 +416,11 @@ def test_emulated_fp64_device_and_batch(gpu):
 
 
 @pytest.mark.parametrize("name", ["6-31gss-fit", "6-31gs-fit"])
-def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
-    """The warp-cooperative J/K kernel of the large classes (total L >= 4), forced
-    on every such list, FP64, emulated FP64 and FP32, against the 8-fold oracle."""
+@pytest.mark.parametrize("shape", [0, -16, -8])
+def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name, shape):
+    """The warp-cooperative J/K kernel of the large classes (total L >= 4) with
+    32, 16 and 8 lanes per quartet (1, 2, 4 quartets per warp), forced on every
+    such list, FP64, emulated FP64 and FP32, against the 8-fold oracle."""
     import rchem_gb300 as rc
 
     O = oracle_mod
@@ -433,8 +435,8 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
         wc = [k for k, c in enumerate(b.class_stats()) if sum(c["class"]) >= 4]
         assert len(wc) == 13
         for k in wc:
-            b.set_tile_shape(k, 0, 0)
-            b.set_tile_shape(k, 1, 0)
+            b.set_tile_shape(k, 0, shape)
+            b.set_tile_shape(k, 1, shape)
         rc.JK_direct(J, K, b, D, schwarz_tau=0.0)
         assert np.abs(J - Jr).max() < 1e-12
         assert np.abs(K - Kr).max() < 1e-12
@@ -445,7 +447,9 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name):
         rc.JK_direct(Jm, Km, b, D, schwarz_tau=0.0, fp32_tau=1e30)  # every quartet in FP32
         assert np.abs(Jm - Jr).max() < 1e-5 and np.abs(Km - Kr).max() < 1e-5
         with pytest.raises(rc.RchemError):
-            b.set_tile_shape(0, 0, 0)  # (ss|ss) has no warp-cooperative kernel
+            b.set_tile_shape(0, 0, shape)  # (ss|ss) has no warp-cooperative kernel
+        with pytest.raises(rc.RchemError):
+            b.set_tile_shape(wc[0], 0, -4)  # no 4-lane form
 
 
 def test_exponent_table_on_and_off_vs_oracle(gpu, oracle_mod):
@@ -465,11 +469,11 @@ def test_exponent_table_on_and_off_vs_oracle(gpu, oracle_mod):
     with rc.Basis(Z, R, name) as b:
         n = b.nbf
         out = {}
-        for wc in (False, True):
-            if wc:
+        for wc in (None, 0, -8):
+            if wc is not None:
                 for k, c in enumerate(b.class_stats()):
                     if sum(c["class"]) >= 4:
-                        b.set_tile_shape(k, 0, 0)
+                        b.set_tile_shape(k, 0, wc)
             for emulated in (False, True):
                 for on in (True, False):
                     b.set_exponent_table(on)
