@@ -424,6 +424,9 @@ def other_targets(rc, torch):
            "scf_driver": "rchem_rhf (the whole SCF loop in the library)"}
     for tag, tau32, emul in (("fp64", 0.0, False), ("mixed", 1e-6, False), ("emulated_mixed", 1e-6, True)):
         bb.autotune(SCHWARZ_TAU, tau32, emulated=emul)
+        # warm-up of this form's gradient (its work plan and graphs are built on first use)
+        rc.batch.gradient_batch(bb, rc.batch.rhf_native(bb, max_iter=2, fp32_tau=tau32, emulated=emul),
+                                fp32_tau=tau32, emulated=emul)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r = rc.batch.rhf_native(bb, thresh_e=1e-10, fp32_tau=tau32, emulated=emul)

@@ -59,19 +59,22 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == key:
         return LIB
     _generate()
-    srcs = [os.path.join(CSRC, f) for f in ("rchem_gpu.cu", "peak.cu", "grad_sp_f64.cu", "grad_sp_f32.cu",
+    srcs = [os.path.join(CSRC, f) for f in ("rchem_gpu.cu", "peak.cu", "grad_sp_f64.cu", "grad_pppp_f64.cu", "grad_sp_f32.cu",
                                             "grad_sp_df64.cu", "grad_sp_df64b.cu", "grad_sd_f64.cu",
                                             "grad_sd_f32.cu", "onee_cls.cu")]
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("eri_") and f.endswith(".cu"))
     nvcc = _nvcc()
 
-    headers = [os.path.join(CSRC, f) for f in ("eri_kernel.cuh", "boys.cuh", "df64.cuh", "rchem_types.h")]
+    headers = [os.path.join(CSRC, f) for f in ("eri_kernel.cuh", "boys.cuh", "df64.cuh", "pq_table.cuh", "rchem_types.h")]
+
+    def tag(src):  # the class of a generated translation unit (eri_<tag>.cu, eri_<tag>_cls.cu)
+        return os.path.basename(src)[4:8]
 
     def deps(src):
         base = os.path.basename(src)
         if base.startswith("eri_") and src.startswith(GEN):
-            prog = os.path.join(GEN, base.replace("eri_", "eri_prog_").replace(".cu", ".inc"))
-            return ([src, os.path.join(GEN, base.replace("eri_", "eri_class_").replace(".cu", ".inc"))] +
+            prog = os.path.join(GEN, "eri_prog_%s.inc" % tag(src))
+            return ([src, os.path.join(GEN, "eri_class_%s.inc" % tag(src))] +
                     ([prog] if os.path.exists(prog) else []) + headers)
         if base == "peak.cu":
             return [src, os.path.join(INCLUDE, "rchem_bench.h")]
@@ -79,11 +82,18 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
-        okey = _digest(deps(src), (ARCH, NVFLAGS, nvcc))
+        # ptxas -O1 for the one-lane-group kernels of the classes of total
+        # angular momentum 6 and 7 (csrc/gen_eri.py SPLIT_L) and the FP64
+        # (pp|pp) gradient kernel: it keeps their values in registers (255 of
+        # them, 2-8 KB of local memory per thread) where -O3 gives the L = 6
+        # ERI kernels 32 registers and ~19 KB (twice as slow) and the gradient
+        # one ~30 KB, and takes minutes over the L = 7 one
+        extra = ["-Xptxas", "-O1"] if src.endswith(("_cls.cu", "grad_pppp_f64.cu")) else []
+        okey = _digest(deps(src), (ARCH, NVFLAGS, extra, nvcc))
         hfile = obj + ".key"
         if not force and os.path.exists(obj) and os.path.exists(hfile) and open(hfile).read() == okey:
             return obj
-        cmd = [nvcc, *ARCH, *NVFLAGS, "-I", CSRC, "-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *NVFLAGS, *extra, "-I", CSRC, "-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, r.stdout[-4000:], r.stderr[-8000:]))
@@ -94,8 +104,11 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         return obj
 
     # biggest classes first so the long compiles start early
-    srcs.sort(key=lambda s: -os.path.getsize(s.replace("eri_", "eri_class_").replace(".cu", ".inc"))
-              if os.path.exists(s.replace("eri_", "eri_class_").replace(".cu", ".inc")) else 0)
+    def class_size(s):
+        inc = os.path.join(GEN, "eri_class_%s.inc" % tag(s))
+        return os.path.getsize(inc) if s.startswith(GEN) and os.path.exists(inc) else 0
+
+    srcs.sort(key=lambda s: -class_size(s))
     with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"

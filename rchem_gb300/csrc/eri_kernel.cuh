@@ -797,12 +797,37 @@ void launch_wc_jk(const EriArgs &a, cudaStream_t s) {
     else launch_wc<LA, LB, LC, LD, R, EPI_JK, 32>(a, s);
 }
 
+// The one-lane-group-per-quartet kernel of a class list.  The classes of total
+// angular momentum 6 build it in a translation unit of its own (compiled with
+// ptxas -O1, see build.py) and reach it through launch_eri_class's ext.
 template <int LA, int LB, int LC, int LD>
-void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
+void launch_eri_cls_only(const EriArgs &a, int prec, int epi, cudaStream_t s) {
+    if constexpr (!EriClass<LA, LB, LC, LD>::WC_ONLY) {
+        if (a.ntasks <= 0) return;
+        const int threads = 128;
+        const long long nthreads = (long long)a.ntasks * 32;
+        const int blocks = (int)((nthreads + threads - 1) / threads);
+        if (epi == EPI_JK) {
+            if (prec == 1) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
+            else if constexpr (LA + LB + LC + LD <= 4) {
+                if (prec == 2) eri_class_kernel<LA, LB, LC, LD, df64, EPI_JK><<<blocks, threads, 0, s>>>(a);
+                else eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+            } else {
+                eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
+            }
+        } else if (epi == EPI_STORE) {
+            eri_class_kernel<LA, LB, LC, LD, double, EPI_STORE><<<blocks, threads, 0, s>>>(a);
+        } else if constexpr (LA == LC && LB == LD) {
+            eri_class_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<blocks, threads, 0, s>>>(a);
+        }
+    }
+}
+
+using EriClsLaunch = void (*)(const EriArgs &, int, int, cudaStream_t);
+
+template <int LA, int LB, int LC, int LD, bool EXT_CLS = false>
+void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s, EriClsLaunch ext = nullptr) {
     if (a.ntasks <= 0) return;
-    const int threads = 128;
-    const long long nthreads = (long long)a.ntasks * 32;
-    const int blocks = (int)((nthreads + threads - 1) / threads);
     if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
         // the largest classes exist only as warp-cooperative kernels (one quartet per
         // task in every plan); their straight-line code would take minutes to compile
@@ -823,19 +848,6 @@ void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s) {
             return;
         }
     }
-    if constexpr (!EriClass<LA, LB, LC, LD>::WC_ONLY) {
-    if (epi == EPI_JK) {
-        if (prec == 1) eri_class_kernel<LA, LB, LC, LD, float, EPI_JK><<<blocks, threads, 0, s>>>(a);
-        else if constexpr (LA + LB + LC + LD <= 4) {
-            if (prec == 2) eri_class_kernel<LA, LB, LC, LD, df64, EPI_JK><<<blocks, threads, 0, s>>>(a);
-            else eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
-        } else {
-            eri_class_kernel<LA, LB, LC, LD, double, EPI_JK><<<blocks, threads, 0, s>>>(a);
-        }
-    } else if (epi == EPI_STORE) {
-        eri_class_kernel<LA, LB, LC, LD, double, EPI_STORE><<<blocks, threads, 0, s>>>(a);
-    } else if constexpr (LA == LC && LB == LD) {
-        eri_class_kernel<LA, LB, LC, LD, double, EPI_DIAG><<<blocks, threads, 0, s>>>(a);
-    }
-    }
+    if constexpr (EXT_CLS) ext(a, prec, epi, s);
+    else launch_eri_cls_only<LA, LB, LC, LD>(a, prec, epi, s);
 }

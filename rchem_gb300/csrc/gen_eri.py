@@ -420,7 +420,14 @@ def setup_ops(la, lb, lc, ld):
 # 32 lanes taking the independent terms of a level.  The DAG is the same one
 # the straight-line code follows (same direction choices, same terms).
 WC_MINL = 4  # classes with l_a+l_b+l_c+l_d >= WC_MINL get a program
-WC_ONLY_MINL = 7  # ... and from here on have no one-lane-group-per-quartet kernel at all
+WC_ONLY_MINL = 8  # ... and from here on have no one-lane-group-per-quartet kernel at all
+# Total angular momenta whose one-lane-group kernel is a translation unit of
+# its own, compiled with ptxas -O1: at -O3 the L = 6 kernels got 32 registers
+# and ~19 KB of local memory per thread, at -O1 255 registers and ~3 KB, and
+# ran twice as fast, and the L = 7 one ((dd|dp)) compiles in under a minute
+# instead of minutes; the other kernels of these classes (warp-cooperative)
+# stay at -O3, where they are faster.
+SPLIT_L = (6, 7)
 
 
 def _levels(depth, order, key):
@@ -698,17 +705,33 @@ def main(outdir):
         with open(os.path.join(outdir, "eri_class_%s.inc" % tag), "w") as f:
             f.write("\n".join(lines) + "\n")
         table.append((la, lb, lc, ld, prim_flops, contr_flops, NA * NB * NC * ND))
-    # one translation unit per class (compiled in parallel)
+    # one translation unit per class (compiled in parallel); the classes of
+    # total angular momentum in SPLIT_L put their one-lane-group kernel in a
+    # second one, eri_<tag>_cls.cu, which build.py compiles with ptxas -O1
     for (la, lb, lc, ld) in cls:
         tag = "%d%d%d%d" % (la, lb, lc, ld)
+        split = la + lb + lc + ld in SPLIT_L
         with open(os.path.join(outdir, "eri_%s.cu" % tag), "w") as f:
             f.write("// generated by gen_eri.py -- do not edit\n")
             f.write('#include "../eri_kernel.cuh"\n#include "eri_class_%s.inc"\n' % tag)
             if la + lb + lc + ld >= WC_MINL:
                 f.write('#include "eri_prog_%s.inc"\n' % tag)
+            if split:
+                f.write("void rchem_launch_eri_cls_%s(const EriArgs &a, int prec, int epi, cudaStream_t s);"
+                        "  // eri_%s_cls.cu\n" % (tag, tag))
             f.write("void rchem_launch_eri_%s(const EriArgs &a, int fp32, int epi, cudaStream_t s) {\n" % tag)
-            f.write("    launch_eri_class<%d, %d, %d, %d>(a, fp32, epi, s);\n}\n" % (la, lb, lc, ld))
+            if split:
+                f.write("    launch_eri_class<%d, %d, %d, %d, true>(a, fp32, epi, s, rchem_launch_eri_cls_%s);\n}\n"
+                        % (la, lb, lc, ld, tag))
+            else:
+                f.write("    launch_eri_class<%d, %d, %d, %d>(a, fp32, epi, s);\n}\n" % (la, lb, lc, ld))
             f.write("cudaError_t rchem_prepare_eri_%s() { return prepare_eri_class<%d, %d, %d, %d>(); }\n" % (tag, la, lb, lc, ld))
+        if split:
+            with open(os.path.join(outdir, "eri_%s_cls.cu" % tag), "w") as f:
+                f.write("// generated by gen_eri.py -- do not edit\n")
+                f.write('#include "../eri_kernel.cuh"\n#include "eri_class_%s.inc"\n' % tag)
+                f.write("void rchem_launch_eri_cls_%s(const EriArgs &a, int prec, int epi, cudaStream_t s) {\n" % tag)
+                f.write("    launch_eri_cls_only<%d, %d, %d, %d>(a, prec, epi, s);\n}\n" % (la, lb, lc, ld))
     with open(os.path.join(outdir, "eri_dispatch.h"), "w") as f:
         f.write("// generated by gen_eri.py -- do not edit\n#pragma once\n#include <cuda_runtime.h>\n")
         f.write('#include "../rchem_types.h"\n')

@@ -193,6 +193,7 @@ bool rchem_grad_sp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t s
 bool rchem_grad_sp_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sp_df64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sd_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
+bool rchem_grad_pppp_f64(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_sd_f32(int k, const GradArgs &g, unsigned blocks, cudaStream_t st);
 bool rchem_grad_wc_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
 void rchem_grad_rt_f32(const GradArgs &g, unsigned blocks, cudaStream_t st);
@@ -1045,8 +1046,11 @@ static int create_impl(rchem_basis *out, int ngeom, const int *geom_natoms, int 
     rchem_basis b = new rchem_basis_s();
     b->dev = dev;
     for (int k = 0; k < RCHEM_NCLASS; ++k) {
+        // until rchem_autotune chooses: the warp-cooperative kernel for (dd|dp) and
+        // up, one lane group per quartet below
+        const int L = rchem_class_l[k][0] + rchem_class_l[k][1] + rchem_class_l[k][2] + rchem_class_l[k][3];
         b->ppl[k][0] = b->ppl[k][1] = kMinPrimPerLane;
-        b->wc[k][0] = b->wc[k][1] = 0;
+        b->wc[k][0] = b->wc[k][1] = (rchem_class_wc[k] && L >= 7) ? 32 : 0;
     }
     b->natoms = natoms;
     b->Z.assign(atomnos, atomnos + natoms);
@@ -1640,7 +1644,8 @@ extern "C" int rchem_gradient(rchem_basis b, const double *D, const double *W, d
                 const int cls = k / 2;
                 const bool ok = (k & 1) ? (rchem_grad_sp_f32(cls, g, blocks, st) || rchem_grad_sd_f32(cls, g, blocks, st))
                                         : (((o.emulated & RCHEM_JK_EMULATED) && rchem_grad_sp_df64(cls, g, blocks, st)) ||
-                                           rchem_grad_sp_f64(cls, g, blocks, st) || rchem_grad_sd_f64(cls, g, blocks, st));
+                                           rchem_grad_sp_f64(cls, g, blocks, st) || rchem_grad_pppp_f64(cls, g, blocks, st) ||
+                                           rchem_grad_sd_f64(cls, g, blocks, st));
                 if (!ok) return set_err(RCHEM_ERR_UNSUPPORTED, "gradient list %d has no specialised kernel", k);
                 CK(cudaGetLastError());
                 continue;

@@ -416,11 +416,13 @@ def test_emulated_fp64_device_and_batch(gpu):
 
 
 @pytest.mark.parametrize("name", ["6-31gss-fit", "6-31gs-fit"])
-@pytest.mark.parametrize("shape", [0, -16, -8])
+@pytest.mark.parametrize("shape", [0, -16, -8, 16])
 def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name, shape):
     """The warp-cooperative J/K kernel of the large classes (total L >= 4) with
-    32, 16 and 8 lanes per quartet (1, 2, 4 quartets per warp), forced on every
-    such list, FP64, emulated FP64 and FP32, against the 8-fold oracle."""
+    32, 16 and 8 lanes per quartet (1, 2, 4 quartets per warp), or their
+    one-lane-group kernel (16 primitive quartets per lane; (dd|dd) has none and
+    stays warp-cooperative), forced on every such list, FP64, emulated FP64 and
+    FP32, against the 8-fold oracle."""
     import rchem_gb300 as rc
 
     O = oracle_mod
@@ -446,8 +448,9 @@ def test_warp_cooperative_classes_vs_oracle(gpu, oracle_mod, name, shape):
         Jm, Km = np.zeros((n, n)), np.zeros((n, n))
         rc.JK_direct(Jm, Km, b, D, schwarz_tau=0.0, fp32_tau=1e30)  # every quartet in FP32
         assert np.abs(Jm - Jr).max() < 1e-5 and np.abs(Km - Kr).max() < 1e-5
-        with pytest.raises(rc.RchemError):
-            b.set_tile_shape(0, 0, shape)  # (ss|ss) has no warp-cooperative kernel
+        if shape <= 0:
+            with pytest.raises(rc.RchemError):
+                b.set_tile_shape(0, 0, shape)  # (ss|ss) has no warp-cooperative kernel
         with pytest.raises(rc.RchemError):
             b.set_tile_shape(wc[0], 0, -4)  # no 4-lane form
 
