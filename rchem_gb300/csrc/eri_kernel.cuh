@@ -829,8 +829,9 @@ template <int LA, int LB, int LC, int LD, bool EXT_CLS = false>
 void launch_eri_class(const EriArgs &a, int prec, int epi, cudaStream_t s, EriClsLaunch ext = nullptr) {
     if (a.ntasks <= 0) return;
     if constexpr (EriClass<LA, LB, LC, LD>::WC_ONLY) {
-        // the largest classes exist only as warp-cooperative kernels (one quartet per
-        // task in every plan); their straight-line code would take minutes to compile
+        // the largest class, (dd|dd), exists only as warp-cooperative kernels (one
+        // quartet per task in every plan); its straight-line code would take
+        // minutes to compile
         if (epi == EPI_STORE) {
             launch_wc<LA, LB, LC, LD, double, EPI_STORE, 32>(a, s);
             return;
