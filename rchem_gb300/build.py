@@ -50,6 +50,17 @@ def _digest(paths, extra):
     return h.hexdigest()
 
 
+def ptxas_extra(src: str) -> list:
+    """Extra nvcc flags of one translation unit: ptxas -O1 for the one-lane-group
+    kernels of the classes of total angular momentum 6 and 7 (csrc/gen_eri.py
+    SPLIT_L, generated as eri_<class>_cls.cu) and the FP64 (pp|pp) gradient
+    kernel.  At -O1 ptxas keeps their values in registers (255 of them, 2-8 KB
+    of local memory per thread) where -O3 gives the L = 6 ERI kernels 32
+    registers and ~19 KB (twice as slow) and the gradient one ~30 KB, and takes
+    minutes over the L = 7 one."""
+    return ["-Xptxas", "-O1"] if src.endswith(("_cls.cu", "grad_pppp_f64.cu")) else []
+
+
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
     hand = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h", ".py"))]
@@ -82,13 +93,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
-        # ptxas -O1 for the one-lane-group kernels of the classes of total
-        # angular momentum 6 and 7 (csrc/gen_eri.py SPLIT_L) and the FP64
-        # (pp|pp) gradient kernel: it keeps their values in registers (255 of
-        # them, 2-8 KB of local memory per thread) where -O3 gives the L = 6
-        # ERI kernels 32 registers and ~19 KB (twice as slow) and the gradient
-        # one ~30 KB, and takes minutes over the L = 7 one
-        extra = ["-Xptxas", "-O1"] if src.endswith(("_cls.cu", "grad_pppp_f64.cu")) else []
+        extra = ptxas_extra(src)
         okey = _digest(deps(src), (ARCH, NVFLAGS, extra, nvcc))
         hfile = obj + ".key"
         if not force and os.path.exists(obj) and os.path.exists(hfile) and open(hfile).read() == okey:

@@ -125,3 +125,38 @@ def test_boys_evaluator(hostlib, port):
             ex = port.boys_exact(m, x)
             assert abs(hostlib.host_boys(m, x, 0) - ex) <= 4e-15 * ex, (m, x)
             assert abs(hostlib.host_boys(m, x, 1) - ex) <= 2e-6 * ex, (m, x)
+
+
+def test_generated_translation_units(tmp_path):
+    """One translation unit per class; the classes of total angular momentum 6
+    and 7 put their one-lane-group kernel in a second one (eri_<class>_cls.cu),
+    which the build compiles with ptxas -O1 and the first reaches through an
+    external launcher; (dd|dd) alone is warp-cooperative only."""
+    import importlib.util
+    import re
+
+    spec = importlib.util.spec_from_file_location("gen_eri_tu", os.path.join(CSRC, "gen_eri.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.main(str(tmp_path))
+    from rchem_gb300 import build as B
+
+    for c in CLASSES:
+        tag = "%d%d%d%d" % c
+        main = (tmp_path / ("eri_%s.cu" % tag)).read_text()
+        cls_tu = tmp_path / ("eri_%s_cls.cu" % tag)
+        split = sum(c) in (6, 7)
+        assert cls_tu.exists() == split, c
+        assert B.ptxas_extra(str(tmp_path / ("eri_%s.cu" % tag))) == []
+        if split:
+            assert "launch_eri_class<%d, %d, %d, %d, true>(a, fp32, epi, s, rchem_launch_eri_cls_%s)" % (c + (tag,)) \
+                in main
+            assert "launch_eri_cls_only<%d, %d, %d, %d>(a, prec, epi, s)" % c in cls_tu.read_text()
+            assert B.ptxas_extra(str(cls_tu)) == ["-Xptxas", "-O1"]
+        else:
+            assert "launch_eri_class<%d, %d, %d, %d>(a, fp32, epi, s)" % c in main
+        inc = (tmp_path / ("eri_class_%s.inc" % tag)).read_text()
+        wc_only = re.search(r"WC_ONLY = (true|false)", inc).group(1) == "true"
+        assert wc_only == (c == (2, 2, 2, 2)), c
+    assert B.ptxas_extra(os.path.join(CSRC, "grad_pppp_f64.cu")) == ["-Xptxas", "-O1"]
+    assert B.ptxas_extra(os.path.join(CSRC, "grad_sp_f64.cu")) == []
